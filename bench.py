@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Headline benchmark: FP64 cell-updates/s of the two-layer time step on the
+2048 x 2048 second-order (MUSCL + TVD-RK2) spherical fjord (0.0002 degree
+cells at 60 N, 2e7 m^3 slide), synthetic seeded input.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one full time step of the whole grid (both RK stages).  Timed on
+the device with CUDA events around exactly K steps (one CUDA graph launch per
+16 steps), barrier + synchronize on both sides, max over ranks.  Inputs are
+larger than L2 (state + accumulators + slopes ~ 1 GB), so no flush is needed.
+N > 1 runs independent replicas, one per GPU (the time step has no
+cross-replica exchange; the reference's MPI row decomposition is out of scope),
+so scaling is weak and `value` sums all ranks' cell-updates.
+
+--impl reference times the reference scheme on the host cores instead: the
+FP64 CPU restatement in oracle/ (the reference's own CPU-side code has no
+time step -- its solver exists only as CUDA kernels), all host threads, the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 cell-updates/s at 2048^2"
+UNIT = "cell-updates/s"
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=48)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=2048, help="grid size (n x n); the headline is 2048")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, local, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def workload(n):
+    from landslidehysea_gb300 import scenarios
+    sc = scenarios.fjord(n=n)
+    return sc
+
+
+def config_dict(sc, n, extra=None):
+    d = {"workload": f"fjord{n}x{n}_order2_spherical", "grid": [n, n], "cells": n * n, "order": 2,
+         "coords": "spherical", "cell_deg": 0.0002, "lat_c": 60.0, "slide_m3": 2e7, "seed": 0,
+         "wet_fraction": round(sc.meta["wet_fraction"], 4), "cfl": sc.params.cfl,
+         "l2": "inputs larger than L2 (state+accumulators+slopes ~1 GB)", "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        exe = shutil.which("nvidia-smi")
+        if exe:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen([exe, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def algorithmic_bytes_per_launch(kernel_index, order, cells):
+    """Bytes one launch of kernel `kernel_index` of a step must move (8-byte
+    doubles), from the kernel's dataflow: each edge pass touches every cell
+    once, reading its state (7) and, at second order, the 7 slopes of the
+    pass direction, plus a read-modify-write of its 7 accumulators (the first
+    pass only writes them)."""
+    d = 8
+    if order == 2:
+        names = ["recon", "edge_h0", "edge_h1", "edge_v0", "edge_v1", "volume1",
+                 "recon", "edge_h0", "edge_h1", "edge_v0", "edge_v1", "volume2", "clock"]
+        per = {"recon": 7 + 14, "edge_h0": 14 + 7, "edge_h1": 14 + 14, "edge_v0": 14 + 14, "edge_v1": 14 + 14,
+               "volume1": 7 + 7 + 4 + 6, "volume2": 6 + 1 + 7 + 4 + 6 + 6, "clock": 0}
+    else:
+        names = ["edge_h0", "edge_h1", "edge_v0", "edge_v1", "volume", "clock"]
+        per = {"edge_h0": 7 + 7, "edge_h1": 7 + 14, "edge_v0": 7 + 14, "edge_v1": 7 + 14, "volume": 7 + 7 + 6,
+               "clock": 0}
+    nm = names[kernel_index]
+    return nm, per[nm] * d * cells
+
+
+def cpu_baseline_sample(sc, steps):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    threads = pyoracle.set_threads(0)
+    arrs = pyoracle.state_arrays(sc.state)
+    dt0 = pyoracle.initial_dt(sc.params, arrs)
+    t0 = time.perf_counter()
+    pyoracle.run(sc.params, arrs, steps, dt=dt0)
+    el = time.perf_counter() - t0
+    return sc.nx * sc.ny * steps / el, threads, el
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    sc = workload(args.n)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    threads = pyoracle.set_threads(0)
+    arrs = pyoracle.state_arrays(sc.state)
+    dt = pyoracle.initial_dt(sc.params, arrs)
+    t = 0.0
+    steps = max(1, min(args.steps, 12))
+    warm = max(1, min(args.warmup, 3))
+    t, dt, _ = pyoracle.run(sc.params, arrs, warm, t=t, dt=dt)
+    t0 = time.perf_counter()
+    t, dt, _ = pyoracle.run(sc.params, arrs, steps, t=t, dt=dt)
+    el = time.perf_counter() - t0
+    value = sc.nx * sc.ny * steps / el
+    sample = f"{steps} full steps of the {args.n}^2 grid after {warm} warm-up steps"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(sc, args.n, {"runner": "FP64 CPU restatement of the reference scheme (oracle/)"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    dist = init_dist(world, local, "nccl")
+    torch.cuda.set_device(local)
+    from landslidehysea_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    if dist:
+        dist.barrier()
+    from landslidehysea_gb300._abi import VARS
+    from landslidehysea_gb300.solver import Solver, probe_fp64_peak
+
+    sc = workload(args.n)
+    cells = sc.nx * sc.ny
+    stream = torch.cuda.current_stream()
+    s = Solver(sc.params, device=local)
+    s.set_stream(stream.cuda_stream)
+    s.set_state(sc.state)
+    s.step(args.warmup)
+    s.synchronize()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    launches0 = s.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = s.launch_count() - launches0
+    s.synchronize()
+    t_sim, dt_next, nsteps = s.time()
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * cells * args.steps / (ms * 1e-3)
+
+    # per-kernel event timing of a few extra steps (dominant kernel for the roofline)
+    prof = [s.profile_step() for _ in range(3)]
+    nk = len(prof[0])
+    mean = [statistics.mean(p[k] for p in prof) for k in range(nk)]
+    order = sc.params.order
+    names_ms = {}
+    for k in range(nk):
+        nm, _ = algorithmic_bytes_per_launch(k, order, cells)
+        names_ms.setdefault(nm, []).append(mean[k])
+    dom_k = max(range(nk), key=lambda k: mean[k])
+    dom_name, dom_bytes = algorithmic_bytes_per_launch(dom_k, order, cells)
+    hbm, peak_kind = peaks()
+    achieved = dom_bytes / (mean[dom_k] * 1e-3) / 1e9
+    try:
+        fp64_peak = probe_fp64_peak(local)
+    except Exception:
+        fp64_peak = None
+    roofline = {"bound": "hbm", "kernel": f"k_edges ({dom_name})", "achieved": round(achieved, 2),
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": None,
+                "peak_kind": f"{peak_kind} hbm_gbs", "step_kernel_ms": {k: round(statistics.mean(v), 4)
+                                                                        for k, v in names_ms.items()},
+                "fp64_peak_gflops_measured": round(fp64_peak, 1) if fp64_peak else None,
+                "note": "FP64-pipe bound; see profiles/ for the FP64 instruction roofline"}
+    s.close()
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(sc, local, args, torch, np, VARS, Solver, dist)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, threads, el = cpu_baseline_sample(sc, 2)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"2 full steps of the {args.n}^2 grid ({el:.1f} s) with the FP64 oracle, all host threads"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config_dict(sc, args.n, {"sim_time_s": t_sim, "dt_s": dt_next}),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_e2e(sc, local, args, torch, np, VARS, Solver, dist):
+    """The same metric through the C ABI with HOST buffers: upload the state
+    from pinned host memory (lsh_set_state), then per step one lsh_step and a
+    blocking read of the step's result (t, dt: lsh_get_time, as the
+    reference reads dt back every step), then download the state
+    (lsh_get_state), all inside the timed region."""
+    cells = sc.nx * sc.ny
+    pinned = {}
+    for v in VARS:
+        t = torch.empty((sc.ny, sc.nx), dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = sc.state[v]
+        pinned[v] = t
+    host_in = {v: pinned[v].numpy() for v in VARS}
+    s = Solver(sc.params, device=local)
+    s.set_state(host_in)
+    s.step(2)
+    s.synchronize()
+    if dist:
+        dist.barrier()
+    steps = args.steps
+    t0 = time.perf_counter()
+    s.set_state(host_in)
+    for _ in range(steps):
+        s.step(1)
+        s.time()
+    out = s.get_state()
+    el = time.perf_counter() - t0
+    s.close()
+    if dist:
+        tt = torch.tensor([el], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        el = float(tt.item())
+    world = dist.get_world_size() if dist else 1
+    state_bytes = 7 * cells * 8
+    return {"value": world * cells * steps / el, "unit": UNIT, "h2d_bytes_per_step": state_bytes / steps,
+            "d2h_bytes_per_step": 64 + state_bytes / steps, "seconds": el,
+            "what": "lsh_set_state(pinned host) + K x (lsh_step(1) + lsh_get_time) + lsh_get_state"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

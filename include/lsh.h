@@ -1,0 +1,172 @@
+/*
+ * lsh.h -- C ABI of the GB300-native two-layer finite-volume time step
+ * (shallow water over a Savage-Hutter granular layer, LandSlide-HySEA scheme).
+ *
+ * Everything here is plain C: opaque context, plain pointers and sizes, int
+ * status codes.  No CUDA or torch types appear in any signature; streams are
+ * passed as `void*` (a cudaStream_t).
+ *
+ * Reference interface this replaces:
+ *   extern "C" int shallowWater(TDatoCluster*, float xmin, ..., int num_puntos_guardar)
+ *     src/GPU/ShallowWater.cu:125-131 (definition), src/GPU/main.cxx:12-18 (declaration)
+ *   extern "C" int comprobarSoporteCUDA()     src/GPU/ComprobarSoporteCUDA.cu:5
+ * The one-call compatibility entry point with the reference's exact argument
+ * list is declared in lsh_compat.h.  The functions below split that call into
+ * create / set-state / step / read-back so a host (C, C++, ctypes) can drive the
+ * time loop, keep the state resident in HBM and capture the loop in a CUDA graph.
+ *
+ * Grid convention (same as the reference): cell (i, j) has linear index
+ * j*nx + i, i = column (x, east), j = row (y).  Horizontal edge row y lies
+ * between rows y-1 and y; its normal points toward increasing j
+ * (Arista_kernel.cu:754-834).  Row 0's outer edge is the "sup" boundary, row
+ * ny-1's the "inf" boundary, column 0's the "izq" boundary, column nx-1's the
+ * "der" boundary.  In spherical coordinates row j lies at latitude
+ * lat0 + (j + 0.5)*dlat and column i at longitude lon0 + (i + 0.5)*dlon.
+ *
+ * State arrays are FP64, nx*ny each, in this order:
+ *   h1 (water depth), q1x, q1y (water discharge), h2 (granular thickness),
+ *   q2x, q2y (granular discharge), H (bottom depth below the reference level,
+ *   positive downward).  Free surface eta1 = h1 + h2 - H.
+ */
+#ifndef LSH_H
+#define LSH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  0/1/2 keep the reference's meaning (ShallowWater.cu:124,
+ * 50-57, 212-216); the rest are new. */
+#define LSH_OK              0
+#define LSH_ERR_GPU_OOM     1  /* device allocation failed                       */
+#define LSH_ERR_HOST_OOM    2  /* host allocation failed                         */
+#define LSH_ERR_INVALID     3  /* bad argument / size / parameter                */
+#define LSH_ERR_CUDA        4  /* a CUDA runtime call failed                     */
+#define LSH_ERR_NUMERIC     5  /* NaN or negative depth detected in the state    */
+#define LSH_ERR_IO          6  /* file missing / unreadable / malformed          */
+#define LSH_ERR_NO_DEVICE   7  /* no CUDA device (comprobarSoporteCUDA == 1 / 2)  */
+#define LSH_ERR_TIMEOUT     8  /* a bounded device wait gave up                   */
+#define LSH_ERR_STALL       9  /* time step collapsed below dt_min                */
+
+#define LSH_NVARS 7            /* h1 q1x q1y h2 q2x q2y H */
+
+enum { LSH_COORDS_CARTESIAN = 0, LSH_COORDS_SPHERICAL = 1 };
+enum { LSH_FRICTION_COULOMB = 0, LSH_FRICTION_POULIQUEN = 1 };
+
+/*
+ * Solver parameters.  Field meaning follows the reference's shallowWater()
+ * arguments (ShallowWater.cu:125-131) and data.dat (main.cxx:24-60), in the
+ * reference's normalised units when L/H normalisation is used
+ * (Problema.cxx:262-285).  Angles are in radians (Problema.cxx:239-256).
+ * Fields the reference hard-codes are exposed with its values as defaults
+ * (lsh_params_default): peso = beta = 1 (main.cxx:161), eps_h = 5e-3/H
+ * (Problema.cxx:287).
+ */
+typedef struct lsh_params {
+    int32_t nx, ny;          /* cells in x (columns) and y (rows)                     */
+    int32_t order;           /* 1: first order + forward Euler (the reference scheme) */
+                             /* 2: MUSCL (minmod) reconstruction + TVD-RK2 (Heun)     */
+    int32_t coords;          /* LSH_COORDS_*                                          */
+    int32_t friction_law;    /* LSH_FRICTION_* (reference #define COULOMB)            */
+    int32_t track_eta_max;   /* 1: update eta1 max / time every step (A18)            */
+    double dx, dy;           /* Cartesian cell width / height (ancho_vol, alto_vol)   */
+    double lon0, lat0;       /* spherical: corner longitude / latitude, degrees       */
+    double dlon, dlat;       /* spherical: cell size, degrees                         */
+    double radius;           /* spherical: sphere radius, same length unit as dx      */
+    double borde_sup, borde_inf, borde_izq, borde_der; /* 1 open, -1 wall, 0 no-flux   */
+    double cfl;              /* CFL number                                            */
+    double r;                /* density ratio rho1/rho2                               */
+    double angle1, angle2, angle3, angle4; /* friction angles, radians (2..4: Pouliquen) */
+    double mfc, mf0, mfs;    /* interlayer, water-bottom (Manning), sediment-bottom   */
+    double vmax1, vmax2;     /* speed caps (<= 0: off)                                */
+    double gravity;          /* 9.81, or 1 when normalised                           */
+    double eps_h;            /* dry threshold                                         */
+    double L, H;             /* normalisation scales (1, 1 when not normalised)       */
+    double peso, beta;       /* reference constants, 1 and 1                          */
+    double dt_min;           /* stall guard: dt below this sets LSH_ERR_STALL (0 off) */
+} lsh_params;
+
+typedef struct lsh_ctx lsh_ctx;  /* opaque solver context: owns all device memory */
+
+/* Fill `p` with the reference defaults (Coulomb law, first order, Cartesian,
+ * walls, CFL 0.9, r 0.5, g 9.81, eps_h 5e-3, peso = beta = 1, L = H = 1). */
+int lsh_params_default(lsh_params* p);
+
+/* comprobarSoporteCUDA (ComprobarSoporteCUDA.cu:5-25): 0 = a CUDA device is
+ * present, 1 = no device, 2 = no CUDA-capable device. */
+int lsh_check_device(void);
+
+/* Create a context on `device` (-1: current device).  Allocates the FP64 SoA
+ * state (ping-pong), accumulators and the device-resident time/dt record.
+ * Replaces inicializarDatosCuda (ShallowWater.cu:14-110). */
+int lsh_create(const lsh_params* p, int device, lsh_ctx** out);
+int lsh_destroy(lsh_ctx* ctx);
+
+/* Run subsequent work on this cudaStream_t (NULL: the context's own stream). */
+int lsh_set_stream(lsh_ctx* ctx, void* cuda_stream);
+
+/* Upload the state from HOST arrays (nx*ny doubles each, order above; pointers
+ * may be pageable or pinned).  Resets t = 0, eta1 max = h1 + h2 - H with time
+ * 0 (Problema.cxx:542-546) and runs the initial-dt edge pass
+ * (ShallowWater.cu:236-263).  `dt0_out` (may be NULL) receives that dt. */
+int lsh_set_state(lsh_ctx* ctx, const double* const host_state[LSH_NVARS], double* dt0_out);
+
+/* Same, from DEVICE arrays already resident on the context's device. */
+int lsh_set_state_device(lsh_ctx* ctx, const double* const dev_state[LSH_NVARS], double* dt0_out);
+
+/* Advance `nsteps` time steps on the device.  Asynchronous: enqueues a CUDA
+ * graph of the steps on the context stream and returns.  dt and t stay on the
+ * device (no host sync per step, unlike ShallowWater.cu:439-442). */
+int lsh_step(lsh_ctx* ctx, int nsteps);
+
+/* Advance until t >= t_end (the reference's loop condition, ShallowWater.cu:269)
+ * or `max_steps` steps (<= 0: no limit).  Synchronous.  `steps_done` may be NULL. */
+int lsh_run_until(lsh_ctx* ctx, double t_end, long long max_steps, long long* steps_done);
+
+/* Wait for queued work; returns the sticky device error word as a status. */
+int lsh_synchronize(lsh_ctx* ctx);
+
+/* Copy the state to HOST arrays (synchronous). */
+int lsh_get_state(lsh_ctx* ctx, double* const host_state[LSH_NVARS]);
+
+/* Copy the state into DEVICE arrays on the context stream (asynchronous). */
+int lsh_get_state_device(lsh_ctx* ctx, double* const dev_state[LSH_NVARS]);
+
+/* Current time, the dt the next step will use, and the number of steps taken. */
+int lsh_get_time(lsh_ctx* ctx, double* t, double* dt_next, long long* steps);
+
+/* eta1 maximum and its time, nx*ny each (either may be NULL). */
+int lsh_get_eta_max(lsh_ctx* ctx, double* eta_max, double* eta_max_time);
+
+/* Per-cell bit mask of the current state: bit0 h1 >= eps_h, bit1 h2 >= eps_h,
+ * bit2 granular layer at rest (h2 >= eps_h and q2 == 0: Coulomb stop). */
+int lsh_get_masks(lsh_ctx* ctx, uint8_t* host_mask);
+
+/* Number of kernels this library launched since the context was created
+ * (each graph replay counts its kernel nodes). */
+int lsh_get_launch_count(lsh_ctx* ctx, long long* launches);
+
+/* Diagnostics (no counterpart in the reference).
+ * lsh_profile_step: run ONE time step eagerly (not from a graph) with a CUDA
+ * event between consecutive kernels on the context stream; ms_out[i] gets the
+ * duration of the i-th kernel of the step (order 1: 6 kernels -- 4 edge
+ * passes, volume, clock; order 2: 13 -- per stage reconstruction, 4 edge
+ * passes, volume; then clock).  *n_kernels gets the count (<= cap written).
+ * lsh_probe_fp64_peak: FP64 FMA throughput of this device, GFLOP/s
+ * (2 flops per DFMA), from a dependent-chain microkernel timed with events. */
+int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels);
+int lsh_probe_fp64_peak(int device, double* gflops);
+
+/* Human-readable text for a status code. */
+const char* lsh_status_string(int status);
+
+/* Last CUDA error text recorded by the library (thread-local). */
+const char* lsh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSH_H */

@@ -1,0 +1,968 @@
+// lsh_core.cu -- sm_103a kernels and the C ABI (include/lsh.h) of the
+// two-layer finite-volume time step.
+//
+// Layout in HBM: FP64 structure-of-arrays, one array of nx*ny doubles per
+// variable (h1 q1x q1y h2 q2x q2y H), row-major (cell j*nx + i).  The step:
+//   order 1 (the reference scheme, ShallowWater.cu:391-442):
+//     4 colour passes over edges (hor-even, hor-odd, ver-even, ver-odd),
+//     accumulating into 7 SoA accumulators; the first pass writes instead of
+//     accumulating, which replaces the reference's two cudaMemset per step;
+//     then one volume kernel updates the state IN PLACE (each thread owns
+//     one cell), folds the per-cell dt into a block min and one 64-bit
+//     atomicMin on the bit pattern of the (positive) double, and a 1-thread
+//     kernel advances t and dt on the device.  No host sync per step, no
+//     texture copy-back (ShallowWater.cu:447-454), so a run of steps is one
+//     CUDA graph launch.
+//   order 2: minmod reconstruction kernel + the same 4 passes on face values
+//     + volume kernel, twice (Heun / TVD-RK2), the second volume kernel
+//     averaging with the step's initial state.
+// The FP64 math lives in lsh_scheme.cuh.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lsh.h"
+#include "lsh_scheme.cuh"
+
+using lsh::Consts;
+using lsh::EdgeIn;
+using lsh::Geo;
+using lsh::TimeRec;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr unsigned long long kDtInitBits = 0x7fefffffffffffffULL;  // DBL_MAX
+constexpr int kEdgeBlock = 128;
+constexpr int kCellBlock = 256;
+constexpr int kGraphChunk = 16;
+
+thread_local std::string g_last_error;
+
+struct KArgs {
+    Consts c;
+    Geo geo;
+    const double* W[7];   // input state (face values are W + slopes at order 2)
+    double* Wout[6];      // output state of the volume kernel
+    const double* Xavg[6];  // order 2, stage 2: the step's initial state for the average
+    double* acc[7];
+    const double* sx[7];
+    const double* sy[7];
+    double* sxw[7];       // reconstruction kernel outputs
+    double* syw[7];
+    double* eta_max;
+    double* eta_time;
+    TimeRec* tm;
+};
+
+// ------------------------------------------------------------------ kernels
+
+template <int ORDER>
+__device__ __forceinline__ void load_face(const KArgs& a, int id, int side, double W[6], double& Hf) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) W[k] = a.W[k][id];
+    Hf = a.W[6][id];
+    if (ORDER == 2) {
+        const double* const* s = (side < 2) ? a.sx : a.sy;
+        const double sg = (side & 1) ? 1.0 : -1.0;
+        const double de1 = s[0][id], de2 = s[3][id], dH = s[6][id];
+        W[0] = W[0] + sg * (de1 - de2);
+        W[1] = W[1] + sg * s[1][id];
+        W[2] = W[2] + sg * s[2][id];
+        W[3] = W[3] + sg * (de2 + dH);
+        W[4] = W[4] + sg * s[4][id];
+        W[5] = W[5] + sg * s[5][id];
+        Hf = Hf + sg * dH;
+    }
+}
+
+// One edge: gather both sides, evaluate, scatter to the accumulators.
+// dir 0: horizontal edge row y between rows y-1 and y, column x.
+// dir 1: vertical edge column x between columns x-1 and x, row y.
+template <int DIR, bool FIRST, int ORDER>
+__device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    EdgeIn e;
+    int id0, id1 = -1, side0, row0, row1 = 0;
+    double bor = 0.0;
+    if (DIR == 0) {
+        e.len = a.geo.len_h[y];
+        e.nx = 0.0;
+        if (y == 0) { id0 = x; row0 = 0; e.ny = -1.0; bor = a.c.borde_sup; side0 = 2; }
+        else if (y == ny) { id0 = (ny - 1) * nx + x; row0 = ny - 1; e.ny = 1.0; bor = a.c.borde_inf; side0 = 3; }
+        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; row0 = y - 1; row1 = y; e.ny = 1.0; side0 = 3; }
+    } else {
+        e.len = a.geo.len_v[y];
+        e.ny = 0.0;
+        row0 = row1 = y;
+        if (x == 0) { id0 = y * nx; e.nx = -1.0; bor = a.c.borde_izq; side0 = 0; }
+        else if (x == nx) { id0 = y * nx + nx - 1; e.nx = 1.0; bor = a.c.borde_der; side0 = 1; }
+        else { id0 = y * nx + x - 1; id1 = id0 + 1; e.nx = 1.0; side0 = 1; }
+    }
+    e.interior = (id1 >= 0);
+    load_face<ORDER>(a, id0, side0, e.W0, e.H0);
+    e.area0 = a.geo.area[row0];
+    e.hc0[0] = a.W[0][id0];
+    e.hc0[1] = a.W[3][id0];
+    if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
+    else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
+    if (e.interior) {
+        load_face<ORDER>(a, id1, (DIR == 0) ? 2 : 0, e.W1, e.H1);
+        e.area1 = a.geo.area[row1];
+        e.hc1[0] = a.W[0][id1];
+        e.hc1[1] = a.W[3][id1];
+        if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
+        else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) e.W1[k] = e.W0[k];
+        const int kn = (DIR == 0) ? 2 : 1;
+        e.W1[kn] = e.W0[kn] * bor;
+        e.W1[kn + 3] = e.W0[kn + 3] * bor;
+        e.H1 = e.H0;
+        e.area1 = e.area0;
+        e.hc1[0] = e.hc1[1] = 0.0;
+        e.acc1h[0] = e.acc1h[1] = 0.0;
+    }
+    double d0[6], d1[6], wave;
+    const bool wet = lsh::edge_flux(e, dt, a.c, d0, d1, wave);
+    if (FIRST) {
+        // every cell meets exactly one hor-even edge: write, do not accumulate
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] = wet ? (0.0 - d0[k]) : 0.0;
+        a.acc[6][id0] = wet ? (0.0 + wave) : 0.0;
+        if (e.interior) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] = wet ? (0.0 - d1[k]) : 0.0;
+            a.acc[6][id1] = wet ? (0.0 + wave) : 0.0;
+        }
+    } else if (wet) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] -= d0[k];
+        a.acc[6][id0] += wave;
+        if (e.interior) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] -= d1[k];
+            a.acc[6][id1] += wave;
+        }
+    }
+}
+
+// Horizontal edges of parity `par`: x along threads, edge rows along blocks.
+template <bool FIRST, int ORDER>
+__global__ void __launch_bounds__(kEdgeBlock) k_edges_h(KArgs a, int par) {
+    if (a.tm->done) return;
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nx) return;
+    const double dt = a.tm->dt;
+    const int nlines = (ny - par) / 2 + 1;
+    for (int t = blockIdx.y; t < nlines; t += gridDim.y) do_edge<0, FIRST, ORDER>(a, x, par + 2 * t, dt);
+}
+
+// Vertical edges of parity `par`: edge columns along threads, rows along blocks.
+template <int ORDER>
+__global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
+    if (a.tm->done) return;
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = par + 2 * t;
+    if (x > nx) return;
+    const double dt = a.tm->dt;
+    for (int y = blockIdx.y; y < ny; y += gridDim.y) do_edge<1, false, ORDER>(a, x, y, dt);
+}
+
+__device__ __forceinline__ double minmod(double a, double b) {
+    if (a > 0.0 && b > 0.0) return (a < b) ? a : b;
+    if (a < 0.0 && b < 0.0) return (a > b) ? a : b;
+    return 0.0;
+}
+
+__device__ __forceinline__ double recon_var(const KArgs& a, int id, int k) {
+    if (k == 0) return (a.W[0][id] + a.W[3][id]) - a.W[6][id];
+    if (k == 3) return a.W[3][id] - a.W[6][id];
+    return a.W[k][id];
+}
+
+// Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
+// with a first-order fallback where a reconstructed depth would be negative.
+__global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
+    if (a.tm->done) return;
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nx * ny) return;
+    const int j = id / nx, i = id - j * nx;
+    double sx[7], sy[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const double pc = recon_var(a, id, k);
+        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - recon_var(a, id - 1, k), recon_var(a, id + 1, k) - pc) : 0.0;
+        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - recon_var(a, id - nx, k), recon_var(a, id + nx, k) - pc) : 0.0;
+    }
+    const double h1 = a.W[0][id], h2 = a.W[3][id];
+    const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
+    const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
+    const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
+                     (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        a.sxw[k][id] = bad ? 0.0 : sx[k];
+        a.syw[k][id] = bad ? 0.0 : sy[k];
+    }
+}
+
+__device__ __forceinline__ void block_min_bits(unsigned long long v, TimeRec* tm) {
+    __shared__ unsigned long long red[kCellBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = (w < v) ? w : v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kDtInitBits;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+            v = (w < v) ? w : v;
+        }
+        if (lane == 0) atomicMin(&tm->dtmin_bits, v);
+    }
+}
+
+// MODE 0: order 1, in place; per-cell dt min.  MODE 1: order 2 stage 1
+// (W -> Wout), per-cell dt min.  MODE 2: order 2 stage 2, Wout = (Xavg + E(W)) / 2.
+template <int MODE>
+__global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
+    if (a.tm->done) return;
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const double dt = a.tm->dt;
+    unsigned long long bits = kDtInitBits;
+    if (id < nx * ny) {
+        const int j = id / nx;
+        double wo[6], acc[7], w[6], dti;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) acc[k] = a.acc[k][id];
+        if (a.c.order == 2) {
+            // cell-midpoint integral of g h d(eta) over the reconstructed cell
+            const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
+            const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
+            const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
+            const double wx = a.geo.wx[j], wy = a.geo.wy[j];
+            acc[1] -= a.c.peso * (gh1 * e1x * wx);
+            acc[4] -= a.c.peso * (gh2 * ((1.0 - a.c.r) * e2x + a.c.r * e1x) * wx);
+            acc[2] -= a.c.peso * (gh1 * e1y * wy);
+            acc[5] -= a.c.peso * (gh2 * ((1.0 - a.c.r) * e2y + a.c.r * e1y) * wy);
+        }
+        if (MODE != 2 && a.c.track_eta) {
+            // actualizarEta1MaximaGPU (Volumen_kernel.cu:182-213): state before the step
+            const double v = wo[0] - a.W[6][id];
+            if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
+        }
+        lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.tanR[j], dt, a.c);
+        if (MODE == 2) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = 0.5 * (a.Xavg[k][id] + w[k]);
+        }
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
+        if (bad) atomicOr(&a.tm->err, 1 << LSH_ERR_NUMERIC);
+        bits = (unsigned long long)__double_as_longlong(dti);
+    }
+    if (MODE != 2) block_min_bits(bits, a.tm);
+}
+
+// Advance the device clock: t += dt, dt = min per-cell dt (ShallowWater.cu:436-442).
+__global__ void k_advance(TimeRec* tm) {
+    if (tm->done) return;
+    tm->t += tm->dt;
+    tm->steps += 1;
+    const double nd = __longlong_as_double((long long)tm->dtmin_bits);
+    tm->dt = nd;
+    tm->dtmin_bits = kDtInitBits;
+    if (tm->t >= tm->t_end) tm->done = 1;
+    if (tm->dt_min > 0.0 && nd < tm->dt_min) { tm->err |= 1 << LSH_ERR_STALL; tm->done = 1; }
+    if (tm->err) tm->done = 1;
+}
+
+// Initial-dt edge pass (procesarAristasDeltaTInicialGPU), writing acc[6].
+template <int DIR, bool FIRST>
+__global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nlines = (DIR == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
+    const int nalong = (DIR == 0) ? nx : ny;
+    // DIR 0: threads along x, lines along blocks.y; DIR 1: threads along edge columns
+    for (int bl = blockIdx.y; bl < ((DIR == 0) ? nlines : nalong); bl += gridDim.y) {
+        int x, y;
+        if (DIR == 0) { x = tid; y = par + 2 * bl; if (x >= nx) return; }
+        else { x = par + 2 * tid; y = bl; if (tid >= nlines) return; }
+        int id0, id1 = -1;
+        double nxv, nyv, bor = 0.0, len;
+        if (DIR == 0) {
+            len = a.geo.len_h[y];
+            nxv = 0.0;
+            if (y == 0) { id0 = x; nyv = -1.0; bor = a.c.borde_sup; }
+            else if (y == ny) { id0 = (ny - 1) * nx + x; nyv = 1.0; bor = a.c.borde_inf; }
+            else { id0 = (y - 1) * nx + x; id1 = id0 + nx; nyv = 1.0; }
+        } else {
+            len = a.geo.len_v[y];
+            nyv = 0.0;
+            if (x == 0) { id0 = y * nx; nxv = -1.0; bor = a.c.borde_izq; }
+            else if (x == nx) { id0 = y * nx + nx - 1; nxv = 1.0; bor = a.c.borde_der; }
+            else { id0 = y * nx + x - 1; id1 = id0 + 1; nxv = 1.0; }
+        }
+        double W0[6], W1[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) W0[k] = a.W[k][id0];
+        if (id1 >= 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) W1[k] = a.W[k][id1];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) W1[k] = W0[k];
+            const int kn = (DIR == 0) ? 2 : 1;
+            W1[kn] = W0[kn] * bor;
+            W1[kn + 3] = W0[kn + 3] * bor;
+        }
+        const double wv = lsh::edge_initial_wave(W0, W1, nxv, nyv, len, a.c);
+        if (FIRST) {
+            a.acc[6][id0] = 0.0 + wv;
+            if (id1 >= 0) a.acc[6][id1] = 0.0 + wv;
+        } else {
+            a.acc[6][id0] += wv;
+            if (id1 >= 0) a.acc[6][id1] += wv;
+        }
+    }
+}
+
+// Per-cell dt of the initial wave pass (obtenerDeltaTVolumenesGPU) and its min.
+__global__ void __launch_bounds__(kCellBlock) k_cell_dt(KArgs a) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long bits = kDtInitBits;
+    if (id < nx * ny) {
+        const int j = id / nx;
+        const double w = a.acc[6][id];
+        const double d = (w < lsh::kEps) ? lsh::kBig : (2.0 * a.c.cfl * a.geo.area[j]) / w;
+        bits = (unsigned long long)__double_as_longlong(d);
+    }
+    block_min_bits(bits, a.tm);
+}
+
+__global__ void k_init_finish(TimeRec* tm) {
+    tm->dt = __longlong_as_double((long long)tm->dtmin_bits);
+    tm->dtmin_bits = kDtInitBits;
+    tm->t = 0.0;
+    tm->steps = 0;
+    tm->done = 0;
+    tm->err = 0;
+}
+
+// eta1 max initial value h1 + h2 - H, time 0 (Problema.cxx:542-546)
+__global__ void __launch_bounds__(kCellBlock) k_init_eta(KArgs a) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.c.nx * a.c.ny) return;
+    a.eta_max[id] = a.W[0][id] + a.W[3][id] - a.W[6][id];
+    a.eta_time[id] = 0.0;
+}
+
+// FP64 throughput probe: 8 independent DFMA chains per thread.
+__global__ void k_fp64_probe(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 12345.678) out[0] = s;  // keeps the chains live; never true in practice
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+
+struct lsh_ctx {
+    lsh_params p;
+    Consts c;
+    int device = 0;
+    cudaStream_t own = nullptr;     // created by the library; used for graph capture
+    cudaStream_t stream = nullptr;  // where work runs (own, or the caller's)
+    size_t N = 0;
+    void* slab = nullptr;           // one device allocation for every array
+    double* X[7] = {};              // state (X[6] = H)
+    double* Y[6] = {};              // order-2 stage buffer
+    double* acc[7] = {};
+    double* sx[7] = {};
+    double* sy[7] = {};
+    double* eta_max = nullptr;
+    double* eta_time = nullptr;
+    double* geo_buf = nullptr;
+    Geo geo{};
+    TimeRec* tm = nullptr;
+    TimeRec* tm_host = nullptr;     // pinned mirror for reads
+    cudaGraphExec_t g_chunk = nullptr, g_one = nullptr;
+    long long launches = 0;
+    int kernels_per_step = 0;
+    bool has_state = false;
+};
+
+namespace {
+
+int fail_cuda(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    (void)cudaGetLastError();
+    return (e == cudaErrorMemoryAllocation) ? LSH_ERR_GPU_OOM : LSH_ERR_CUDA;
+}
+
+#define LSH_CUDA(call)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return fail_cuda(e_, #call);     \
+    } while (0)
+
+int check_params(const lsh_params* p) {
+    if (!p) return LSH_ERR_INVALID;
+    if (p->nx < 1 || p->ny < 1) { g_last_error = "nx and ny must be >= 1"; return LSH_ERR_INVALID; }
+    if ((long long)p->nx * p->ny >= (1LL << 31) - 1024) { g_last_error = "grid too large for 32-bit indexing"; return LSH_ERR_INVALID; }
+    if (p->order != 1 && p->order != 2) { g_last_error = "order must be 1 or 2"; return LSH_ERR_INVALID; }
+    if (p->coords != LSH_COORDS_CARTESIAN && p->coords != LSH_COORDS_SPHERICAL) { g_last_error = "bad coords"; return LSH_ERR_INVALID; }
+    if (p->friction_law != LSH_FRICTION_COULOMB && p->friction_law != LSH_FRICTION_POULIQUEN) { g_last_error = "bad friction law"; return LSH_ERR_INVALID; }
+    if (!(p->eps_h > 0) || !(p->gravity > 0) || !(p->r >= 0 && p->r < 1) || !(p->peso > 0) || !(p->cfl > 0) || !(p->H > 0) || !(p->L > 0)) {
+        g_last_error = "eps_h, gravity, peso, cfl, L, H must be > 0 and 0 <= r < 1";
+        return LSH_ERR_INVALID;
+    }
+    if (p->coords == LSH_COORDS_CARTESIAN && !(p->dx > 0 && p->dy > 0)) { g_last_error = "dx, dy must be > 0"; return LSH_ERR_INVALID; }
+    if (p->coords == LSH_COORDS_SPHERICAL &&
+        !(p->dlon > 0 && p->dlat > 0 && p->radius > 0 && std::fabs(p->lat0) < 90 && std::fabs(p->lat0 + p->ny * p->dlat) < 90)) {
+        g_last_error = "spherical grid needs dlon, dlat, radius > 0 and latitudes inside (-90, 90)";
+        return LSH_ERR_INVALID;
+    }
+    return LSH_OK;
+}
+
+Consts make_consts(const lsh_params& p) {
+    Consts c{};
+    c.g = p.gravity; c.r = p.r; c.gp = p.gravity * (1.0 - p.r);
+    c.eps_h = p.eps_h; c.peso = p.peso; c.beta = p.beta; c.cfl = p.cfl;
+    c.mu = std::fabs(std::tan(p.angle1)) * (p.L / p.H);  // defTerminoFriccion, Coulomb
+    c.mfc = p.mfc; c.mf0 = p.mf0; c.mfs = p.mfs; c.vmax1 = p.vmax1; c.vmax2 = p.vmax2;
+    c.L = p.L; c.H = p.H;
+    c.tan1 = std::tan(p.angle1); c.tan2 = std::tan(p.angle2); c.tan3 = std::tan(p.angle3); c.tan4 = std::tan(p.angle4);
+    c.borde_sup = p.borde_sup; c.borde_inf = p.borde_inf; c.borde_izq = p.borde_izq; c.borde_der = p.borde_der;
+    c.law = p.friction_law; c.order = p.order; c.nx = p.nx; c.ny = p.ny; c.track_eta = p.track_eta_max;
+    return c;
+}
+
+// Per-row geometry on the host (same formulas as the CPU oracle).
+void make_geo(const lsh_params& p, std::vector<double>& area, std::vector<double>& len_v, std::vector<double>& len_h,
+              std::vector<double>& tanR, std::vector<double>& wx, std::vector<double>& wy) {
+    const int ny = p.ny;
+    area.resize(ny); len_v.resize(ny); len_h.resize(ny + 1); tanR.resize(ny); wx.resize(ny); wy.resize(ny);
+    if (p.coords == LSH_COORDS_SPHERICAL) {
+        const double d2r = kPi / 180.0;
+        const double R = p.radius, dl = p.dlon * d2r, dp = p.dlat * d2r;
+        for (int y = 0; y <= ny; ++y) len_h[y] = R * std::cos((p.lat0 + y * p.dlat) * d2r) * dl;
+        for (int j = 0; j < ny; ++j) {
+            const double ps = (p.lat0 + j * p.dlat) * d2r, pn = (p.lat0 + (j + 1) * p.dlat) * d2r;
+            const double pc = (p.lat0 + (j + 0.5) * p.dlat) * d2r;
+            area[j] = R * R * dl * (std::sin(pn) - std::sin(ps));
+            len_v[j] = R * dp;
+            tanR[j] = std::tan(pc) / R;
+            wx[j] = area[j] / (R * std::cos(pc) * dl);
+            wy[j] = area[j] / (R * dp);
+        }
+    } else {
+        for (int y = 0; y <= ny; ++y) len_h[y] = p.dx;
+        for (int j = 0; j < ny; ++j) {
+            area[j] = p.dx * p.dy;  // Problema.cxx:296
+            len_v[j] = p.dy;
+            tanR[j] = 0.0;
+            wx[j] = p.dy;
+            wy[j] = p.dx;
+        }
+    }
+}
+
+KArgs base_args(const lsh_ctx* ctx) {
+    KArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.c = ctx->c;
+    a.geo = ctx->geo;
+    for (int k = 0; k < 7; ++k) {
+        a.acc[k] = ctx->acc[k];
+        a.sx[k] = ctx->sx[k]; a.sy[k] = ctx->sy[k];
+        a.sxw[k] = ctx->sx[k]; a.syw[k] = ctx->sy[k];
+    }
+    a.eta_max = ctx->eta_max;
+    a.eta_time = ctx->eta_time;
+    a.tm = ctx->tm;
+    return a;
+}
+
+dim3 grid_h(const lsh_ctx* ctx, int par) {
+    const int nlines = (ctx->p.ny - par) / 2 + 1;
+    return dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min(nlines, 65535));
+}
+
+dim3 grid_v(const lsh_ctx* ctx, int par) {
+    const int nlines = (ctx->p.nx - par) / 2 + 1;
+    return dim3((nlines + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535));
+}
+
+unsigned cell_blocks(const lsh_ctx* ctx) { return unsigned((ctx->N + kCellBlock - 1) / kCellBlock); }
+
+template <int ORDER>
+void enqueue_passes(const lsh_ctx* ctx, const KArgs& a, cudaStream_t s) {
+    k_edges_h<true, ORDER><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0);
+    k_edges_h<false, ORDER><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1);
+    k_edges_v<ORDER><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0);
+    k_edges_v<ORDER><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1);
+}
+
+// Enqueue one time step; returns the number of kernels launched.
+int enqueue_step(const lsh_ctx* ctx, cudaStream_t s) {
+    const unsigned nb = cell_blocks(ctx);
+    if (ctx->p.order == 1) {
+        KArgs a = base_args(ctx);
+        for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
+        for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
+        enqueue_passes<1>(ctx, a, s);
+        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+        k_advance<<<1, 1, 0, s>>>(ctx->tm);
+        return 6;
+    }
+    KArgs a1 = base_args(ctx);
+    for (int k = 0; k < 7; ++k) a1.W[k] = ctx->X[k];
+    for (int k = 0; k < 6; ++k) a1.Wout[k] = ctx->Y[k];
+    k_recon<<<nb, kCellBlock, 0, s>>>(a1);
+    enqueue_passes<2>(ctx, a1, s);
+    k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+    KArgs a2 = base_args(ctx);
+    for (int k = 0; k < 6; ++k) a2.W[k] = ctx->Y[k];
+    a2.W[6] = ctx->X[6];
+    for (int k = 0; k < 6; ++k) { a2.Wout[k] = ctx->X[k]; a2.Xavg[k] = ctx->X[k]; }
+    k_recon<<<nb, kCellBlock, 0, s>>>(a2);
+    enqueue_passes<2>(ctx, a2, s);
+    k_volume<2><<<nb, kCellBlock, 0, s>>>(a2);
+    k_advance<<<1, 1, 0, s>>>(ctx->tm);
+    return 13;
+}
+
+int build_graph(lsh_ctx* ctx, int nsteps, cudaGraphExec_t* out) {
+    cudaGraph_t graph = nullptr;
+    LSH_CUDA(cudaStreamBeginCapture(ctx->own, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < nsteps; ++i) enqueue_step(ctx, ctx->own);
+    cudaError_t e = cudaStreamEndCapture(ctx->own, &graph);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+    return LSH_OK;
+}
+
+int err_bits_to_status(int bits) {
+    for (int s = 1; s < 31; ++s)
+        if (bits & (1 << s)) return s;
+    return LSH_OK;
+}
+
+int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKind kind, double* dt0_out) {
+    const size_t bytes = ctx->N * sizeof(double);
+    for (int k = 0; k < 7; ++k) {
+        if (!src[k]) { g_last_error = "null state pointer"; return LSH_ERR_INVALID; }
+        LSH_CUDA(cudaMemcpyAsync(ctx->X[k], src[k], bytes, kind, ctx->stream));
+    }
+    KArgs a = base_args(ctx);
+    for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
+    const unsigned nb = cell_blocks(ctx);
+    cudaStream_t s = ctx->stream;
+    k_init_eta<<<nb, kCellBlock, 0, s>>>(a);
+    TimeRec init{};
+    init.dtmin_bits = kDtInitBits;
+    init.t_end = INFINITY;
+    init.dt_min = ctx->p.dt_min;
+    LSH_CUDA(cudaMemcpyAsync(ctx->tm, &init, sizeof(TimeRec), cudaMemcpyHostToDevice, s));
+    k_init_wave<0, true><<<dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ctx->p.ny) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+    k_init_wave<0, false><<<dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ctx->p.ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+    k_init_wave<1, false><<<dim3(((ctx->p.nx) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+    k_init_wave<1, false><<<dim3(((ctx->p.nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+    k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
+    k_init_finish<<<1, 1, 0, s>>>(ctx->tm);
+    ctx->launches += 7;
+    LSH_CUDA(cudaGetLastError());
+    LSH_CUDA(cudaMemcpyAsync(ctx->tm_host, ctx->tm, sizeof(TimeRec), cudaMemcpyDeviceToHost, s));
+    LSH_CUDA(cudaStreamSynchronize(s));
+    ctx->has_state = true;
+    if (dt0_out) *dt0_out = ctx->tm_host->dt;
+    return LSH_OK;
+}
+
+int read_time(lsh_ctx* ctx) {
+    LSH_CUDA(cudaMemcpyAsync(ctx->tm_host, ctx->tm, sizeof(TimeRec), cudaMemcpyDeviceToHost, ctx->stream));
+    LSH_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LSH_OK;
+}
+
+int set_t_end(lsh_ctx* ctx, double t_end) {
+    // update t_end and recompute `done` on the device stream (small H2D copy of two fields)
+    if (int s = read_time(ctx)) return s;
+    ctx->tm_host->t_end = t_end;
+    ctx->tm_host->done = (ctx->tm_host->t >= t_end || ctx->tm_host->err) ? 1 : 0;
+    LSH_CUDA(cudaMemcpyAsync(ctx->tm, ctx->tm_host, sizeof(TimeRec), cudaMemcpyHostToDevice, ctx->stream));
+    return LSH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lsh_params_default(lsh_params* p) {
+    if (!p) return LSH_ERR_INVALID;
+    std::memset(p, 0, sizeof(*p));
+    p->nx = p->ny = 1;
+    p->order = 1;
+    p->coords = LSH_COORDS_CARTESIAN;
+    p->friction_law = LSH_FRICTION_COULOMB;
+    p->dx = p->dy = 1.0;
+    p->radius = 6378136.6;
+    p->borde_sup = p->borde_inf = p->borde_izq = p->borde_der = -1.0;
+    p->cfl = 0.9;
+    p->r = 0.5;
+    p->gravity = 9.81;
+    p->eps_h = 5e-3;
+    p->L = p->H = 1.0;
+    p->peso = p->beta = 1.0;
+    return LSH_OK;
+}
+
+int lsh_check_device(void) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) { (void)cudaGetLastError(); return 1; }
+    if (n == 0) return 1;
+    for (int d = 0; d < n; ++d) {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, d) == cudaSuccess && prop.major >= 1) return 0;
+    }
+    return 2;
+}
+
+const char* lsh_status_string(int s) {
+    switch (s) {
+        case LSH_OK: return "ok";
+        case LSH_ERR_GPU_OOM: return "not enough GPU memory";
+        case LSH_ERR_HOST_OOM: return "not enough CPU memory";
+        case LSH_ERR_INVALID: return "invalid argument";
+        case LSH_ERR_CUDA: return "CUDA error";
+        case LSH_ERR_NUMERIC: return "NaN or Inf in the state";
+        case LSH_ERR_IO: return "file missing or malformed";
+        case LSH_ERR_NO_DEVICE: return "no CUDA device";
+        case LSH_ERR_TIMEOUT: return "bounded device wait timed out";
+        case LSH_ERR_STALL: return "time step below dt_min";
+        default: return "unknown status";
+    }
+}
+
+const char* lsh_last_error(void) { return g_last_error.c_str(); }
+
+int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
+    if (!out) return LSH_ERR_INVALID;
+    *out = nullptr;
+    if (int s = check_params(p)) return s;
+    if (lsh_check_device() != 0) { g_last_error = "no CUDA device"; return LSH_ERR_NO_DEVICE; }
+    lsh_ctx* ctx = new (std::nothrow) lsh_ctx();
+    if (!ctx) return LSH_ERR_HOST_OOM;
+    ctx->p = *p;
+    ctx->c = make_consts(*p);
+    ctx->N = size_t(p->nx) * p->ny;
+    auto bail = [&](int s) { lsh_destroy(ctx); return s; };
+    if (device >= 0) {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaSetDevice"));
+    }
+    {
+        cudaError_t e = cudaGetDevice(&ctx->device);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaGetDevice"));
+        e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaStreamCreate"));
+        ctx->stream = ctx->own;
+    }
+    // one slab: X(7) + Y(6) + acc(7) + eta(2) [+ sx, sy (14)] arrays of N, geometry, time record
+    const size_t n_pad = (ctx->N + 31) & ~size_t(31);  // 256-byte aligned arrays
+    const int n_arrays = 7 + 6 + 7 + 2 + ((p->order == 2) ? 14 : 0);
+    const size_t geo_n = size_t(6) * (p->ny + 1);
+    const size_t bytes = (size_t(n_arrays) * n_pad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) + 256;
+    {
+        cudaError_t e = cudaMalloc(&ctx->slab, bytes);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc"));
+        e = cudaMallocHost((void**)&ctx->tm_host, sizeof(TimeRec));
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMallocHost"));
+    }
+    double* cur = static_cast<double*>(ctx->slab);
+    for (int k = 0; k < 7; ++k) { ctx->X[k] = cur; cur += n_pad; }
+    for (int k = 0; k < 6; ++k) { ctx->Y[k] = cur; cur += n_pad; }
+    for (int k = 0; k < 7; ++k) { ctx->acc[k] = cur; cur += n_pad; }
+    ctx->eta_max = cur; cur += n_pad;
+    ctx->eta_time = cur; cur += n_pad;
+    if (p->order == 2) {
+        for (int k = 0; k < 7; ++k) { ctx->sx[k] = cur; cur += n_pad; }
+        for (int k = 0; k < 7; ++k) { ctx->sy[k] = cur; cur += n_pad; }
+    }
+    ctx->geo_buf = cur;
+    cur += (geo_n + 31) & ~size_t(31);
+    ctx->tm = reinterpret_cast<TimeRec*>(cur);
+
+    std::vector<double> area, len_v, len_h, tanR, wx, wy;
+    make_geo(*p, area, len_v, len_h, tanR, wx, wy);
+    std::vector<double> g(geo_n, 0.0);
+    const size_t st = size_t(p->ny + 1);
+    std::copy(area.begin(), area.end(), g.begin());
+    std::copy(len_v.begin(), len_v.end(), g.begin() + st);
+    std::copy(len_h.begin(), len_h.end(), g.begin() + 2 * st);
+    std::copy(tanR.begin(), tanR.end(), g.begin() + 3 * st);
+    std::copy(wx.begin(), wx.end(), g.begin() + 4 * st);
+    std::copy(wy.begin(), wy.end(), g.begin() + 5 * st);
+    {
+        cudaError_t e = cudaMemcpy(ctx->geo_buf, g.data(), geo_n * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy geometry"));
+    }
+    ctx->geo.area = ctx->geo_buf;
+    ctx->geo.len_v = ctx->geo_buf + st;
+    ctx->geo.len_h = ctx->geo_buf + 2 * st;
+    ctx->geo.tanR = ctx->geo_buf + 3 * st;
+    ctx->geo.wx = ctx->geo_buf + 4 * st;
+    ctx->geo.wy = ctx->geo_buf + 5 * st;
+    ctx->kernels_per_step = (p->order == 1) ? 6 : 13;
+    *out = ctx;
+    return LSH_OK;
+}
+
+int lsh_destroy(lsh_ctx* ctx) {
+    if (!ctx) return LSH_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->g_chunk) cudaGraphExecDestroy(ctx->g_chunk);
+    if (ctx->g_one) cudaGraphExecDestroy(ctx->g_one);
+    if (ctx->slab) cudaFree(ctx->slab);
+    if (ctx->tm_host) cudaFreeHost(ctx->tm_host);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    (void)cudaGetLastError();
+    delete ctx;
+    return LSH_OK;
+}
+
+int lsh_set_stream(lsh_ctx* ctx, void* s) {
+    if (!ctx) return LSH_ERR_INVALID;
+    ctx->stream = s ? static_cast<cudaStream_t>(s) : ctx->own;
+    return LSH_OK;
+}
+
+int lsh_set_state(lsh_ctx* ctx, const double* const host_state[LSH_NVARS], double* dt0_out) {
+    if (!ctx || !host_state) return LSH_ERR_INVALID;
+    return upload_state(ctx, host_state, cudaMemcpyHostToDevice, dt0_out);
+}
+
+int lsh_set_state_device(lsh_ctx* ctx, const double* const dev_state[LSH_NVARS], double* dt0_out) {
+    if (!ctx || !dev_state) return LSH_ERR_INVALID;
+    return upload_state(ctx, dev_state, cudaMemcpyDeviceToDevice, dt0_out);
+}
+
+int lsh_step(lsh_ctx* ctx, int nsteps) {
+    if (!ctx || nsteps < 0) return LSH_ERR_INVALID;
+    if (!ctx->has_state) { g_last_error = "lsh_set_state has not been called"; return LSH_ERR_INVALID; }
+    if (nsteps == 0) return LSH_OK;
+    if (!ctx->g_chunk) { if (int s = build_graph(ctx, kGraphChunk, &ctx->g_chunk)) return s; }
+    if (!ctx->g_one) { if (int s = build_graph(ctx, 1, &ctx->g_one)) return s; }
+    const int full = nsteps / kGraphChunk, rest = nsteps % kGraphChunk;
+    for (int i = 0; i < full; ++i) LSH_CUDA(cudaGraphLaunch(ctx->g_chunk, ctx->stream));
+    for (int i = 0; i < rest; ++i) LSH_CUDA(cudaGraphLaunch(ctx->g_one, ctx->stream));
+    ctx->launches += (long long)nsteps * ctx->kernels_per_step;
+    return LSH_OK;
+}
+
+int lsh_synchronize(lsh_ctx* ctx) {
+    if (!ctx) return LSH_ERR_INVALID;
+    if (int s = read_time(ctx)) return s;
+    return err_bits_to_status(ctx->tm_host->err);
+}
+
+int lsh_run_until(lsh_ctx* ctx, double t_end, long long max_steps, long long* steps_done) {
+    if (!ctx) return LSH_ERR_INVALID;
+    if (!ctx->has_state) { g_last_error = "lsh_set_state has not been called"; return LSH_ERR_INVALID; }
+    if (int s = set_t_end(ctx, t_end)) return s;
+    if (int s = read_time(ctx)) return s;
+    const long long start = ctx->tm_host->steps;
+    int status = LSH_OK;
+    while (!ctx->tm_host->done) {
+        long long left = (max_steps > 0) ? max_steps - (ctx->tm_host->steps - start) : (1LL << 40);
+        if (left <= 0) break;
+        const int batch = (int)std::min<long long>(left, 8 * kGraphChunk);
+        if ((status = lsh_step(ctx, batch))) break;
+        if ((status = read_time(ctx))) break;
+    }
+    if (status == LSH_OK) status = err_bits_to_status(ctx->tm_host->err);
+    if (steps_done) *steps_done = ctx->tm_host->steps - start;
+    // step-count mode again for later lsh_step calls
+    int s2 = set_t_end(ctx, INFINITY);
+    if (status == LSH_OK) status = s2;
+    return status;
+}
+
+int lsh_get_state(lsh_ctx* ctx, double* const host_state[LSH_NVARS]) {
+    if (!ctx || !host_state) return LSH_ERR_INVALID;
+    const size_t bytes = ctx->N * sizeof(double);
+    for (int k = 0; k < 7; ++k)
+        if (host_state[k]) LSH_CUDA(cudaMemcpyAsync(host_state[k], ctx->X[k], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    LSH_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LSH_OK;
+}
+
+int lsh_get_state_device(lsh_ctx* ctx, double* const dev_state[LSH_NVARS]) {
+    if (!ctx || !dev_state) return LSH_ERR_INVALID;
+    const size_t bytes = ctx->N * sizeof(double);
+    for (int k = 0; k < 7; ++k)
+        if (dev_state[k]) LSH_CUDA(cudaMemcpyAsync(dev_state[k], ctx->X[k], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return LSH_OK;
+}
+
+int lsh_get_time(lsh_ctx* ctx, double* t, double* dt_next, long long* steps) {
+    if (!ctx) return LSH_ERR_INVALID;
+    if (int s = read_time(ctx)) return s;
+    if (t) *t = ctx->tm_host->t;
+    if (dt_next) *dt_next = ctx->tm_host->dt;
+    if (steps) *steps = ctx->tm_host->steps;
+    return LSH_OK;
+}
+
+int lsh_get_eta_max(lsh_ctx* ctx, double* eta_max, double* eta_time) {
+    if (!ctx) return LSH_ERR_INVALID;
+    const size_t bytes = ctx->N * sizeof(double);
+    if (eta_max) LSH_CUDA(cudaMemcpyAsync(eta_max, ctx->eta_max, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (eta_time) LSH_CUDA(cudaMemcpyAsync(eta_time, ctx->eta_time, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    LSH_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LSH_OK;
+}
+
+int lsh_get_masks(lsh_ctx* ctx, uint8_t* mask) {
+    if (!ctx || !mask) return LSH_ERR_INVALID;
+    std::vector<double> h1(ctx->N), h2(ctx->N), qx(ctx->N), qy(ctx->N);
+    double* dst[LSH_NVARS] = {h1.data(), nullptr, nullptr, h2.data(), qx.data(), qy.data(), nullptr};
+    if (int s = lsh_get_state(ctx, dst)) return s;
+    const double eps = ctx->p.eps_h;
+    for (size_t i = 0; i < ctx->N; ++i) {
+        uint8_t m = 0;
+        if (h1[i] >= eps) m |= 1;
+        if (h2[i] >= eps) { m |= 2; if (qx[i] == 0.0 && qy[i] == 0.0) m |= 4; }
+        mask[i] = m;
+    }
+    return LSH_OK;
+}
+
+int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels) {
+    if (!ctx || !ms_out || cap < 1) return LSH_ERR_INVALID;
+    if (!ctx->has_state) { g_last_error = "lsh_set_state has not been called"; return LSH_ERR_INVALID; }
+    cudaStream_t s = ctx->stream;
+    const int nk = ctx->kernels_per_step;
+    std::vector<cudaEvent_t> ev(nk + 1);
+    for (auto& e : ev) LSH_CUDA(cudaEventCreate(&e));
+    const unsigned nb = cell_blocks(ctx);
+    int i = 0;
+    auto mark = [&]() { cudaEventRecord(ev[i++], s); };
+    mark();
+    if (ctx->p.order == 1) {
+        KArgs a = base_args(ctx);
+        for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
+        for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
+        k_edges_h<true, 1><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
+        k_edges_h<false, 1><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
+        k_edges_v<1><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
+        k_edges_v<1><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
+        k_volume<0><<<nb, kCellBlock, 0, s>>>(a); mark();
+    } else {
+        for (int stage = 0; stage < 2; ++stage) {
+            KArgs a = base_args(ctx);
+            if (stage == 0) {
+                for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
+                for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->Y[k];
+            } else {
+                for (int k = 0; k < 6; ++k) a.W[k] = ctx->Y[k];
+                a.W[6] = ctx->X[6];
+                for (int k = 0; k < 6; ++k) { a.Wout[k] = ctx->X[k]; a.Xavg[k] = ctx->X[k]; }
+            }
+            k_recon<<<nb, kCellBlock, 0, s>>>(a); mark();
+            k_edges_h<true, 2><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
+            k_edges_h<false, 2><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
+            k_edges_v<2><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
+            k_edges_v<2><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
+            if (stage == 0) k_volume<1><<<nb, kCellBlock, 0, s>>>(a);
+            else k_volume<2><<<nb, kCellBlock, 0, s>>>(a);
+            mark();
+        }
+    }
+    k_advance<<<1, 1, 0, s>>>(ctx->tm); mark();
+    ctx->launches += nk;
+    int status = LSH_OK;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[nk]);
+    if (e != cudaSuccess) status = fail_cuda(e, "lsh_profile_step");
+    for (int k = 0; k < nk && k < cap && status == LSH_OK; ++k) cudaEventElapsedTime(&ms_out[k], ev[k], ev[k + 1]);
+    for (auto& ee : ev) cudaEventDestroy(ee);
+    if (n_kernels) *n_kernels = nk;
+    return status;
+}
+
+int lsh_probe_fp64_peak(int device, double* gflops) {
+    if (!gflops) return LSH_ERR_INVALID;
+    if (lsh_check_device() != 0) return LSH_ERR_NO_DEVICE;
+    if (device >= 0) LSH_CUDA(cudaSetDevice(device));
+    int dev = 0, sms = 0;
+    LSH_CUDA(cudaGetDevice(&dev));
+    LSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* out = nullptr;
+    LSH_CUDA(cudaMalloc(&out, sizeof(double)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    k_fp64_probe<<<blocks, threads>>>(out, 64, 1.0000001, 1e-9);  // warm-up
+    cudaEventRecord(e0);
+    k_fp64_probe<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail_cuda(e, "lsh_probe_fp64_peak");
+    const double flops = 2.0 * 8.0 * double(iters) * threads * blocks;
+    *gflops = flops / (ms * 1e-3) / 1e9;
+    return LSH_OK;
+}
+
+int lsh_get_launch_count(lsh_ctx* ctx, long long* launches) {
+    if (!ctx || !launches) return LSH_ERR_INVALID;
+    *launches = ctx->launches;
+    return LSH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,160 @@
+// lsh_fpmath.h -- the few elementary functions the scheme needs beyond
+// +, -, *, /, sqrt and fma, written so the host (CPU oracle) and the device
+// (CUDA kernels) produce bit-identical results: each one uses only IEEE-754
+// basic operations in a fixed order, never a vendor libm.
+//
+//   exp_neg(x) = e^-x, x >= 0.  Cody & Waite argument reduction
+//       (-x = k ln2 + r, ln2 split in a 32-bit-exact high part and a low
+//       part), e^r by its Taylor series to r^13/13! in Horner form, then a
+//       scaling by 2^k built from the exponent bits (two steps below 2^-1021
+//       so subnormal results round once).  Exactly 1 for x < 2^-54 and
+//       exactly 0 for x > 746 (what a correctly rounded exp returns there).
+//   cbrt_pos(x) = x^(1/3), x >= 0.  x = m 2^(3q + rem) with m in [1, 2);
+//       z ~ (m 2^rem)^(-1/3) from a quadratic first guess (4.4% error),
+//       4 Newton steps on f(z) = z^-3 - a (z <- z (4 - a z^3) / 3, no
+//       division), then y = a z^2 and one Newton step y += (a / y^2 - y) / 3.
+//   log_pos(x) = ln x, x > 0.  x = m 2^e with m in [sqrt(1/2), sqrt(2)),
+//       ln m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^23.
+// Accuracy: a few ulp (tests/test_fpmath.py checks them against the C
+// library); what matters here is that both sides compute the same bits.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define LSH_HD __host__ __device__ __forceinline__
+#else
+#define LSH_HD inline
+#endif
+
+namespace lshm {
+
+LSH_HD uint64_t bits_of(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    std::memcpy(&u, &x, sizeof(u));
+    return u;
+#endif
+}
+
+LSH_HD double from_bits(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    std::memcpy(&x, &u, sizeof(x));
+    return x;
+#endif
+}
+
+LSH_HD double fmad(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+    return fma(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+
+LSH_HD double rint_even(double x) {
+#if defined(__CUDA_ARCH__)
+    return rint(x);
+#else
+    return std::nearbyint(x);  // default rounding mode: to nearest, ties to even
+#endif
+}
+
+// 2^k for -1022 <= k <= 1023
+LSH_HD double pow2i(int k) { return from_bits((uint64_t)(k + 1023) << 52); }
+
+LSH_HD double exp_neg(double x) {
+    if (x < 0x1p-54) return (x == x) ? 1.0 : x;  // NaN stays NaN
+    if (x > 746.0) return 0.0;
+    const double inv_ln2 = 1.4426950408889634074;
+    const double ln2_hi = 6.93147180369123816490e-01;  // 0x3fe62e42fee00000: low 32 bits zero
+    const double ln2_lo = 1.90821492927058770002e-10;
+    const double kd = rint_even(-x * inv_ln2);
+    double r = fmad(kd, -ln2_hi, -x);
+    r = fmad(kd, -ln2_lo, r);
+    // Taylor coefficients 1/n!, n = 13 .. 2
+    double p = 1.6059043836821614599e-10;
+    p = fmad(p, r, 2.0876756987868098979e-09);
+    p = fmad(p, r, 2.5052108385441718775e-08);
+    p = fmad(p, r, 2.7557319223985890653e-07);
+    p = fmad(p, r, 2.7557319223985890653e-06);
+    p = fmad(p, r, 2.4801587301587301587e-05);
+    p = fmad(p, r, 1.9841269841269841270e-04);
+    p = fmad(p, r, 1.3888888888888888889e-03);
+    p = fmad(p, r, 8.3333333333333333333e-03);
+    p = fmad(p, r, 4.1666666666666666667e-02);
+    p = fmad(p, r, 1.6666666666666666667e-01);
+    p = fmad(p, r, 0.5);
+    p = fmad(p, r, 1.0);
+    p = fmad(p, r, 1.0);
+    const int k = (int)kd;
+    if (k >= -1021) return p * pow2i(k);
+    return (p * pow2i(k + 600)) * pow2i(-600);
+}
+
+LSH_HD double cbrt_pos(double x) {
+    if (!(x > 0.0)) return x;  // 0 -> 0, NaN -> NaN
+    if (x == INFINITY) return x;
+    int scale = 0;
+    if (x < 0x1p-1000) { x *= 0x1p300; scale = -100; }  // keep the exponent normal
+    const uint64_t u = bits_of(x);
+    const int e = (int)((u >> 52) & 0x7ff) - 1023;
+    const double m = from_bits((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);  // [1, 2)
+    int q = e / 3, rem = e - 3 * q;
+    if (rem < 0) { rem += 3; q -= 1; }
+    const double a = m * (double)(1 << rem);  // [1, 8)
+    double z = fmad(fmad(0.0115, a, -0.1656), a, 1.1098);
+    const double third = 1.0 / 3.0;
+    for (int i = 0; i < 4; ++i) {
+        const double z3 = z * z * z;
+        z = z * ((4.0 - a * z3) * third);
+    }
+    double y = a * z * z;
+    y = fmad(a / (y * y) - y, third, y);  // one Newton step on y^3 = a
+    return y * pow2i(q + scale);
+}
+
+LSH_HD double log_pos(double x) {
+    if (!(x > 0.0)) return (x == 0.0) ? -INFINITY : (x - x) / (x - x);
+    if (x == INFINITY) return x;
+    int scale = 0;
+    if (x < 0x1p-1000) { x *= 0x1p300; scale = -300; }
+    const uint64_t u = bits_of(x);
+    int e = (int)((u >> 52) & 0x7ff) - 1023;
+    double m = from_bits((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);  // [1, 2)
+    if (m > 1.4142135623730950488) { m *= 0.5; e += 1; }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double p = 1.0 / 23.0;
+    p = fmad(p, s2, 1.0 / 21.0);
+    p = fmad(p, s2, 1.0 / 19.0);
+    p = fmad(p, s2, 1.0 / 17.0);
+    p = fmad(p, s2, 1.0 / 15.0);
+    p = fmad(p, s2, 1.0 / 13.0);
+    p = fmad(p, s2, 1.0 / 11.0);
+    p = fmad(p, s2, 1.0 / 9.0);
+    p = fmad(p, s2, 1.0 / 7.0);
+    p = fmad(p, s2, 1.0 / 5.0);
+    p = fmad(p, s2, 1.0 / 3.0);
+    p = fmad(p, s2, 1.0);
+    const double lnm = 2.0 * s * p;
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    const double ed = (double)(e + scale);
+    return fmad(ed, ln2_hi, fmad(ed, ln2_lo, lnm));
+}
+
+// a^b for a > 0 (Pouliquen's (Fr/beta)^chi)
+LSH_HD double pow_pos(double a, double b) {
+    const double y = b * log_pos(a);
+    if (y <= 0.0) return exp_neg(-y);
+    return 1.0 / exp_neg(y);
+}
+
+}  // namespace lshm

@@ -1,0 +1,196 @@
+"""Python host mirror of the C ABI (include/lsh.h) over ctypes.
+
+The solver runs on the GPU through liblsh.so only: there is no CPU path.
+Constructing a :class:`Solver` without the built library, or without a CUDA
+device, raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import LSH_NVARS, VARS, LshParams
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblsh.so")
+
+_lib = None
+
+
+class LshError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = f"{what}: status {status}"
+        if _lib is not None:
+            msg += f" ({_lib.lsh_status_string(status).decode()}; {_lib.lsh_last_error().decode()})"
+        super().__init__(msg)
+
+
+P = ctypes.c_void_p
+DP = ctypes.POINTER(ctypes.c_double)
+
+# name -> (restype, argtypes); the list of every entry point include/lsh.h declares
+SIGNATURES = {
+    "lsh_params_default": (ctypes.c_int, [P]),
+    "lsh_check_device": (ctypes.c_int, []),
+    "lsh_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(P)]),
+    "lsh_destroy": (ctypes.c_int, [P]),
+    "lsh_set_stream": (ctypes.c_int, [P, P]),
+    "lsh_set_state": (ctypes.c_int, [P, P, DP]),
+    "lsh_set_state_device": (ctypes.c_int, [P, P, DP]),
+    "lsh_step": (ctypes.c_int, [P, ctypes.c_int]),
+    "lsh_run_until": (ctypes.c_int, [P, ctypes.c_double, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
+    "lsh_synchronize": (ctypes.c_int, [P]),
+    "lsh_get_state": (ctypes.c_int, [P, P]),
+    "lsh_get_state_device": (ctypes.c_int, [P, P]),
+    "lsh_get_time": (ctypes.c_int, [P, DP, DP, ctypes.POINTER(ctypes.c_longlong)]),
+    "lsh_get_eta_max": (ctypes.c_int, [P, P, P]),
+    "lsh_get_masks": (ctypes.c_int, [P, P]),
+    "lsh_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
+    "lsh_profile_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "lsh_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, DP]),
+    "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "lsh_last_error": (ctypes.c_char_p, []),
+}
+
+
+def load(path=LIB_PATH):
+    """Load liblsh.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with landslidehysea_gb300.build.build() "
+                           "(there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status, what):
+    if status != 0:
+        raise LshError(status, what)
+
+
+def _ptr_array(ptrs):
+    return (ctypes.c_void_p * LSH_NVARS)(*ptrs)
+
+
+def device_available():
+    return load().lsh_check_device() == 0
+
+
+def probe_fp64_peak(device=0):
+    """Measured FP64 FMA throughput of the device, GFLOP/s."""
+    g = ctypes.c_double()
+    _check(load().lsh_probe_fp64_peak(int(device), ctypes.byref(g)), "lsh_probe_fp64_peak")
+    return g.value
+
+
+class Solver:
+    """One solver context on one GPU (wraps lsh_ctx)."""
+
+    def __init__(self, params: LshParams, device: int = 0):
+        self.lib = load()
+        self.params = params.copy()
+        self.nx, self.ny = params.nx, params.ny
+        self._ctx = ctypes.c_void_p()
+        _check(self.lib.lsh_create(ctypes.byref(self.params), int(device), ctypes.byref(self._ctx)), "lsh_create")
+
+    def close(self):
+        if self._ctx:
+            self.lib.lsh_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---------------------------------------------------------------- state
+    def set_state(self, state):
+        """`state`: dict VARS -> array (ny, nx) or a list of 7 arrays.
+        Returns the initial dt."""
+        arrs = [np.ascontiguousarray(state[v] if isinstance(state, dict) else state[i], dtype=np.float64)
+                for i, v in enumerate(VARS)]
+        for a in arrs:
+            if a.size != self.nx * self.ny:
+                raise ValueError("state array size does not match nx*ny")
+        dt = ctypes.c_double()
+        _check(self.lib.lsh_set_state(self._ctx, _ptr_array([a.ctypes.data for a in arrs]), ctypes.byref(dt)),
+               "lsh_set_state")
+        return dt.value
+
+    def set_state_device(self, ptrs):
+        """`ptrs`: 7 device pointers (ints) of FP64 arrays on this device."""
+        dt = ctypes.c_double()
+        _check(self.lib.lsh_set_state_device(self._ctx, _ptr_array(list(ptrs)), ctypes.byref(dt)),
+               "lsh_set_state_device")
+        return dt.value
+
+    def get_state(self):
+        out = {v: np.empty((self.ny, self.nx), dtype=np.float64) for v in VARS}
+        _check(self.lib.lsh_get_state(self._ctx, _ptr_array([out[v].ctypes.data for v in VARS])), "lsh_get_state")
+        return out
+
+    def get_state_device(self, ptrs):
+        _check(self.lib.lsh_get_state_device(self._ctx, _ptr_array(list(ptrs))), "lsh_get_state_device")
+
+    # ---------------------------------------------------------------- time
+    def step(self, n=1):
+        _check(self.lib.lsh_step(self._ctx, int(n)), "lsh_step")
+
+    def synchronize(self):
+        _check(self.lib.lsh_synchronize(self._ctx), "lsh_synchronize")
+
+    def run_until(self, t_end, max_steps=0):
+        done = ctypes.c_longlong()
+        _check(self.lib.lsh_run_until(self._ctx, float(t_end), int(max_steps), ctypes.byref(done)), "lsh_run_until")
+        return done.value
+
+    def time(self):
+        t, dt, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        _check(self.lib.lsh_get_time(self._ctx, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(n)), "lsh_get_time")
+        return t.value, dt.value, n.value
+
+    def eta_max(self):
+        em = np.empty((self.ny, self.nx))
+        et = np.empty((self.ny, self.nx))
+        _check(self.lib.lsh_get_eta_max(self._ctx, em.ctypes.data, et.ctypes.data), "lsh_get_eta_max")
+        return em, et
+
+    def masks(self):
+        m = np.empty((self.ny, self.nx), dtype=np.uint8)
+        _check(self.lib.lsh_get_masks(self._ctx, m.ctypes.data), "lsh_get_masks")
+        return m
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        _check(self.lib.lsh_get_launch_count(self._ctx, ctypes.byref(n)), "lsh_get_launch_count")
+        return n.value
+
+    def profile_step(self):
+        """Run one step with per-kernel CUDA events; returns a list of ms."""
+        buf = (ctypes.c_float * 32)()
+        n = ctypes.c_int()
+        _check(self.lib.lsh_profile_step(self._ctx, buf, 32, ctypes.byref(n)), "lsh_profile_step")
+        return [buf[i] for i in range(n.value)]
+
+    def set_stream(self, stream_ptr):
+        _check(self.lib.lsh_set_stream(self._ctx, ctypes.c_void_p(stream_ptr)), "lsh_set_stream")
+
+
+__all__ = ["Solver", "LshError", "load", "device_available", "SIGNATURES", "_abi"]

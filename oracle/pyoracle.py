@@ -1,0 +1,141 @@
+"""TEST INFRASTRUCTURE -- ctypes access to the FP64 CPU oracle
+(oracle/_build/liblsh_oracle.so) and, where it was built, to the reference's
+own FP32 kernels run on the host (oracle/_ref/liblsh_ref.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
+module.  The product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liblsh_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "liblsh_ref.so")
+
+_lib = None
+_ref = None
+
+
+def build(force=False):
+    """Compile the oracle (a second or two)."""
+    if force or not os.path.exists(ORACLE_SO) or \
+            os.path.getmtime(ORACLE_SO) < os.path.getmtime(os.path.join(HERE, "lsh_oracle.cpp")):
+        subprocess.run(["sh", os.path.join(HERE, "build_oracle.sh")], check=True)
+    return ORACLE_SO
+
+
+def build_ref(reference_root="/root/reference"):
+    """Compile the reference's kernels for the host when its sources exist."""
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), reference_root], check=True)
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(ORACLE_SO)
+        P = ctypes.c_void_p
+        _lib.orc_initial_dt.argtypes = [P, P, ctypes.POINTER(ctypes.c_double)]
+        _lib.orc_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), P, P]
+        _lib.orc_masks.argtypes = [P, P, P]
+        _lib.orc_set_threads.argtypes = [ctypes.c_int]
+        _lib.orc_fpmath.argtypes = [ctypes.c_int, P, P, ctypes.c_longlong]
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError(REF_SO)
+        _ref = ctypes.CDLL(REF_SO)
+        f = ctypes.c_float
+        P = ctypes.c_void_p
+        _ref.lsh_ref_run.argtypes = [ctypes.c_int, ctypes.c_int, P] + [f] * 21 + [ctypes.c_int, P, P, P, P]
+    return _ref
+
+
+def _ptrs(arrays):
+    arr = (ctypes.c_void_p * len(arrays))(*[a.ctypes.data for a in arrays])
+    return arr
+
+
+def set_threads(n):
+    return lib().orc_set_threads(int(n))
+
+
+def state_arrays(state):
+    from landslidehysea_gb300._abi import VARS
+    return [np.ascontiguousarray(state[v], dtype=np.float64).copy() for v in VARS]
+
+
+def initial_dt(params, arrays):
+    dt = ctypes.c_double()
+    st = lib().orc_initial_dt(ctypes.byref(params), _ptrs(arrays), ctypes.byref(dt))
+    if st:
+        raise RuntimeError(f"orc_initial_dt status {st}")
+    return dt.value
+
+
+def run(params, arrays, nsteps, t=0.0, dt=None, t_end=-1.0, eta=None):
+    """Advance `arrays` (list of 7 float64 arrays, modified in place).  Returns
+    (t, dt_next, steps_done).  `eta` = (eta_max, eta_time) arrays or None."""
+    if dt is None:
+        dt = initial_dt(params, arrays)
+    tt = ctypes.c_double(t)
+    dd = ctypes.c_double(dt)
+    done = ctypes.c_longlong(0)
+    em = eta[0].ctypes.data if eta is not None else None
+    et = eta[1].ctypes.data if eta is not None else None
+    st = lib().orc_run(ctypes.byref(params), _ptrs(arrays), int(nsteps), float(t_end), ctypes.byref(tt),
+                       ctypes.byref(dd), ctypes.byref(done), em, et)
+    if st:
+        raise RuntimeError(f"orc_run status {st}")
+    return tt.value, dd.value, done.value
+
+
+def fpmath(which, x):
+    """Shared elementary functions: 'exp_neg', 'cbrt', 'log', 'pow1e-3'."""
+    code = {"exp_neg": 0, "cbrt": 1, "log": 2, "pow1e-3": 3}[which]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    if lib().orc_fpmath(code, x.ctypes.data, y.ctypes.data, x.size):
+        raise RuntimeError("orc_fpmath")
+    return y
+
+
+def masks(params, arrays):
+    out = np.zeros(arrays[0].shape, dtype=np.uint8)
+    lib().orc_masks(ctypes.byref(params), _ptrs(arrays), out.ctypes.data)
+    return out
+
+
+def ref_run(params, state, nsteps, eta=None):
+    """Run the reference's FP32 kernels (host build).  `state`: dict or list
+    of 7 arrays.  Returns (float32 arrays list, dt_trace, t)."""
+    from landslidehysea_gb300._abi import VARS
+    if isinstance(state, dict):
+        arrs = [np.ascontiguousarray(state[v], dtype=np.float32).copy() for v in VARS]
+    else:
+        arrs = [np.ascontiguousarray(a, dtype=np.float32).copy() for a in state]
+    trace = np.zeros(nsteps + 1, dtype=np.float32)
+    t = ctypes.c_float()
+    p = params
+    em = eta[0].ctypes.data if eta is not None else None
+    et = eta[1].ctypes.data if eta is not None else None
+    ref_lib().lsh_ref_run(p.nx, p.ny, _ptrs(arrs), p.borde_sup, p.borde_inf, p.borde_izq, p.borde_der,
+                          p.dx, p.dy, p.dx * p.dy, p.cfl, p.r, p.angle1, p.peso, p.beta, p.mfc, p.mf0, p.mfs,
+                          p.vmax1, p.vmax2, p.gravity, p.eps_h, p.L, p.H, int(nsteps), trace.ctypes.data,
+                          ctypes.byref(t), em, et)
+    return arrs, trace, t.value
