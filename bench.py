@@ -228,7 +228,10 @@ def run_ours(args):
 
     sc = workload(args.n)
     cells = sc.nx * sc.ny
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-legacy) stream shared by the library and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     s = Solver(sc.params, device=local)
     s.set_stream(stream.cuda_stream)
     s.set_state(sc.state)

@@ -66,22 +66,37 @@ struct KArgs {
 
 // ------------------------------------------------------------------ kernels
 
+// Depths of a face (first order: the cell's; second order: reconstructed).
 template <int ORDER>
-__device__ __forceinline__ void load_face(const KArgs& a, int id, int side, double W[6], double& Hf) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) W[k] = a.W[k][id];
+__device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, double& h1, double& h2) {
+    h1 = a.W[0][id];
+    h2 = a.W[3][id];
+    if (ORDER == 2) {
+        const double* const* s = (side < 2) ? a.sx : a.sy;
+        const double d1 = s[0][id] - s[3][id], d2 = s[3][id] + s[6][id];
+        // side & 1: the +slope face (E or N); the sign is a negation, not a multiply
+        h1 = h1 + ((side & 1) ? d1 : -d1);
+        h2 = h2 + ((side & 1) ? d2 : -d2);
+    }
+}
+
+// The rest of a face: discharges and bottom depth.
+template <int ORDER>
+__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, double W[6], double& Hf) {
+    W[1] = a.W[1][id];
+    W[2] = a.W[2][id];
+    W[4] = a.W[4][id];
+    W[5] = a.W[5][id];
     Hf = a.W[6][id];
     if (ORDER == 2) {
         const double* const* s = (side < 2) ? a.sx : a.sy;
-        const double sg = (side & 1) ? 1.0 : -1.0;
-        const double de1 = s[0][id], de2 = s[3][id], dH = s[6][id];
-        W[0] = W[0] + sg * (de1 - de2);
-        W[1] = W[1] + sg * s[1][id];
-        W[2] = W[2] + sg * s[2][id];
-        W[3] = W[3] + sg * (de2 + dH);
-        W[4] = W[4] + sg * s[4][id];
-        W[5] = W[5] + sg * s[5][id];
-        Hf = Hf + sg * dH;
+        const bool pos = (side & 1);
+        const double s1 = s[1][id], s2 = s[2][id], s4 = s[4][id], s5 = s[5][id], sH = s[6][id];
+        W[1] = W[1] + (pos ? s1 : -s1);
+        W[2] = W[2] + (pos ? s2 : -s2);
+        W[4] = W[4] + (pos ? s4 : -s4);
+        W[5] = W[5] + (pos ? s5 : -s5);
+        Hf = Hf + (pos ? sH : -sH);
     }
 }
 
@@ -109,22 +124,38 @@ __device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt)
         else { id0 = y * nx + x - 1; id1 = id0 + 1; e.nx = 1.0; side0 = 1; }
     }
     e.interior = (id1 >= 0);
-    load_face<ORDER>(a, id0, side0, e.W0, e.H0);
+    const int side1 = (DIR == 0) ? 2 : 0;
+    face_depths<ORDER>(a, id0, side0, e.W0[0], e.W0[3]);
+    if (e.interior) face_depths<ORDER>(a, id1, side1, e.W1[0], e.W1[3]);
+    else { e.W1[0] = e.W0[0]; e.W1[3] = e.W0[3]; }
+    // dry edge (Arista_kernel.cu:397): nothing to add; the first pass still
+    // writes the zeros that initialise the accumulators
+    if (!((0.5 * (e.W0[0] + e.W1[0]) >= lsh::kEps) || (0.5 * (e.W0[3] + e.W1[3]) >= lsh::kEps))) {
+        if (FIRST) {
+#pragma unroll
+            for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
+            if (e.interior) {
+#pragma unroll
+                for (int k = 0; k < 7; ++k) a.acc[k][id1] = 0.0;
+            }
+        }
+        return;
+    }
+    face_rest<ORDER>(a, id0, side0, e.W0, e.H0);
     e.area0 = a.geo.area[row0];
     e.hc0[0] = a.W[0][id0];
     e.hc0[1] = a.W[3][id0];
     if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
     else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
     if (e.interior) {
-        load_face<ORDER>(a, id1, (DIR == 0) ? 2 : 0, e.W1, e.H1);
+        face_rest<ORDER>(a, id1, side1, e.W1, e.H1);
         e.area1 = a.geo.area[row1];
         e.hc1[0] = a.W[0][id1];
         e.hc1[1] = a.W[3][id1];
         if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
         else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
     } else {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) e.W1[k] = e.W0[k];
+        e.W1[1] = e.W0[1]; e.W1[2] = e.W0[2]; e.W1[4] = e.W0[4]; e.W1[5] = e.W0[5];
         const int kn = (DIR == 0) ? 2 : 1;
         e.W1[kn] = e.W0[kn] * bor;
         e.W1[kn + 3] = e.W0[kn + 3] * bor;
@@ -201,6 +232,23 @@ __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nx * ny) return;
     const int j = id / nx, i = id - j * nx;
+    // A cell whose own and 4 neighbours' depths are all zero only meets dry
+    // edges (a dry cell's faces always have zero depth: any nonzero depth
+    // slope would make one face negative and trigger the fallback), so its
+    // slopes are never read: store zeros and skip the FP64 work.
+    {
+        using lsh::is_zero;
+        bool dry = is_zero(a.W[0][id]) && is_zero(a.W[3][id]);
+        if (dry && i > 0) dry = is_zero(a.W[0][id - 1]) && is_zero(a.W[3][id - 1]);
+        if (dry && i < nx - 1) dry = is_zero(a.W[0][id + 1]) && is_zero(a.W[3][id + 1]);
+        if (dry && j > 0) dry = is_zero(a.W[0][id - nx]) && is_zero(a.W[3][id - nx]);
+        if (dry && j < ny - 1) dry = is_zero(a.W[0][id + nx]) && is_zero(a.W[3][id + nx]);
+        if (dry) {
+#pragma unroll
+            for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
+            return;
+        }
+    }
     double sx[7], sy[7];
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
@@ -273,7 +321,20 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
             const double v = wo[0] - a.W[6][id];
             if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
         }
-        lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.tanR[j], dt, a.c);
+        // a dry, still cell with nothing flowing in maps to itself through the
+        // whole update (dt contribution 1e30): skip the FP64 work
+        bool still = true;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) still &= lsh::is_zero(wo[k]);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) still &= lsh::is_zero(acc[k]);
+        if (still) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = wo[k];
+            dti = lsh::kBig;
+        } else {
+            lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.tanR[j], dt, a.c);
+        }
         if (MODE == 2) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = 0.5 * (a.Xavg[k][id] + w[k]);

@@ -82,6 +82,9 @@ __device__ __forceinline__ double pow43(double h) { return h * lshm::cbrt_pos(h)
 
 __device__ __forceinline__ int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }
 
+// x == +0 or -0, by bit pattern (integer pipe)
+__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
 __device__ __forceinline__ bool is_bad(double x) {
     // NaN or Inf by bit pattern (integer pipe, no FP64 compare)
     return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
