@@ -149,6 +149,31 @@ int lsh_get_masks(lsh_ctx* ctx, uint8_t* host_mask);
  * (each graph replay counts its kernel nodes). */
 int lsh_get_launch_count(lsh_ctx* ctx, long long* launches);
 
+/* Allocation-free stepping.  No counterpart in the reference.
+ * For hosts that cannot allocate device memory: a coupling framework or plugin
+ * host that owns every byte of GPU memory through its own pool, code running
+ * while a stream is being captured into a CUDA graph (where cudaMalloc is not
+ * allowed), or a real-time loop that must not pay for an allocation.  The
+ * caller owns the state; this call only launches kernels.
+ * Advances the FIRST-ORDER step (order must be 1) `nsteps` times on the
+ * caller's DEVICE arrays dev_state[7] (h1 q1x q1y h2 q2x q2y H, nx*ny each,
+ * updated in place) on `cuda_stream` (NULL: the legacy default stream).
+ * *dt_io: the dt of the first step; <= 0 means "run the initial-dt pass
+ * first".  On return *t_io and *dt_io hold the time and the next step's dt
+ * (the call synchronises the stream to read them).  eta1 max is not tracked.
+ * Its accumulators, per-row geometry and time record live in one file-scope
+ * __device__ array sized for LSH_NOALLOC_MAX_CELLS cells and
+ * LSH_NOALLOC_MAX_ROWS rows (about 3.9 MB), which every GPU that loads the
+ * library holds until the process exits.  Larger grids are rejected with
+ * LSH_ERR_INVALID.  The first call on a device looks that array's device
+ * address up (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array, so calls that overlap on the GPU
+ * (other streams, other host threads) race: serialise them. */
+#define LSH_NOALLOC_MAX_CELLS 65536
+#define LSH_NOALLOC_MAX_ROWS  4096
+int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], int nsteps,
+                     double* t_io, double* dt_io, void* cuda_stream);
+
 /* Diagnostics (no counterpart in the reference).
  * lsh_profile_step: run ONE time step eagerly (not from a graph) with a CUDA
  * event between consecutive kernels on the context stream; ms_out[i] gets the

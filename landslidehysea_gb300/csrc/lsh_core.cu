@@ -1027,3 +1027,154 @@ int lsh_get_launch_count(lsh_ctx* ctx, long long* launches) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free stepping
+//
+// lsh_step_noalloc (include/lsh.h) runs the first-order step with all of its
+// scratch in the file-scope array below instead of allocated memory.  Layout
+// (doubles): 7 accumulators of LSH_NOALLOC_MAX_CELLS, then 6 per-row geometry
+// arrays of LSH_NOALLOC_MAX_ROWS + 1, then the 64-byte time record.  Host code
+// must not use the array's name as an address: the device address is looked
+// up once per device with cudaGetSymbolAddress (with that device current) and
+// passed to the kernels.
+
+namespace {
+
+constexpr size_t kNaAccStride = LSH_NOALLOC_MAX_CELLS;
+constexpr size_t kNaGeoStride = LSH_NOALLOC_MAX_ROWS + 1;
+constexpr size_t kNaGeoOffset = 7 * kNaAccStride;
+constexpr size_t kNaTimeOffset = (kNaGeoOffset + 6 * kNaGeoStride + 31) & ~size_t(31);
+constexpr size_t kNaDoubles = kNaTimeOffset + sizeof(TimeRec) / sizeof(double);
+
+__device__ __align__(256) double g_noalloc_scratch[kNaDoubles];
+
+constexpr int kNaMaxDevices = 64;
+double* g_noalloc_base[kNaMaxDevices] = {};
+std::mutex g_noalloc_mu;
+// host-side geometry staging for the upload (no heap allocation per call)
+double g_noalloc_geo_host[6 * kNaGeoStride];
+
+// Move the running min of per-cell dt into dt (initial-dt pass of a no-alloc call).
+__global__ void k_noalloc_take_dt(TimeRec* tm) {
+    tm->dt = __longlong_as_double((long long)tm->dtmin_bits);
+    tm->dtmin_bits = kDtInitBits;
+}
+
+// Same per-row formulas as make_geo, written into a caller-provided array.
+void noalloc_fill_geo(const lsh_params& p, double* g) {
+    double* area = g;
+    double* len_v = g + kNaGeoStride;
+    double* len_h = g + 2 * kNaGeoStride;
+    double* tanR = g + 3 * kNaGeoStride;
+    double* wx = g + 4 * kNaGeoStride;
+    double* wy = g + 5 * kNaGeoStride;
+    const int ny = p.ny;
+    if (p.coords == LSH_COORDS_SPHERICAL) {
+        const double d2r = kPi / 180.0;
+        const double R = p.radius, dl = p.dlon * d2r, dp = p.dlat * d2r;
+        for (int y = 0; y <= ny; ++y) len_h[y] = R * std::cos((p.lat0 + y * p.dlat) * d2r) * dl;
+        for (int j = 0; j < ny; ++j) {
+            const double ps = (p.lat0 + j * p.dlat) * d2r, pn = (p.lat0 + (j + 1) * p.dlat) * d2r;
+            const double pc = (p.lat0 + (j + 0.5) * p.dlat) * d2r;
+            area[j] = R * R * dl * (std::sin(pn) - std::sin(ps));
+            len_v[j] = R * dp;
+            tanR[j] = std::tan(pc) / R;
+            wx[j] = area[j] / (R * std::cos(pc) * dl);
+            wy[j] = area[j] / (R * dp);
+        }
+    } else {
+        for (int y = 0; y <= ny; ++y) len_h[y] = p.dx;
+        for (int j = 0; j < ny; ++j) {
+            area[j] = p.dx * p.dy;
+            len_v[j] = p.dy;
+            tanR[j] = 0.0;
+            wx[j] = p.dy;
+            wy[j] = p.dx;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], int nsteps,
+                                double* t_io, double* dt_io, void* cuda_stream) {
+    if (int s = check_params(p)) return s;
+    if (!dev_state || !t_io || !dt_io || nsteps < 0) { g_last_error = "lsh_step_noalloc: null pointer or nsteps < 0"; return LSH_ERR_INVALID; }
+    for (int k = 0; k < LSH_NVARS; ++k)
+        if (!dev_state[k]) { g_last_error = "lsh_step_noalloc: null state array"; return LSH_ERR_INVALID; }
+    if (p->order != 1) { g_last_error = "lsh_step_noalloc: only the first-order step (order 1) runs without allocation"; return LSH_ERR_INVALID; }
+    if ((long long)p->nx * p->ny > LSH_NOALLOC_MAX_CELLS || p->ny > LSH_NOALLOC_MAX_ROWS) {
+        g_last_error = "lsh_step_noalloc: grid larger than LSH_NOALLOC_MAX_CELLS (65536) cells or LSH_NOALLOC_MAX_ROWS (4096) rows";
+        return LSH_ERR_INVALID;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    int dev = 0;
+    LSH_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNaMaxDevices) { g_last_error = "lsh_step_noalloc: device index out of range"; return LSH_ERR_INVALID; }
+    if (!g_noalloc_base[dev]) {
+        double* base = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&base), g_noalloc_scratch);
+        if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_base[dev] = base;
+    }
+    double* base = g_noalloc_base[dev];
+
+    noalloc_fill_geo(*p, g_noalloc_geo_host);
+    LSH_CUDA(cudaMemcpyAsync(base + kNaGeoOffset, g_noalloc_geo_host, 6 * kNaGeoStride * sizeof(double),
+                             cudaMemcpyHostToDevice, s));
+    TimeRec* tm = reinterpret_cast<TimeRec*>(base + kNaTimeOffset);
+    TimeRec init{};
+    init.t = *t_io;
+    init.dt = *dt_io;
+    init.t_end = INFINITY;
+    init.dt_min = p->dt_min;
+    init.dtmin_bits = kDtInitBits;
+    LSH_CUDA(cudaMemcpyAsync(tm, &init, sizeof(TimeRec), cudaMemcpyHostToDevice, s));
+
+    KArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.c = make_consts(*p);
+    a.c.track_eta = 0;
+    const double* g = base + kNaGeoOffset;
+    a.geo.area = g;
+    a.geo.len_v = g + kNaGeoStride;
+    a.geo.len_h = g + 2 * kNaGeoStride;
+    a.geo.tanR = g + 3 * kNaGeoStride;
+    a.geo.wx = g + 4 * kNaGeoStride;
+    a.geo.wy = g + 5 * kNaGeoStride;
+    for (int k = 0; k < 7; ++k) { a.W[k] = dev_state[k]; a.acc[k] = base + k * kNaAccStride; }
+    for (int k = 0; k < 6; ++k) a.Wout[k] = dev_state[k];
+    a.tm = tm;
+
+    const int nx = p->nx, ny = p->ny;
+    const unsigned nb = unsigned((size_t(nx) * ny + kCellBlock - 1) / kCellBlock);
+    if (!(*dt_io > 0.0)) {
+        // initial dt (ShallowWater.cu:236-257) into the time record
+        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
+        k_noalloc_take_dt<<<1, 1, 0, s>>>(tm);
+    }
+    const dim3 gh0((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535));
+    const dim3 gh1((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535));
+    const dim3 gv0((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535));
+    const dim3 gv1(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535));
+    for (int i = 0; i < nsteps; ++i) {
+        k_edges_h<true, 1><<<gh0, kEdgeBlock, 0, s>>>(a, 0);
+        k_edges_h<false, 1><<<gh1, kEdgeBlock, 0, s>>>(a, 1);
+        k_edges_v<1><<<gv0, kEdgeBlock, 0, s>>>(a, 0);
+        k_edges_v<1><<<gv1, kEdgeBlock, 0, s>>>(a, 1);
+        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+        k_advance<<<1, 1, 0, s>>>(tm);
+    }
+    LSH_CUDA(cudaGetLastError());
+    TimeRec out{};
+    LSH_CUDA(cudaMemcpyAsync(&out, tm, sizeof(TimeRec), cudaMemcpyDeviceToHost, s));
+    LSH_CUDA(cudaStreamSynchronize(s));
+    *t_io = out.t;
+    *dt_io = out.dt;
+    return err_bits_to_status(out.err);
+}

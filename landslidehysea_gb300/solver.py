@@ -51,6 +51,7 @@ SIGNATURES = {
     "lsh_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_profile_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsh_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, DP]),
+    "lsh_step_noalloc": (ctypes.c_int, [P, P, ctypes.c_int, DP, DP, P]),
     "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "lsh_last_error": (ctypes.c_char_p, []),
 }
