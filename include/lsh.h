@@ -72,6 +72,10 @@ typedef struct lsh_params {
     int32_t coords;          /* LSH_COORDS_*                                          */
     int32_t friction_law;    /* LSH_FRICTION_* (reference #define COULOMB)            */
     int32_t track_eta_max;   /* 1: update eta1 max / time every step (A18)            */
+    int32_t eig_sort;        /* 0: the reference's compare-and-swap sequence for the  */
+                             /*    eigenvalue bounds (Arista_kernel.cu:193-234, with  */
+                             /*    its (2,1) compare: not a full sort); 1: a true     */
+                             /*    ascending sort (mass-exact at walls, see DESIGN)   */
     double dx, dy;           /* Cartesian cell width / height (ancho_vol, alto_vol)   */
     double lon0, lat0;       /* spherical: corner longitude / latitude, degrees       */
     double dlon, dlat;       /* spherical: cell size, degrees                         */

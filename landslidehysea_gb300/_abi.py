@@ -29,6 +29,7 @@ class LshParams(ctypes.Structure):
         ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
         ("order", ctypes.c_int32), ("coords", ctypes.c_int32),
         ("friction_law", ctypes.c_int32), ("track_eta_max", ctypes.c_int32),
+        ("eig_sort", ctypes.c_int32),
         ("dx", ctypes.c_double), ("dy", ctypes.c_double),
         ("lon0", ctypes.c_double), ("lat0", ctypes.c_double),
         ("dlon", ctypes.c_double), ("dlat", ctypes.c_double),
@@ -64,6 +65,7 @@ def default_params(nx=1, ny=1, **kw):
     p.coords = COORDS_CARTESIAN
     p.friction_law = FRICTION_COULOMB
     p.track_eta_max = 0
+    p.eig_sort = 0
     p.dx = p.dy = 1.0
     p.lon0 = p.lat0 = 0.0
     p.dlon = p.dlat = 0.0

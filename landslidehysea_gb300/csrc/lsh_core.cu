@@ -508,6 +508,7 @@ int check_params(const lsh_params* p) {
     if (p->order != 1 && p->order != 2) { g_last_error = "order must be 1 or 2"; return LSH_ERR_INVALID; }
     if (p->coords != LSH_COORDS_CARTESIAN && p->coords != LSH_COORDS_SPHERICAL) { g_last_error = "bad coords"; return LSH_ERR_INVALID; }
     if (p->friction_law != LSH_FRICTION_COULOMB && p->friction_law != LSH_FRICTION_POULIQUEN) { g_last_error = "bad friction law"; return LSH_ERR_INVALID; }
+    if (p->eig_sort != 0 && p->eig_sort != 1) { g_last_error = "eig_sort must be 0 or 1"; return LSH_ERR_INVALID; }
     if (!(p->eps_h > 0) || !(p->gravity > 0) || !(p->r >= 0 && p->r < 1) || !(p->peso > 0) || !(p->cfl > 0) || !(p->H > 0) || !(p->L > 0)) {
         g_last_error = "eps_h, gravity, peso, cfl, L, H must be > 0 and 0 <= r < 1";
         return LSH_ERR_INVALID;
@@ -531,6 +532,7 @@ Consts make_consts(const lsh_params& p) {
     c.tan1 = std::tan(p.angle1); c.tan2 = std::tan(p.angle2); c.tan3 = std::tan(p.angle3); c.tan4 = std::tan(p.angle4);
     c.borde_sup = p.borde_sup; c.borde_inf = p.borde_inf; c.borde_izq = p.borde_izq; c.borde_der = p.borde_der;
     c.law = p.friction_law; c.order = p.order; c.nx = p.nx; c.ny = p.ny; c.track_eta = p.track_eta_max;
+    c.eig_sort = p.eig_sort;
     return c;
 }
 

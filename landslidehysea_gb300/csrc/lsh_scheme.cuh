@@ -39,7 +39,7 @@ struct Consts {
     int order;
     int nx, ny;
     int track_eta;
-    int pad_;
+    int eig_sort;
 };
 
 // Per-row geometry (device arrays, ny or ny+1 entries).
@@ -90,15 +90,17 @@ __device__ __forceinline__ bool is_bad(double x) {
     return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
 }
 
-// Compare-and-swap sequence of Arista_kernel.cu:193-234 (with its (2,1) compare).
-__device__ __forceinline__ void sort_eig(V4<double>& D) {
+// Compare-and-swap sequence of Arista_kernel.cu:193-234 (with its (2,1)
+// compare) or, with `full`, the same sequence made a true sort.
+__device__ __forceinline__ void sort_eig(V4<double>& D, int full) {
     double t;
     if (D.x > D.y) { t = D.y; D.y = D.x; D.x = t; }
     if (D.x > D.z) { t = D.z; D.z = D.x; D.x = t; }
     if (D.x > D.w) { t = D.w; D.w = D.x; D.x = t; }
     if (D.y > D.z) { t = D.z; D.z = D.y; D.y = t; }
     if (D.y > D.w) { t = D.w; D.w = D.y; D.y = t; }
-    if (D.z > D.y) { t = D.y; D.y = D.z; D.z = t; }
+    if (full) { if (D.y > D.z) { t = D.z; D.z = D.y; D.y = t; } }
+    else if (D.z > D.y) { t = D.y; D.y = D.z; D.z = t; }
     if (D.z > D.w) { t = D.w; D.w = D.z; D.z = t; }
 }
 
@@ -115,7 +117,7 @@ __device__ __forceinline__ V4<double> eig_core(double h1, double h2, double u1, 
     const double aux = 1.0 - d * d * F / c.gp;
     const double ci = sqrt(c.gp * h1 * h2 * F * fabs(aux));
     V4<double> D{u - cg, uu - ci, uu + ci, u + cg};
-    sort_eig(D);
+    sort_eig(D, c.eig_sort);
     return D;
 }
 

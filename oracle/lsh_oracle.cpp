@@ -62,6 +62,7 @@ struct Consts {
     double g, r, gp, eps_h, peso, beta, cfl, mu, mfc, mf0, mfs, vmax1, vmax2, L, H;
     double tan1, tan2, tan3, tan4;
     int law;
+    int eig_sort;
 };
 
 struct Geo {
@@ -83,6 +84,7 @@ static Consts make_consts(const lsh_params& p) {
     c.L = p.L; c.H = p.H;
     c.tan1 = tan(p.angle1); c.tan2 = tan(p.angle2); c.tan3 = tan(p.angle3); c.tan4 = tan(p.angle4);
     c.law = p.friction_law;
+    c.eig_sort = p.eig_sort;
     return c;
 }
 
@@ -139,11 +141,13 @@ inline int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }  
 template <class T> struct V4 { T x, y, z, w; };
 
 // The fixed compare-and-swap sequence of Arista_kernel.cu:193-234, including
-// its (i=2, j=1) compare, which leaves the larger of y/z in y.
-template <class T> inline void sort_eig(V4<T>& D) {
+// its (i=2, j=1) compare, which leaves the larger of y/z in y (eig_sort 0);
+// with eig_sort 1 that compare is (1,2) and the sequence is a true sort.
+template <class T> inline void sort_eig(V4<T>& D, int full) {
     auto cs = [](T& a, T& b) { if (a > b) { T t = b; b = a; a = t; } };
     cs(D.x, D.y); cs(D.x, D.z); cs(D.x, D.w); cs(D.y, D.z); cs(D.y, D.w);
-    if (D.z > D.y) { T t = D.y; D.y = D.z; D.z = t; }
+    if (full) cs(D.y, D.z);
+    else if (D.z > D.y) { T t = D.y; D.y = D.z; D.z = t; }
     cs(D.z, D.w);
 }
 
@@ -164,7 +168,7 @@ inline V4<T> eig(const T& h1, const T& a1, const T& h2, const T& a2, bool conser
     const T aux = 1.0 - d * d * F / c.gp;
     const T ci = sqrt(c.gp * h1 * h2 * F * fabs(aux));
     V4<T> D{u - cg, uu - ci, uu + ci, u + cg};
-    sort_eig(D);
+    sort_eig(D, c.eig_sort);
     return D;
 }
 

@@ -48,6 +48,10 @@ def case(name):
         p.order = 2
         p.cfl = 0.45
         return p, st, 20
+    if name == "shelf48_o2_fullsort":
+        sc = scenarios.shelf(n=48, dx=25.0 * 200 / 48, order=2, cfl=0.5)
+        sc.params.eig_sort = 1
+        return sc.params, sc.state, 60
     if name == "pouliquen":
         p, st = golden_case("slope")
         p.friction_law = 1
@@ -57,7 +61,7 @@ def case(name):
 
 
 PARITY_CASES = ["shelf48_o1", "golden_random17x9", "golden_dam1d", "golden_column", "golden_slope",
-                "golden_shelf40", "shelf40x24_o2", "random_o2", "fjord64_o2", "fjord64_o1_sph", "pouliquen"]
+                "golden_shelf40", "shelf40x24_o2", "random_o2", "fjord64_o2", "fjord64_o1_sph", "pouliquen", "shelf48_o2_fullsort"]
 
 
 def rel_linf(a, b):
