@@ -80,24 +80,31 @@ __device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, do
     }
 }
 
-// The rest of a face: discharges and bottom depth.
-template <int ORDER>
-__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, double W[6], double& Hf) {
-    W[1] = a.W[1][id];
-    W[2] = a.W[2][id];
-    W[4] = a.W[4][id];
-    W[5] = a.W[5][id];
-    Hf = a.W[6][id];
+// The rest of a face in the edge frame.  DIR 1 (vertical edge, normal
+// (sg, 0)): qn = sg qx, qt = sg qy; DIR 0 (horizontal, normal (0, sg)):
+// qn = sg qy, qt = -sg qx (Arista_kernel.cu:363-371, 509-525) -- selections
+// and negations, no FP64 arithmetic.
+template <int DIR, int ORDER>
+__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Face& f) {
+    double qx1 = a.W[1][id], qy1 = a.W[2][id], qx2 = a.W[4][id], qy2 = a.W[5][id], H = a.W[6][id];
     if (ORDER == 2) {
         const double* const* s = (side < 2) ? a.sx : a.sy;
         const bool pos = (side & 1);
         const double s1 = s[1][id], s2 = s[2][id], s4 = s[4][id], s5 = s[5][id], sH = s[6][id];
-        W[1] = W[1] + (pos ? s1 : -s1);
-        W[2] = W[2] + (pos ? s2 : -s2);
-        W[4] = W[4] + (pos ? s4 : -s4);
-        W[5] = W[5] + (pos ? s5 : -s5);
-        Hf = Hf + (pos ? sH : -sH);
+        qx1 = qx1 + (pos ? s1 : -s1);
+        qy1 = qy1 + (pos ? s2 : -s2);
+        qx2 = qx2 + (pos ? s4 : -s4);
+        qy2 = qy2 + (pos ? s5 : -s5);
+        H = H + (pos ? sH : -sH);
     }
+    if (DIR == 1) {
+        f.qn1 = pos_normal ? qx1 : -qx1; f.qt1 = pos_normal ? qy1 : -qy1;
+        f.qn2 = pos_normal ? qx2 : -qx2; f.qt2 = pos_normal ? qy2 : -qy2;
+    } else {
+        f.qn1 = pos_normal ? qy1 : -qy1; f.qt1 = pos_normal ? -qx1 : qx1;
+        f.qn2 = pos_normal ? qy2 : -qy2; f.qt2 = pos_normal ? -qx2 : qx2;
+    }
+    f.H = H;
 }
 
 // One edge: gather both sides, evaluate, scatter to the accumulators.
@@ -106,31 +113,30 @@ __device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, doub
 template <int DIR, bool FIRST, int ORDER>
 __device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt) {
     const int nx = a.c.nx, ny = a.c.ny;
-    EdgeIn e;
+    lsh::EdgeIn e;
     int id0, id1 = -1, side0, row0, row1 = 0;
     double bor = 0.0;
+    bool pos_normal = true;
     if (DIR == 0) {
         e.len = a.geo.len_h[y];
-        e.nx = 0.0;
-        if (y == 0) { id0 = x; row0 = 0; e.ny = -1.0; bor = a.c.borde_sup; side0 = 2; }
-        else if (y == ny) { id0 = (ny - 1) * nx + x; row0 = ny - 1; e.ny = 1.0; bor = a.c.borde_inf; side0 = 3; }
-        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; row0 = y - 1; row1 = y; e.ny = 1.0; side0 = 3; }
+        if (y == 0) { id0 = x; row0 = 0; pos_normal = false; bor = a.c.borde_sup; side0 = 2; }
+        else if (y == ny) { id0 = (ny - 1) * nx + x; row0 = ny - 1; bor = a.c.borde_inf; side0 = 3; }
+        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; row0 = y - 1; row1 = y; side0 = 3; }
     } else {
         e.len = a.geo.len_v[y];
-        e.ny = 0.0;
         row0 = row1 = y;
-        if (x == 0) { id0 = y * nx; e.nx = -1.0; bor = a.c.borde_izq; side0 = 0; }
-        else if (x == nx) { id0 = y * nx + nx - 1; e.nx = 1.0; bor = a.c.borde_der; side0 = 1; }
-        else { id0 = y * nx + x - 1; id1 = id0 + 1; e.nx = 1.0; side0 = 1; }
+        if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; side0 = 0; }
+        else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; side0 = 1; }
+        else { id0 = y * nx + x - 1; id1 = id0 + 1; side0 = 1; }
     }
     e.interior = (id1 >= 0);
     const int side1 = (DIR == 0) ? 2 : 0;
-    face_depths<ORDER>(a, id0, side0, e.W0[0], e.W0[3]);
-    if (e.interior) face_depths<ORDER>(a, id1, side1, e.W1[0], e.W1[3]);
-    else { e.W1[0] = e.W0[0]; e.W1[3] = e.W0[3]; }
+    face_depths<ORDER>(a, id0, side0, e.A.h1, e.A.h2);
+    if (e.interior) face_depths<ORDER>(a, id1, side1, e.B.h1, e.B.h2);
+    else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
     // dry edge (Arista_kernel.cu:397): nothing to add; the first pass still
     // writes the zeros that initialise the accumulators
-    if (!((0.5 * (e.W0[0] + e.W1[0]) >= lsh::kEps) || (0.5 * (e.W0[3] + e.W1[3]) >= lsh::kEps))) {
+    if (!((0.5 * (e.A.h1 + e.B.h1) >= lsh::kEps) || (0.5 * (e.A.h2 + e.B.h2) >= lsh::kEps))) {
         if (FIRST) {
 #pragma unroll
             for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
@@ -141,49 +147,74 @@ __device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt)
         }
         return;
     }
-    face_rest<ORDER>(a, id0, side0, e.W0, e.H0);
+    face_rest<DIR, ORDER>(a, id0, side0, pos_normal, e.A);
     e.area0 = a.geo.area[row0];
+    e.inv_area0 = a.geo.inv_area[row0];
     e.hc0[0] = a.W[0][id0];
     e.hc0[1] = a.W[3][id0];
     if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
     else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
     if (e.interior) {
-        face_rest<ORDER>(a, id1, side1, e.W1, e.H1);
+        face_rest<DIR, ORDER>(a, id1, side1, pos_normal, e.B);
         e.area1 = a.geo.area[row1];
+        e.inv_area1 = a.geo.inv_area[row1];
         e.hc1[0] = a.W[0][id1];
         e.hc1[1] = a.W[3][id1];
         if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
         else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
     } else {
-        e.W1[1] = e.W0[1]; e.W1[2] = e.W0[2]; e.W1[4] = e.W0[4]; e.W1[5] = e.W0[5];
-        const int kn = (DIR == 0) ? 2 : 1;
-        e.W1[kn] = e.W0[kn] * bor;
-        e.W1[kn + 3] = e.W0[kn + 3] * bor;
-        e.H1 = e.H0;
+        // ghost: the cell's face with the normal discharges times the boundary factor
+        e.B = e.A;
+        e.B.qn1 = e.A.qn1 * bor;
+        e.B.qn2 = e.A.qn2 * bor;
         e.area1 = e.area0;
+        e.inv_area1 = e.inv_area0;
         e.hc1[0] = e.hc1[1] = 0.0;
         e.acc1h[0] = e.acc1h[1] = 0.0;
     }
-    double d0[6], d1[6], wave;
-    const bool wet = lsh::edge_flux(e, dt, a.c, d0, d1, wave);
+    lsh::EdgeOut o;
+    using lsh::is_zero;
+    if (is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2))
+        lsh::edge_flux<false>(e, dt, a.c, o);
+    else
+        lsh::edge_flux<true>(e, dt, a.c, o);
+    // back to x/y: DIR 1: (qx, qy) = sg (fn, ft); DIR 0: qx = -sg ft, qy = sg fn
+    double d0[6], d1[6];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const int k = 3 * l;
+        d0[k] = o.m[k];
+        d1[k] = o.p[k];
+        if (DIR == 1) {
+            d0[k + 1] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
+            d0[k + 2] = pos_normal ? o.m[k + 2] : -o.m[k + 2];
+            d1[k + 1] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
+            d1[k + 2] = pos_normal ? o.p[k + 2] : -o.p[k + 2];
+        } else {
+            d0[k + 1] = pos_normal ? -o.m[k + 2] : o.m[k + 2];
+            d0[k + 2] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
+            d1[k + 1] = pos_normal ? -o.p[k + 2] : o.p[k + 2];
+            d1[k + 2] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
+        }
+    }
     if (FIRST) {
         // every cell meets exactly one hor-even edge: write, do not accumulate
 #pragma unroll
-        for (int k = 0; k < 6; ++k) a.acc[k][id0] = wet ? (0.0 - d0[k]) : 0.0;
-        a.acc[6][id0] = wet ? (0.0 + wave) : 0.0;
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] = 0.0 - d0[k];
+        a.acc[6][id0] = 0.0 + o.wave;
         if (e.interior) {
 #pragma unroll
-            for (int k = 0; k < 6; ++k) a.acc[k][id1] = wet ? (0.0 - d1[k]) : 0.0;
-            a.acc[6][id1] = wet ? (0.0 + wave) : 0.0;
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] = 0.0 - d1[k];
+            a.acc[6][id1] = 0.0 + o.wave;
         }
-    } else if (wet) {
+    } else {
 #pragma unroll
         for (int k = 0; k < 6; ++k) a.acc[k][id0] -= d0[k];
-        a.acc[6][id0] += wave;
+        a.acc[6][id0] += o.wave;
         if (e.interior) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) a.acc[k][id1] -= d1[k];
-            a.acc[6][id1] += wave;
+            a.acc[6][id1] += o.wave;
         }
     }
 }
@@ -305,24 +336,14 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
         for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
 #pragma unroll
         for (int k = 0; k < 7; ++k) acc[k] = a.acc[k][id];
-        if (a.c.order == 2) {
-            // cell-midpoint integral of g h d(eta) over the reconstructed cell
-            const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
-            const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
-            const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
-            const double wx = a.geo.wx[j], wy = a.geo.wy[j];
-            acc[1] -= a.c.peso * (gh1 * e1x * wx);
-            acc[4] -= a.c.peso * (gh2 * ((1.0 - a.c.r) * e2x + a.c.r * e1x) * wx);
-            acc[2] -= a.c.peso * (gh1 * e1y * wy);
-            acc[5] -= a.c.peso * (gh2 * ((1.0 - a.c.r) * e2y + a.c.r * e1y) * wy);
-        }
         if (MODE != 2 && a.c.track_eta) {
             // actualizarEta1MaximaGPU (Volumen_kernel.cu:182-213): state before the step
             const double v = wo[0] - a.W[6][id];
             if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
         }
         // a dry, still cell with nothing flowing in maps to itself through the
-        // whole update (dt contribution 1e30): skip the FP64 work
+        // whole update (dt contribution 1e30; its second-order pressure
+        // integral is g*0*... = 0): skip the FP64 work
         bool still = true;
 #pragma unroll
         for (int k = 0; k < 6; ++k) still &= lsh::is_zero(wo[k]);
@@ -333,7 +354,18 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
             for (int k = 0; k < 6; ++k) w[k] = wo[k];
             dti = lsh::kBig;
         } else {
-            lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.tanR[j], dt, a.c);
+            if (a.c.order == 2) {
+                // cell-midpoint integral of g h d(eta) over the reconstructed cell
+                const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
+                const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
+                const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
+                const double wx = a.geo.wx[j], wy = a.geo.wy[j];
+                acc[1] -= a.c.peso * ((gh1 * e1x) * wx);
+                acc[4] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2x, a.c.r * e1x)) * wx);
+                acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
+                acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
+            }
+            lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
         }
         if (MODE == 2) {
 #pragma unroll
@@ -374,34 +406,33 @@ __global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
         if (DIR == 0) { x = tid; y = par + 2 * bl; if (x >= nx) return; }
         else { x = par + 2 * tid; y = bl; if (tid >= nlines) return; }
         int id0, id1 = -1;
-        double nxv, nyv, bor = 0.0, len;
+        double bor = 0.0, len;
+        bool pos_normal = true;
         if (DIR == 0) {
             len = a.geo.len_h[y];
-            nxv = 0.0;
-            if (y == 0) { id0 = x; nyv = -1.0; bor = a.c.borde_sup; }
-            else if (y == ny) { id0 = (ny - 1) * nx + x; nyv = 1.0; bor = a.c.borde_inf; }
-            else { id0 = (y - 1) * nx + x; id1 = id0 + nx; nyv = 1.0; }
+            if (y == 0) { id0 = x; pos_normal = false; bor = a.c.borde_sup; }
+            else if (y == ny) { id0 = (ny - 1) * nx + x; bor = a.c.borde_inf; }
+            else { id0 = (y - 1) * nx + x; id1 = id0 + nx; }
         } else {
             len = a.geo.len_v[y];
-            nyv = 0.0;
-            if (x == 0) { id0 = y * nx; nxv = -1.0; bor = a.c.borde_izq; }
-            else if (x == nx) { id0 = y * nx + nx - 1; nxv = 1.0; bor = a.c.borde_der; }
-            else { id0 = y * nx + x - 1; id1 = id0 + 1; nxv = 1.0; }
+            if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; }
+            else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; }
+            else { id0 = y * nx + x - 1; id1 = id0 + 1; }
         }
-        double W0[6], W1[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) W0[k] = a.W[k][id0];
+        lsh::Face A, B;
+        A.h1 = a.W[0][id0];
+        A.h2 = a.W[3][id0];
+        face_rest<DIR, 1>(a, id0, 0, pos_normal, A);
         if (id1 >= 0) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) W1[k] = a.W[k][id1];
+            B.h1 = a.W[0][id1];
+            B.h2 = a.W[3][id1];
+            face_rest<DIR, 1>(a, id1, 0, pos_normal, B);
         } else {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) W1[k] = W0[k];
-            const int kn = (DIR == 0) ? 2 : 1;
-            W1[kn] = W0[kn] * bor;
-            W1[kn + 3] = W0[kn + 3] * bor;
+            B = A;
+            B.qn1 = A.qn1 * bor;
+            B.qn2 = A.qn2 * bor;
         }
-        const double wv = lsh::edge_initial_wave(W0, W1, nxv, nyv, len, a.c);
+        const double wv = lsh::edge_initial_wave(A, B, len, a.c);
         if (FIRST) {
             a.acc[6][id0] = 0.0 + wv;
             if (id1 >= 0) a.acc[6][id1] = 0.0 + wv;
@@ -420,7 +451,7 @@ __global__ void __launch_bounds__(kCellBlock) k_cell_dt(KArgs a) {
     if (id < nx * ny) {
         const int j = id / nx;
         const double w = a.acc[6][id];
-        const double d = (w < lsh::kEps) ? lsh::kBig : (2.0 * a.c.cfl * a.geo.area[j]) / w;
+        const double d = (w < lsh::kEps) ? lsh::kBig : ((2.0 * a.c.cfl) * a.geo.area[j]) / w;
         bits = (unsigned long long)__double_as_longlong(d);
     }
     block_min_bits(bits, a.tm);
@@ -531,6 +562,13 @@ Consts make_consts(const lsh_params& p) {
     c.L = p.L; c.H = p.H;
     c.tan1 = std::tan(p.angle1); c.tan2 = std::tan(p.angle2); c.tan3 = std::tan(p.angle3); c.tan4 = std::tan(p.angle4);
     c.borde_sup = p.borde_sup; c.borde_inf = p.borde_inf; c.borde_izq = p.borde_izq; c.borde_der = p.borde_der;
+    c.omr = 1.0 - p.r;
+    c.inv_gp = 1.0 / c.gp;
+    c.inv_eps = 1.0 / p.eps_h;
+    c.inv_peso = 1.0 / p.peso;
+    c.eps_1r = p.eps_h * (1.0 + p.r);
+    c.g_mf02 = (p.gravity * p.mf0) * p.mf0;
+    c.g_mfs2 = (p.gravity * p.mfs) * p.mfs;
     c.law = p.friction_law; c.order = p.order; c.nx = p.nx; c.ny = p.ny; c.track_eta = p.track_eta_max;
     c.eig_sort = p.eig_sort;
     return c;
@@ -538,7 +576,8 @@ Consts make_consts(const lsh_params& p) {
 
 // Per-row geometry on the host (same formulas as the CPU oracle).
 void make_geo(const lsh_params& p, std::vector<double>& area, std::vector<double>& len_v, std::vector<double>& len_h,
-              std::vector<double>& tanR, std::vector<double>& wx, std::vector<double>& wy) {
+              std::vector<double>& tanR, std::vector<double>& wx, std::vector<double>& wy,
+              std::vector<double>& inv_area) {
     const int ny = p.ny;
     area.resize(ny); len_v.resize(ny); len_h.resize(ny + 1); tanR.resize(ny); wx.resize(ny); wy.resize(ny);
     if (p.coords == LSH_COORDS_SPHERICAL) {
@@ -564,6 +603,8 @@ void make_geo(const lsh_params& p, std::vector<double>& area, std::vector<double
             wy[j] = p.dx;
         }
     }
+    inv_area.resize(ny);
+    for (int j = 0; j < ny; ++j) inv_area[j] = 1.0 / area[j];
 }
 
 KArgs base_args(const lsh_ctx* ctx) {
@@ -773,7 +814,7 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     // one slab: X(7) + Y(6) + acc(7) + eta(2) [+ sx, sy (14)] arrays of N, geometry, time record
     const size_t n_pad = (ctx->N + 31) & ~size_t(31);  // 256-byte aligned arrays
     const int n_arrays = 7 + 6 + 7 + 2 + ((p->order == 2) ? 14 : 0);
-    const size_t geo_n = size_t(6) * (p->ny + 1);
+    const size_t geo_n = size_t(7) * (p->ny + 1);
     const size_t bytes = (size_t(n_arrays) * n_pad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) + 256;
     {
         cudaError_t e = cudaMalloc(&ctx->slab, bytes);
@@ -795,8 +836,8 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     cur += (geo_n + 31) & ~size_t(31);
     ctx->tm = reinterpret_cast<TimeRec*>(cur);
 
-    std::vector<double> area, len_v, len_h, tanR, wx, wy;
-    make_geo(*p, area, len_v, len_h, tanR, wx, wy);
+    std::vector<double> area, len_v, len_h, tanR, wx, wy, inv_area;
+    make_geo(*p, area, len_v, len_h, tanR, wx, wy, inv_area);
     std::vector<double> g(geo_n, 0.0);
     const size_t st = size_t(p->ny + 1);
     std::copy(area.begin(), area.end(), g.begin());
@@ -805,6 +846,7 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     std::copy(tanR.begin(), tanR.end(), g.begin() + 3 * st);
     std::copy(wx.begin(), wx.end(), g.begin() + 4 * st);
     std::copy(wy.begin(), wy.end(), g.begin() + 5 * st);
+    std::copy(inv_area.begin(), inv_area.end(), g.begin() + 6 * st);
     {
         cudaError_t e = cudaMemcpy(ctx->geo_buf, g.data(), geo_n * sizeof(double), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy geometry"));
@@ -815,6 +857,7 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     ctx->geo.tanR = ctx->geo_buf + 3 * st;
     ctx->geo.wx = ctx->geo_buf + 4 * st;
     ctx->geo.wy = ctx->geo_buf + 5 * st;
+    ctx->geo.inv_area = ctx->geo_buf + 6 * st;
     ctx->kernels_per_step = (p->order == 1) ? 6 : 13;
     *out = ctx;
     return LSH_OK;
@@ -1045,7 +1088,7 @@ namespace {
 constexpr size_t kNaAccStride = LSH_NOALLOC_MAX_CELLS;
 constexpr size_t kNaGeoStride = LSH_NOALLOC_MAX_ROWS + 1;
 constexpr size_t kNaGeoOffset = 7 * kNaAccStride;
-constexpr size_t kNaTimeOffset = (kNaGeoOffset + 6 * kNaGeoStride + 31) & ~size_t(31);
+constexpr size_t kNaTimeOffset = (kNaGeoOffset + 7 * kNaGeoStride + 31) & ~size_t(31);
 constexpr size_t kNaDoubles = kNaTimeOffset + sizeof(TimeRec) / sizeof(double);
 
 __device__ __align__(256) double g_noalloc_scratch[kNaDoubles];
@@ -1054,7 +1097,7 @@ constexpr int kNaMaxDevices = 64;
 double* g_noalloc_base[kNaMaxDevices] = {};
 std::mutex g_noalloc_mu;
 // host-side geometry staging for the upload (no heap allocation per call)
-double g_noalloc_geo_host[6 * kNaGeoStride];
+double g_noalloc_geo_host[7 * kNaGeoStride];
 
 // Move the running min of per-cell dt into dt (initial-dt pass of a no-alloc call).
 __global__ void k_noalloc_take_dt(TimeRec* tm) {
@@ -1070,6 +1113,7 @@ void noalloc_fill_geo(const lsh_params& p, double* g) {
     double* tanR = g + 3 * kNaGeoStride;
     double* wx = g + 4 * kNaGeoStride;
     double* wy = g + 5 * kNaGeoStride;
+    double* inv_area = g + 6 * kNaGeoStride;
     const int ny = p.ny;
     if (p.coords == LSH_COORDS_SPHERICAL) {
         const double d2r = kPi / 180.0;
@@ -1094,6 +1138,7 @@ void noalloc_fill_geo(const lsh_params& p, double* g) {
             wy[j] = p.dx;
         }
     }
+    for (int j = 0; j < ny; ++j) inv_area[j] = 1.0 / area[j];
 }
 
 }  // namespace
@@ -1123,7 +1168,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     double* base = g_noalloc_base[dev];
 
     noalloc_fill_geo(*p, g_noalloc_geo_host);
-    LSH_CUDA(cudaMemcpyAsync(base + kNaGeoOffset, g_noalloc_geo_host, 6 * kNaGeoStride * sizeof(double),
+    LSH_CUDA(cudaMemcpyAsync(base + kNaGeoOffset, g_noalloc_geo_host, 7 * kNaGeoStride * sizeof(double),
                              cudaMemcpyHostToDevice, s));
     TimeRec* tm = reinterpret_cast<TimeRec*>(base + kNaTimeOffset);
     TimeRec init{};
@@ -1145,6 +1190,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     a.geo.tanR = g + 3 * kNaGeoStride;
     a.geo.wx = g + 4 * kNaGeoStride;
     a.geo.wy = g + 5 * kNaGeoStride;
+    a.geo.inv_area = g + 6 * kNaGeoStride;
     for (int k = 0; k < 7; ++k) { a.W[k] = dev_state[k]; a.acc[k] = base + k * kNaAccStride; }
     for (int k = 0; k < 6; ++k) a.Wout[k] = dev_state[k];
     a.tm = tm;

@@ -34,6 +34,8 @@ constexpr double kBig = 1e30;
 struct Consts {
     double g, r, gp, eps_h, peso, beta, cfl, mu, mfc, mf0, mfs, vmax1, vmax2, L, H;
     double tan1, tan2, tan3, tan4;
+    // host-derived, with the same formulas as the CPU oracle's make_consts
+    double omr, inv_gp, inv_eps, inv_peso, eps_1r, g_mf02, g_mfs2;
     double borde_sup, borde_inf, borde_izq, borde_der;
     int law;
     int order;
@@ -45,6 +47,7 @@ struct Consts {
 // Per-row geometry (device arrays, ny or ny+1 entries).
 struct Geo {
     const double* area;   // [ny]
+    const double* inv_area;  // [ny]
     const double* len_v;  // [ny]
     const double* len_h;  // [ny+1]
     const double* tanR;   // [ny]
@@ -64,18 +67,18 @@ struct TimeRec {
     int err;                         // sticky error bits (LSH status values as bits)
 };
 
-template <class T> struct V4 { T x, y, z, w; };
+struct V4 { double x, y, z, w; };
 
 __device__ __forceinline__ double tmin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double tmax(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double max0(double a) { return (a > 0.0) ? a : 0.0; }
-
+__device__ __forceinline__ double fmad(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ double exp_neg(double x) { return lshm::exp_neg(x); }
 
 __device__ __forceinline__ double vfac(double h, double eps_h) {
     const double m = (h > eps_h) ? h : eps_h;
     const double h2 = h * h, m2 = m * m;
-    return (kSqrt2 * h) / sqrt(h2 * h2 + m2 * m2);
+    return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
 __device__ __forceinline__ double pow43(double h) { return h * lshm::cbrt_pos(h); }
@@ -92,7 +95,7 @@ __device__ __forceinline__ bool is_bad(double x) {
 
 // Compare-and-swap sequence of Arista_kernel.cu:193-234 (with its (2,1)
 // compare) or, with `full`, the same sequence made a true sort.
-__device__ __forceinline__ void sort_eig(V4<double>& D, int full) {
+__device__ __forceinline__ void sort_eig(V4& D, int full) {
     double t;
     if (D.x > D.y) { t = D.y; D.y = D.x; D.x = t; }
     if (D.x > D.z) { t = D.z; D.z = D.x; D.x = t; }
@@ -104,19 +107,23 @@ __device__ __forceinline__ void sort_eig(V4<double>& D, int full) {
     if (D.z > D.w) { t = D.w; D.w = D.z; D.z = t; }
 }
 
-// aproximarAutovalores1D: (u1, u2) velocities and the factor vfac(h1 + h2)
-// already known; returns the sorted 4 estimates.
-__device__ __forceinline__ V4<double> eig_core(double h1, double h2, double u1, double u2, double q,
-                                               const Consts& c) {
-    const double h = h1 + h2;
+// aproximarAutovalores1D (Arista_kernel.cu:152-237).  L2 == false: the
+// granular layer is absent (h2 = 0, u2 = 0), so the internal pair is exactly
+// zero and its square root is skipped.
+template <bool L2>
+__device__ __forceinline__ V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c) {
+    const double h = L2 ? h1 + h2 : h1;
     const double F = vfac(h, c.eps_h);
     const double u = q * F;
     const double cg = sqrt(c.g * h);
-    const double uu = (u1 * h2 + u2 * h1) * F;
-    const double d = u1 - u2;
-    const double aux = 1.0 - d * d * F / c.gp;
-    const double ci = sqrt(c.gp * h1 * h2 * F * fabs(aux));
-    V4<double> D{u - cg, uu - ci, uu + ci, u + cg};
+    double uu = 0.0, ci = 0.0;
+    if (L2) {
+        uu = fmad(u1, h2, u2 * h1) * F;
+        const double d = u1 - u2;
+        const double aux = fmad(-((d * d) * F), c.inv_gp, 1.0);
+        ci = sqrt((((c.gp * h1) * h2) * F) * fabs(aux));
+    }
+    V4 D{u - cg, uu - ci, uu + ci, u + cg};
     sort_eig(D, c.eig_sort);
     return D;
 }
@@ -124,152 +131,198 @@ __device__ __forceinline__ V4<double> eig_core(double h1, double h2, double u1, 
 // defTerminoFriccion (Arista_kernel.cu:11-58)
 __device__ __forceinline__ double friction_mu(double h1, double u1, double h2, double u2, const Consts& c) {
     if (c.law == 0) return c.mu;
-    const double a = 10.0 * h1 / c.eps_h;
+    const double a = (10.0 * h1) * c.inv_eps;
     const double rr = 1.0 - c.r * (1.0 - exp_neg(a * a));
     const double gp = c.g * rr;
-    const double fr1 = u1 * u1 * vfac(h1, c.eps_h) / gp;
-    const double fr2 = u2 * u2 * vfac(h2, c.eps_h) / gp;
-    const double fr = sqrt(fr1 + fr2 + (1.0 - rr) * fr1 * fr2);
-    const double beta = 0.136, L2 = 8.0e-4, chi = 1.0e-3;
-    const double mustop = c.tan1 + (c.tan2 - c.tan1) / (1.0 + h2 / L2);
-    const double mustart = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2);
+    const double fr1 = ((u1 * u1) * vfac(h1, c.eps_h)) / gp;
+    const double fr2 = ((u2 * u2) * vfac(h2, c.eps_h)) / gp;
+    const double fr = sqrt(fmad((1.0 - rr) * fr1, fr2, fr1 + fr2));
+    const double beta = 0.136, L2c = 8.0e-4, chi = 1.0e-3;
+    const double mustop = c.tan1 + (c.tan2 - c.tan1) / (1.0 + h2 / L2c);
+    const double mustart = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2c);
     double muf;
-    if (fr > beta) muf = c.tan1 + (c.tan2 - c.tan1) / (1.0 + beta * h2 / (fr * L2));
-    else if (fabs(fr) < kEps) muf = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2);
-    else muf = mustart + lshm::pow_pos(fr / beta, chi) * (mustop - mustart);
-    return muf * c.L / c.H;
+    if (fr > beta) muf = c.tan1 + (c.tan2 - c.tan1) / (1.0 + beta * h2 / (fr * L2c));
+    else if (fabs(fr) < kEps) muf = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2c);
+    else muf = fmad(lshm::pow_pos(fr / beta, chi), mustop - mustart, mustart);
+    return (muf * c.L) / c.H;
 }
 
 __device__ __forceinline__ double fsc_of(double h1, const Consts& c) {
-    const double a = 10.0 * h1 / c.eps_h;
+    const double a = (10.0 * h1) * c.inv_eps;
     return 1.0 - c.r * (1.0 - exp_neg(a * a));
 }
 
-// Inputs of one edge (see the CPU oracle's EdgeIn for the meaning).
+// One face state in the edge's normal frame: depth, normal and tangential
+// discharge of each layer, bottom depth.
+struct Face { double h1, qn1, qt1, h2, qn2, qt2, H; };
+
+// Inputs of one edge (the CPU oracle's EdgeIn): the two facing states A, B,
+// cell-average depths and partial accumulators for the positivity limiter.
 struct EdgeIn {
-    double W0[6], W1[6];
-    double H0, H1;
-    double nx, ny, len, area0, area1;
+    Face A, B;
+    double len, area0, area1, inv_area0, inv_area1;
     double hc0[2], hc1[2];
     double acc0h[2], acc1h[2];
     bool interior;
 };
 
-// procesarArista: returns false for a dry edge; otherwise d0/d1 (to subtract
-// from the two cells' accumulators) and the wave term.
-__device__ __forceinline__ bool edge_flux(const EdgeIn& e, double dt, const Consts& c, double d0[6],
-                                          double d1[6], double& wave) {
-    const double nx = e.nx, ny = e.ny, eps = c.eps_h;
-    V4<double> A{e.W0[0], e.W0[1] * nx + e.W0[2] * ny, e.W0[3], e.W0[4] * nx + e.W0[5] * ny};
-    V4<double> B{e.W1[0], e.W1[1] * nx + e.W1[2] * ny, e.W1[3], e.W1[4] * nx + e.W1[5] * ny};
-    const double H0 = e.H0, H1 = e.H1;
+// Normal-frame output: per layer (mass, normal momentum, tangential
+// momentum) to subtract from cell 0 (m) and cell 1 (p), and the wave term.
+struct EdgeOut { double m[6], p[6]; double wave; };
 
-    // the edge is dry when both averaged depths are below EPSILON (:397); the
-    // depths do not depend on the discharges, so test before any heavy work
-    const double h1ij = 0.5 * (A.x + B.x);
-    const double h2ij = 0.5 * (A.z + B.z);
-    if (!((h1ij >= kEps) || (h2ij >= kEps))) return false;
+// procesarArista (Arista_kernel.cu:324-645), the depths already known to be
+// wet (the caller skips dry edges, :397).  L2 == false: both faces have no
+// granular layer (h2 = qn2 = 0); every layer-1 value is then the same as in
+// the general path and every layer-2 output is zero, so that work is skipped.
+template <bool L2>
+__device__ __forceinline__ void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
+    const double eps = c.eps_h;
+    double Aq1 = e.A.qn1, Aq2 = L2 ? e.A.qn2 : 0.0, Bq1 = e.B.qn1, Bq2 = L2 ? e.B.qn2 : 0.0;
+    const double Ah1 = e.A.h1, Bh1 = e.B.h1;
+    const double Ah2 = L2 ? e.A.h2 : 0.0, Bh2 = L2 ? e.B.h2 : 0.0;
+    const double H0 = e.A.H, H1 = e.B.H;
+    const double h1ij = 0.5 * (Ah1 + Bh1);
+    const double h2ij = L2 ? 0.5 * (Ah2 + Bh2) : 0.0;
 
-    if ((A.z < eps) && (H1 - B.z > H0)) B.w = 0.0;
-    if ((B.z < eps) && (H0 - A.z > H1)) A.w = 0.0;
-    if ((A.x < eps) && (H1 - B.x - B.z > H0 - A.z)) B.y = 0.0;
-    if ((B.x < eps) && (H0 - A.x - A.z > H1 - B.z)) A.y = 0.0;
-    if ((A.z + A.x < eps) && (H1 - B.x - B.z > H0)) { B.y = 0.0; B.w = 0.0; }
-    if ((B.z + B.x < eps) && (H0 - A.x - A.z > H1)) { A.y = 0.0; A.w = 0.0; }
+    // tratamientoSecoMojado (Arista_kernel.cu:301-321)
+    if (L2) {
+        if ((Ah2 < eps) && (H1 - Bh2 > H0)) Bq2 = 0.0;
+        if ((Bh2 < eps) && (H0 - Ah2 > H1)) Aq2 = 0.0;
+        if ((Ah1 < eps) && (H1 - Bh1 - Bh2 > H0 - Ah2)) Bq1 = 0.0;
+        if ((Bh1 < eps) && (H0 - Ah1 - Ah2 > H1 - Bh2)) Aq1 = 0.0;
+        if ((Ah2 + Ah1 < eps) && (H1 - Bh1 - Bh2 > H0)) { Bq1 = 0.0; Bq2 = 0.0; }
+        if ((Bh2 + Bh1 < eps) && (H0 - Ah1 - Ah2 > H1)) { Aq1 = 0.0; Aq2 = 0.0; }
+    } else {
+        if ((Ah1 < eps) && (H1 - Bh1 > H0)) Bq1 = 0.0;
+        if ((Bh1 < eps) && (H0 - Ah1 > H1)) Aq1 = 0.0;
+    }
 
-    const double fA1 = vfac(A.x, eps), fB1 = vfac(B.x, eps);
-    const double fA2 = vfac(A.z, eps), fB2 = vfac(B.z, eps);
-    double sa = sqrt(A.x), sb = sqrt(B.x);
-    const double u1ij = (sa * (fA1 * A.y) + sb * (fB1 * B.y)) / (sa + sb + kEps);
-    sa = sqrt(A.z); sb = sqrt(B.z);
-    const double u2ij = (sa * (fA2 * A.w) + sb * (fB2 * B.w)) / (sa + sb + kEps);
+    const double fA1 = vfac(Ah1, eps), fB1 = vfac(Bh1, eps);
+    const double fA2 = L2 ? vfac(Ah2, eps) : 0.0, fB2 = L2 ? vfac(Bh2, eps) : 0.0;
+    double sa = sqrt(Ah1), sb = sqrt(Bh1);
+    const double u1ij = fmad(sa, fA1 * Aq1, sb * (fB1 * Bq1)) / (sa + sb + kEps);
+    double u2ij = 0.0;
+    if (L2) {
+        sa = sqrt(Ah2); sb = sqrt(Bh2);
+        u2ij = fmad(sa, fA2 * Aq2, sb * (fB2 * Bq2)) / (sa + sb + kEps);
+    }
 
     const double Hm = tmin(H0, H1);
-    const double deta1 = max0(B.x + B.z - H1 + Hm) - max0(A.x + A.z - H0 + Hm);
-    const double deta2 = max0(B.z - H1 + Hm) - max0(A.z - H0 + Hm);
-    const V4<double> tp{0.0, c.g * h1ij * deta1, 0.0, c.g * h2ij * ((1.0 - c.r) * deta2 + c.r * deta1)};
+    const double deta1 = L2 ? max0(Bh1 + Bh2 - H1 + Hm) - max0(Ah1 + Ah2 - H0 + Hm)
+                            : max0(Bh1 - H1 + Hm) - max0(Ah1 - H0 + Hm);
+    const double deta2 = L2 ? max0(Bh2 - H1 + Hm) - max0(Ah2 - H0 + Hm) : 0.0;
+    const double gh1 = c.g * h1ij, gh2 = c.g * h2ij;
+    const V4 tp{0.0, gh1 * deta1, 0.0, L2 ? gh2 * fmad(c.omr, deta2, c.r * deta1) : 0.0};
 
-    const double mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
-    const double sc = fsc_of(h1ij, c) * mu * c.g * h2ij;
-    const bool coul = fabs(h2ij * u2ij) < c.peso * sc * dt;
-    V4<double> tp2 = tp;
-    if (coul) tp2.w = c.g * h2ij * c.r * deta1;
+    bool coul = false;
+    V4 tp2 = tp;
+    if (L2) {
+        const double mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
+        const double sc = ((fsc_of(h1ij, c) * mu) * c.g) * h2ij;
+        coul = fabs(h2ij * u2ij) < (c.peso * sc) * dt;
+        if (coul) tp2.w = (gh2 * c.r) * deta1;
+    }
 
-    const V4<double> D = eig_core(h1ij, h2ij, u1ij, u2ij, h1ij * u1ij + h2ij * u2ij, c);
-    const V4<double> E0 = eig_core(A.x, A.z, fA1 * A.y, fA2 * A.w, A.y + A.w, c);
-    const V4<double> E1 = eig_core(B.x, B.z, fB1 * B.y, fB2 * B.w, B.y + B.w, c);
+    const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, L2 ? fmad(h1ij, u1ij, h2ij * u2ij) : h1ij * u1ij, c);
+    const V4 E0 = eig<L2>(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, L2 ? Aq1 + Aq2 : Aq1, c);
+    const V4 E1 = eig<L2>(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, L2 ? Bq1 + Bq2 : Bq1, c);
     const double aut1 = tmin(D.x, tmin(E0.x, E1.x));
     const double aut3 = tmax(D.w, tmax(E0.w, E1.w));
     double lmax = tmax(fabs(aut3), fabs(aut1));
-    const double umax = tmax(fabs(u1ij), fabs(u2ij));
+    const double umax = L2 ? tmax(fabs(u1ij), fabs(u2ij)) : fabs(u1ij);
     if (umax > lmax) lmax = umax;
     double aut2 = tmax(fabs(D.y), fabs(D.z));
     if (sgn(aut1 + aut3) < 0) aut2 = -aut2;
 
-    double a0, a1, a2;
+    double a0, a1, a2 = 0.0;
     if ((fabs(aut1 - aut3) >= kEps) && (fabs(aut1 - aut2) >= kEps) && (fabs(aut2 - aut3) >= kEps)) {
-        if ((h1ij >= eps) && (h2ij >= eps)) {
-            const double a = fabs(aut1) / ((aut1 - aut3) * (aut1 - aut2));
-            const double b = fabs(aut2) / ((aut2 - aut1) * (aut2 - aut3));
-            const double cc = fabs(aut3) / ((aut3 - aut1) * (aut3 - aut2));
-            a0 = a * aut2 * aut3 + b * aut1 * aut3 + cc * aut1 * aut2;
-            a1 = -a * (aut2 + aut3) - b * (aut1 + aut3) - cc * (aut1 + aut2);
+        if (L2 && (h1ij >= eps) && (h2ij >= eps)) {
+            const double d12 = aut1 - aut2, d13 = aut1 - aut3, d23 = aut2 - aut3;
+            const double inv = 1.0 / ((d12 * d13) * d23);
+            const double a = (fabs(aut1) * d23) * inv;
+            const double b = -((fabs(aut2) * d13) * inv);
+            const double cc = (fabs(aut3) * d12) * inv;
+            a0 = fmad(a * aut2, aut3, fmad(b * aut1, aut3, (cc * aut1) * aut2));
+            a1 = -fmad(a, aut2 + aut3, fmad(b, aut1 + aut3, cc * (aut1 + aut2)));
             a2 = a + b + cc;
         } else {
-            a0 = (aut3 * fabs(aut1) - aut1 * fabs(aut3)) / (aut3 - aut1);
-            a1 = (fabs(aut3) - fabs(aut1)) / (aut3 - aut1);
-            a2 = 0.0;
+            const double inv = 1.0 / (aut3 - aut1);
+            a0 = fmad(aut3, fabs(aut1), -(aut1 * fabs(aut3))) * inv;
+            a1 = (fabs(aut3) - fabs(aut1)) * inv;
         }
     } else {
-        a0 = lmax; a1 = 0.0; a2 = 0.0;
+        a0 = lmax; a1 = 0.0;
     }
 
-    const V4<double> FA{A.y, (A.x < kEps) ? 0.0 : (fA1 * A.y) * A.y, A.w, (A.z < kEps) ? 0.0 : (fA2 * A.w) * A.w};
-    const V4<double> FB{B.y, (B.x < kEps) ? 0.0 : (fB1 * B.y) * B.y, B.w, (B.z < kEps) ? 0.0 : (fB2 * B.w) * B.w};
-    const V4<double> dF{FB.x - FA.x, FB.y - FA.y, FB.z - FA.z, FB.w - FA.w};
-    tp2 = V4<double>{tp2.x + dF.x, tp2.y + dF.y, tp2.z + dF.z, tp2.w + dF.w};
-    const V4<double> half{0.5 * (dF.x + tp.x), 0.5 * (dF.y + tp.y), 0.5 * (dF.z + tp.z), 0.5 * (dF.w + tp.w)};
+    const double FAy = (Ah1 < kEps) ? 0.0 : (fA1 * Aq1) * Aq1, FBy = (Bh1 < kEps) ? 0.0 : (fB1 * Bq1) * Bq1;
+    const double dFx = Bq1 - Aq1, dFy = FBy - FAy;
+    double dFz = 0.0, dFw = 0.0, FAw = 0.0, FBw = 0.0;
+    if (L2) {
+        FAw = (Ah2 < kEps) ? 0.0 : (fA2 * Aq2) * Aq2;
+        FBw = (Bh2 < kEps) ? 0.0 : (fB2 * Bq2) * Bq2;
+        dFz = Bq2 - Aq2;
+        dFw = FBw - FAw;
+    }
+    tp2 = V4{tp2.x + dFx, tp2.y + dFy, tp2.z + dFz, tp2.w + dFw};
+    const double half_x = 0.5 * (dFx + tp.x), half_y = 0.5 * (dFy + tp.y);
 
-    const double ga = c.g * h1ij, gb = c.g * h2ij;
-    const V4<double> At{tp2.y, (ga - u1ij * u1ij) * tp2.x + 2.0 * u1ij * tp2.y + ga * tp2.z, tp2.w,
-                        c.r * gb * tp2.x + (gb - u2ij * u2ij) * tp2.z + 2.0 * u2ij * tp2.w};
+    const double Atx = tp2.y;
+    const double Aty = fmad(gh1, tp2.z, fmad(u1ij + u1ij, tp2.y, fmad(-u1ij, u1ij, gh1) * tp2.x));
 
-    V4<double> I{deta1, B.y - A.y, 0.0, B.w - A.w};
+    V4 I{deta1, Bq1 - Aq1, 0.0, Bq2 - Aq2};
     if (!coul) {
-        if ((A.x > eps) && (B.x > eps)) I.x = I.x - deta2;
+        if ((Ah1 > eps) && (Bh1 > eps)) I.x = I.x - deta2;
         I.z = deta2;
     }
 
-    const V4<double> Q{0.5 * (a0 * I.x + a1 * tp2.x + a2 * At.x), 0.5 * (a0 * I.y + a1 * tp2.y + a2 * At.y),
-                       0.5 * (a0 * I.z + a1 * tp2.z + a2 * At.z), 0.5 * (a0 * I.w + a1 * tp2.w + a2 * At.w)};
-    const V4<double> Fm{half.x + (FA.x - Q.x), half.y + (FA.y - Q.y), half.z + (FA.z - Q.z), half.w + (FA.w - Q.w)};
-    const V4<double> Fp{half.x + (Q.x - FB.x), half.y + (Q.y - FB.y), half.z + (Q.z - FB.z), half.w + (Q.w - FB.w)};
+    double Qx, Qy;
+    if (L2) {
+        Qx = 0.5 * fmad(a0, I.x, fmad(a1, tp2.x, a2 * Atx));
+        Qy = 0.5 * fmad(a0, I.y, fmad(a1, tp2.y, a2 * Aty));
+    } else {
+        Qx = 0.5 * fmad(a0, I.x, a1 * tp2.x);
+        Qy = 0.5 * fmad(a0, I.y, a1 * tp2.y);
+    }
+    const double Fmx = half_x + (Aq1 - Qx), Fmy = half_y + (FAy - Qy);
+    const double Fpx = half_x + (Qx - Bq1), Fpy = half_y + (Qy - FBy);
 
-    const double ut0 = fA1 * (e.W0[2] * nx - e.W0[1] * ny), ut1 = fB1 * (e.W1[2] * nx - e.W1[1] * ny);
-    const double u1t = (fabs(Fm.x) < kEps) ? 0.0 : ((Fm.x > 0.0) ? ut0 : ut1);
-    const double vt0 = fA2 * (e.W0[5] * nx - e.W0[4] * ny), vt1 = fB2 * (e.W1[5] * nx - e.W1[4] * ny);
-    const double u2t = (fabs(Fm.z) < kEps) ? 0.0 : ((Fm.z > 0.0) ? vt0 : vt1);
-
-    const double s1 = Fm.x * u1t, s2 = Fm.z * u2t;
-    double P[6] = {Fp.x, Fp.y * nx + s1 * ny, Fp.y * ny - s1 * nx, Fp.z, Fp.w * nx + s2 * ny, Fp.w * ny - s2 * nx};
-    double M[6] = {Fm.x, Fm.y * nx - s1 * ny, Fm.y * ny + s1 * nx, Fm.z, Fm.w * nx - s2 * ny, Fm.w * ny + s2 * nx};
+    const double u1t = (fabs(Fmx) < kEps) ? 0.0 : ((Fmx > 0.0) ? fA1 * e.A.qt1 : fB1 * e.B.qt1);
+    const double s1 = Fmx * u1t;
+    double M[6] = {Fmx, Fmy, s1, 0.0, 0.0, 0.0};
+    double P[6] = {Fpx, Fpy, -s1, 0.0, 0.0, 0.0};
+    if (L2) {
+        const double Atz = tp2.w;
+        const double Atw = fmad(c.r * gh2, tp2.x, fmad(fmad(-u2ij, u2ij, gh2), tp2.z, (u2ij + u2ij) * tp2.w));
+        const double Qz = 0.5 * fmad(a0, I.z, fmad(a1, tp2.z, a2 * Atz));
+        const double Qw = 0.5 * fmad(a0, I.w, fmad(a1, tp2.w, a2 * Atw));
+        const double half_z = 0.5 * (dFz + tp.z), half_w = 0.5 * (dFw + tp.w);
+        const double Fmz = half_z + (Aq2 - Qz), Fmw = half_w + (FAw - Qw);
+        const double Fpz = half_z + (Qz - Bq2), Fpw = half_w + (Qw - FBw);
+        const double u2t = (fabs(Fmz) < kEps) ? 0.0 : ((Fmz > 0.0) ? fA2 * e.A.qt2 : fB2 * e.B.qt2);
+        const double s2 = Fmz * u2t;
+        M[3] = Fmz; M[4] = Fmw; M[5] = s2;
+        P[3] = Fpz; P[4] = Fpw; P[5] = -s2;
+    }
+    constexpr int KL = L2 ? 6 : 3;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) { P[k] = e.len * P[k]; M[k] = e.len * M[k]; }
+    for (int k = 0; k < KL; ++k) { P[k] = e.len * P[k]; M[k] = e.len * M[k]; }
 
-    const double b0 = dt / e.area0;
-    const double hp00 = e.hc0[0] + b0 * e.acc0h[0], hp01 = e.hc0[1] + b0 * e.acc0h[1];
+    const double b0 = dt * e.inv_area0;
+    const double hp00 = fmad(b0, e.acc0h[0], e.hc0[0]);
+    const double hp01 = L2 ? fmad(b0, e.acc0h[1], e.hc0[1]) : 0.0;
     double hp10 = 0.0, hp11 = 0.0;
     if (e.interior) {
-        const double b1 = dt / e.area1;
-        hp10 = e.hc1[0] + b1 * e.acc1h[0]; hp11 = e.hc1[1] + b1 * e.acc1h[1];
+        const double b1 = dt * e.inv_area1;
+        hp10 = fmad(b1, e.acc1h[0], e.hc1[0]);
+        if (L2) hp11 = fmad(b1, e.acc1h[1], e.hc1[1]);
     }
     const double factor = 1.0 * c.beta;
 #pragma unroll
-    for (int layer = 0; layer < 2; ++layer) {
+    for (int layer = 0; layer < (L2 ? 2 : 1); ++layer) {
         const int k = 3 * layer;
         double dta = kBig, dtb = kBig;
-        if (M[k] > 0.0) dta = (layer ? hp01 : hp00) * e.area0 / (factor * M[k] + kEps);
-        if (e.interior && P[k] > 0.0) dtb = (layer ? hp11 : hp10) * e.area1 / (factor * P[k] + kEps);
+        if (M[k] > 0.0) dta = ((layer ? hp01 : hp00) * e.area0) / fmad(factor, M[k], kEps);
+        if (e.interior && P[k] > 0.0) dtb = ((layer ? hp11 : hp10) * e.area1) / fmad(factor, P[k], kEps);
         const double dtl = tmin(dta, dtb);
         if (!(dt <= dtl)) {
             const double alpha = dtl / (dt + kEps);
@@ -279,25 +332,28 @@ __device__ __forceinline__ bool edge_flux(const EdgeIn& e, double dt, const Cons
     }
 
     if (lmax < eps) lmax = lmax + eps;
-    wave = e.len * lmax / c.peso;
+    o.wave = e.len * lmax;
+    if (c.peso != 1.0) {
+        o.wave = o.wave * c.inv_peso;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) { d0[k] = c.peso * M[k]; d1[k] = c.peso * P[k]; }
-    return true;
+        for (int k = 0; k < 6; ++k) { M[k] = c.peso * M[k]; P[k] = c.peso * P[k]; }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { o.m[k] = M[k]; o.p[k] = P[k]; }
 }
 
 // procesarAristaDeltaTInicial: wave-speed bound for the initial dt.
-__device__ __forceinline__ double edge_initial_wave(const double W0[6], const double W1[6], double nx, double ny,
-                                                    double len, const Consts& c) {
+__device__ __forceinline__ double edge_initial_wave(const Face& A, const Face& B, double len, const Consts& c) {
     const double eps = c.eps_h;
-    const V4<double> A{W0[0], W0[1] * nx + W0[2] * ny, W0[3], W0[4] * nx + W0[5] * ny};
-    const V4<double> B{W1[0], W1[1] * nx + W1[2] * ny, W1[3], W1[4] * nx + W1[5] * ny};
-    const double h1ij = 0.5 * (A.x + B.x);
-    double sa = sqrt(A.x), sb = sqrt(B.x);
-    const double u1ij = (sa * (vfac(A.x, eps) * A.y) + sb * (vfac(B.x, eps) * B.y)) / (sa + sb + kEps);
-    const double h2ij = 0.5 * (A.z + B.z);
-    sa = sqrt(A.z); sb = sqrt(B.z);
-    const double u2ij = (sa * (vfac(A.z, eps) * A.w) + sb * (vfac(B.z, eps) * B.w)) / (sa + sb + kEps);
-    const V4<double> D = eig_core(h1ij, h2ij, u1ij, u2ij, h1ij * u1ij + h2ij * u2ij, c);
+    const double h1ij = 0.5 * (A.h1 + B.h1);
+    const double fA1 = vfac(A.h1, eps), fB1 = vfac(B.h1, eps);
+    double sa = sqrt(A.h1), sb = sqrt(B.h1);
+    const double u1ij = fmad(sa, fA1 * A.qn1, sb * (fB1 * B.qn1)) / (sa + sb + kEps);
+    const double h2ij = 0.5 * (A.h2 + B.h2);
+    const double fA2 = vfac(A.h2, eps), fB2 = vfac(B.h2, eps);
+    sa = sqrt(A.h2); sb = sqrt(B.h2);
+    const double u2ij = fmad(sa, fA2 * A.qn2, sb * (fB2 * B.qn2)) / (sa + sb + kEps);
+    const V4 D = eig<true>(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
     double lmax = tmax(D.x, D.w);
     const double b = tmax(fabs(u1ij), fabs(u2ij));
     if (b > lmax) lmax = b;
@@ -312,9 +368,9 @@ __device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) 
 #pragma unroll
     for (int layer = 0; layer < 2; ++layer) {
         const int k = 3 * layer;
-        const double x = w[k] / c.eps_h;
+        const double x = w[k] * c.inv_eps;
         const double x2 = x * x;
-        const double aux0 = 1.0 / (x2 * x2 + kEps);
+        const double aux0 = 1.0 / fmad(x2, x2, kEps);
         const double aux = exp_neg(dt * aux0);
         w[k + 1] = w[k + 1] * aux;
         w[k + 2] = w[k + 2] * aux;
@@ -327,9 +383,10 @@ __device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) 
             const double h = w[k];
             const double f = vfac(h, c.eps_h);
             double ux = f * w[k + 1], uy = f * w[k + 2];
-            const double u = sqrt(ux * ux + uy * uy);
+            const double u = sqrt(fmad(ux, ux, uy * uy));
             if (u > vmax) {
-                ux = ux * (vmax / u); uy = uy * (vmax / u);
+                const double s = vmax / u;
+                ux = ux * s; uy = uy * s;
                 w[k + 1] = ux * h; w[k + 2] = uy * h;
             }
         }
@@ -347,50 +404,58 @@ __device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], d
     const double fo1 = vfac(wo[0], eps), fo2 = vfac(wo[3], eps);
     const double uo1x = fo1 * wo[1], uo1y = fo1 * wo[2], uo2x = fo2 * wo[4], uo2y = fo2 * wo[5];
     const double dx = uo1x - uo2x, dy = uo1y - uo2y;
-    const double du = sqrt(dx * dx + dy * dy);
-    const double u1 = sqrt(uo1x * uo1x + uo1y * uo1y);
-    const double u2 = sqrt(uo2x * uo2x + uo2y * uo2y);
-    const double hmod = h2 + c.r * h1;
-    const double mfl = eps * (1.0 + c.r);
-    const double m = (hmod > mfl) ? hmod : mfl;
-    const double hm2 = hmod * hmod, m2 = m * m;
-    const double hmodm = sqrt(hm2 * hm2 + m2 * m2);
+    const double du = sqrt(fmad(dx, dx, dy * dy));
+    const double u1 = sqrt(fmad(uo1x, uo1x, uo1y * uo1y));
+    const double u2 = sqrt(fmad(uo2x, uo2x, uo2y * uo2y));
     if ((h1 > 0.0) && (h2 > 0.0)) {
-        const double c1 = dt * kSqrt2 * h2 * hmod / hmodm * c.mfc * du;
-        const double c2 = dt * c.r * kSqrt2 * h1 * hmod / hmodm * c.mfc * du;
-        const double c3 = dt * c.g * c.mfs * c.mfs * u2 / (pow43(h2) + kEps);
-        const double det = 1.0 / ((1.0 + c1) * (1.0 + c2 + c3) - c1 * c2);
-        w[1] = h1 * (u1x * (1.0 + c2 + c3) + c1 * u2x) * det;
-        w[4] = h2 * (u2x * (1.0 + c1) + c2 * u1x) * det;
-        w[2] = h1 * (u1y * (1.0 + c2 + c3) + c1 * u2y) * det;
-        w[5] = h2 * (u2y * (1.0 + c1) + c2 * u1y) * det;
+        const double hmod = fmad(c.r, h1, h2);
+        const double m = (hmod > c.eps_1r) ? hmod : c.eps_1r;
+        const double hm2 = hmod * hmod, m2 = m * m;
+        const double hh = hmod / sqrt(fmad(hm2, hm2, m2 * m2));
+        const double k12 = ((dt * kSqrt2) * hh) * (c.mfc * du);
+        const double c1 = k12 * h2;
+        const double c2 = (k12 * c.r) * h1;
+        const double c3 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
+        const double e1 = 1.0 + c1, e2 = 1.0 + c2 + c3;
+        const double det = 1.0 / fmad(e1, e2, -(c1 * c2));
+        w[1] = (h1 * fmad(u1x, e2, c1 * u2x)) * det;
+        w[4] = (h2 * fmad(u2x, e1, c2 * u1x)) * det;
+        w[2] = (h1 * fmad(u1y, e2, c1 * u2y)) * det;
+        w[5] = (h2 * fmad(u2y, e1, c2 * u1y)) * det;
     }
     if ((h1 > 0.0) && (h2 < eps)) {
         u1x = f1 * w[1]; u1y = f1 * w[2];
-        const double c1 = dt * c.g * c.mf0 * c.mf0 * u1 / (pow43(h1) + kEps);
-        w[1] = h1 * u1x / (1.0 + c1);
-        w[2] = h1 * u1y / (1.0 + c1);
+        const double c1 = ((dt * c.g_mf02) * u1) / (pow43(h1) + kEps);
+        const double inv = 1.0 / (1.0 + c1);
+        w[1] = (h1 * u1x) * inv;
+        w[2] = (h1 * u1y) * inv;
     }
     if ((h2 > 0.0) && (h1 < eps)) {
         u2x = f2 * w[4]; u2y = f2 * w[5];
-        const double c1 = dt * c.g * c.mfs * c.mfs * u2 / (pow43(h2) + kEps);
-        w[4] = h2 * u2x / (1.0 + c1);
-        w[5] = h2 * u2y / (1.0 + c1);
+        const double c1 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
+        const double inv = 1.0 / (1.0 + c1);
+        w[4] = (h2 * u2x) * inv;
+        w[5] = (h2 * u2y) * inv;
     }
 }
 
 // coulomb (Volumen_kernel.cu:7-26)
 __device__ __forceinline__ void coulomb(double w[6], double dt, const Consts& c) {
+    if (!(w[3] > 0.0)) {
+        w[4] = w[4] * 0.0;
+        w[5] = w[5] * 0.0;
+        return;
+    }
     double mu = c.mu;
     if (c.law != 0) {
-        const double u1 = sqrt(w[1] * w[1] + w[2] * w[2]) * vfac(w[0], c.eps_h);
-        const double u2 = sqrt(w[4] * w[4] + w[5] * w[5]) * vfac(w[3], c.eps_h);
+        const double u1 = sqrt(fmad(w[1], w[1], w[2] * w[2])) * vfac(w[0], c.eps_h);
+        const double u2 = sqrt(fmad(w[4], w[4], w[5] * w[5])) * vfac(w[3], c.eps_h);
         mu = friction_mu(w[0], u1, w[3], u2, c);
     }
-    const double sc = fsc_of(w[0], c) * mu * c.g * w[3] * dt * 1.0;
-    const double normq = sqrt(w[4] * w[4] + w[5] * w[5]);
+    const double sc = ((((fsc_of(w[0], c) * mu) * c.g) * w[3]) * dt);
+    const double normq = sqrt(fmad(w[4], w[4], w[5] * w[5]));
     double aux = 0.0;
-    if ((normq + sc >= kEps) && (w[3] > 0.0)) aux = (normq >= sc) ? normq / (normq + sc) : 0.0;
+    if ((normq + sc >= kEps) && (normq >= sc)) aux = normq / (normq + sc);
     w[4] = w[4] * aux;
     w[5] = w[5] * aux;
 }
@@ -398,18 +463,20 @@ __device__ __forceinline__ void coulomb(double w[6], double dt, const Consts& c)
 // One cell of obtenerEstadoYDeltaTVolumenesGPU (Volumen_kernel.cu:231-284),
 // plus the spherical metric source (tanR = tan(lat)/R, 0 for Cartesian).
 __device__ __forceinline__ void volume_update(const double wo[6], const double acc[7], double w[6], double& dti,
-                                              double area, double tanR, double dt, const Consts& c) {
-    dti = (acc[6] < kEps) ? kBig : (2.0 * c.cfl * area) / acc[6];
-    const double b = dt / area;
+                                              double area, double inv_area, double tanR, double dt,
+                                              const Consts& c) {
+    dti = (acc[6] < kEps) ? kBig : ((2.0 * c.cfl) * area) / acc[6];
+    const double b = dt * inv_area;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) w[k] = wo[k] + b * acc[k];
+    for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
     if (tanR != 0.0) {
 #pragma unroll
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
             const double ux = vfac(wo[k], c.eps_h) * wo[k + 1];
-            w[k + 1] = w[k + 1] + dt * (ux * wo[k + 2] * tanR);
-            w[k + 2] = w[k + 2] - dt * (ux * wo[k + 1] * tanR);
+            const double s = dt * (ux * tanR);
+            w[k + 1] = fmad(s, wo[k + 2], w[k + 1]);
+            w[k + 2] = fmad(-s, wo[k + 1], w[k + 2]);
         }
     }
     filtro(w, dt, c);

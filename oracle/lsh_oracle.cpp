@@ -61,6 +61,14 @@ using std::tan;
 struct Consts {
     double g, r, gp, eps_h, peso, beta, cfl, mu, mfc, mf0, mfs, vmax1, vmax2, L, H;
     double tan1, tan2, tan3, tan4;
+    // derived on the host, identically in the CUDA library (lsh_core.cu make_consts)
+    double omr;       // 1 - r
+    double inv_gp;    // 1 / (g (1 - r))
+    double inv_eps;   // 1 / eps_h
+    double inv_peso;  // 1 / peso
+    double eps_1r;    // eps_h (1 + r)
+    double g_mf02;    // g mf0^2
+    double g_mfs2;    // g mfs^2
     int law;
     int eig_sort;
 };
@@ -68,6 +76,7 @@ struct Consts {
 struct Geo {
     int nx, ny;
     std::vector<double> area;    // [ny]   cell area of row j
+    std::vector<double> inv_area;  // [ny] 1 / area
     std::vector<double> len_v;   // [ny]   length of the vertical edges of row j
     std::vector<double> len_h;   // [ny+1] length of horizontal edge row y
     std::vector<double> tanR;    // [ny]   tan(lat_j)/R, 0 for Cartesian
@@ -83,6 +92,13 @@ static Consts make_consts(const lsh_params& p) {
     c.mfc = p.mfc; c.mf0 = p.mf0; c.mfs = p.mfs; c.vmax1 = p.vmax1; c.vmax2 = p.vmax2;
     c.L = p.L; c.H = p.H;
     c.tan1 = tan(p.angle1); c.tan2 = tan(p.angle2); c.tan3 = tan(p.angle3); c.tan4 = tan(p.angle4);
+    c.omr = 1.0 - p.r;
+    c.inv_gp = 1.0 / c.gp;
+    c.inv_eps = 1.0 / p.eps_h;
+    c.inv_peso = 1.0 / p.peso;
+    c.eps_1r = p.eps_h * (1.0 + p.r);
+    c.g_mf02 = (p.gravity * p.mf0) * p.mf0;
+    c.g_mfs2 = (p.gravity * p.mfs) * p.mfs;
     c.law = p.friction_law;
     c.eig_sort = p.eig_sort;
     return c;
@@ -92,7 +108,7 @@ static Geo make_geo(const lsh_params& p) {
     Geo g;
     g.nx = p.nx; g.ny = p.ny;
     g.area.resize(p.ny); g.len_v.resize(p.ny); g.len_h.resize(p.ny + 1);
-    g.tanR.resize(p.ny); g.wx.resize(p.ny); g.wy.resize(p.ny);
+    g.tanR.resize(p.ny); g.wx.resize(p.ny); g.wy.resize(p.ny); g.inv_area.resize(p.ny);
     if (p.coords == LSH_COORDS_SPHERICAL) {
         const double d2r = kPi / 180.0;
         const double R = p.radius, dl = p.dlon * d2r, dp = p.dlat * d2r;
@@ -116,172 +132,181 @@ static Geo make_geo(const lsh_params& p) {
             g.wy[j] = p.dx;
         }
     }
+    for (int j = 0; j < p.ny; ++j) g.inv_area[j] = 1.0 / g.area[j];
     return g;
 }
 
 // ---------------------------------------------------------------- helpers
-template <class T> inline T tmin(const T& a, const T& b) { return (b < a) ? b : a; }
-template <class T> inline T tmax(const T& a, const T& b) { return (b > a) ? b : a; }
-template <class T> inline T max0(const T& a) { return (a > 0.0) ? a : T(0.0); }
+// The arithmetic below fixes every fused multiply-add (fmad) and every
+// reciprocal of a constant (inv_*) explicitly; the CUDA kernels
+// (landslidehysea_gb300/csrc/lsh_scheme.cuh) evaluate the same sequence.
 
+inline double tmin(double a, double b) { return (b < a) ? b : a; }
+inline double tmax(double a, double b) { return (b > a) ? b : a; }
+inline double max0(double a) { return (a > 0.0) ? a : 0.0; }
+inline double fmad(double a, double b, double c) { return lshm::fmad(a, b, c); }
 inline double exp_neg(double x) { return lshm::exp_neg(x); }
 
 // sqrt(2) h / sqrt(h^4 + max(h, eps_h)^4): the desingularised 1/h factor
 // (Arista_kernel.cu:74,380; Volumen_kernel.cu:13,44,48)
-template <class T> inline T vfac(const T& h, double eps_h) {
-    const T m = (h > eps_h) ? h : T(eps_h);
-    const T h2 = h * h, m2 = m * m;
-    return (kSqrt2 * h) / sqrt(h2 * h2 + m2 * m2);
+inline double vfac(double h, double eps_h) {
+    const double m = (h > eps_h) ? h : eps_h;
+    const double h2 = h * h, m2 = m * m;
+    return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
-template <class T> inline T pow43(const T& h) { return h * lshm::cbrt_pos(h); }
+inline double pow43(double h) { return h * lshm::cbrt_pos(h); }
 
 inline int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }  // Constantes.hxx:14
 
-template <class T> struct V4 { T x, y, z, w; };
+struct V4 { double x, y, z, w; };
 
 // The fixed compare-and-swap sequence of Arista_kernel.cu:193-234, including
 // its (i=2, j=1) compare, which leaves the larger of y/z in y (eig_sort 0);
 // with eig_sort 1 that compare is (1,2) and the sequence is a true sort.
-template <class T> inline void sort_eig(V4<T>& D, int full) {
-    auto cs = [](T& a, T& b) { if (a > b) { T t = b; b = a; a = t; } };
+inline void sort_eig(V4& D, int full) {
+    auto cs = [](double& a, double& b) { if (a > b) { double t = b; b = a; a = t; } };
     cs(D.x, D.y); cs(D.x, D.z); cs(D.x, D.w); cs(D.y, D.z); cs(D.y, D.w);
     if (full) cs(D.y, D.z);
-    else if (D.z > D.y) { T t = D.y; D.y = D.z; D.z = t; }
+    else if (D.z > D.y) { double t = D.y; D.y = D.z; D.z = t; }
     cs(D.z, D.w);
 }
 
-// aproximarAutovalores1D (Arista_kernel.cu:152-237).  conserved == false:
-// (a1, a2) are the edge-averaged normal velocities (flag 0); conserved == true:
-// (a1, a2) are the rotated normal discharges of one cell (flag 1).
-template <class T>
-inline V4<T> eig(const T& h1, const T& a1, const T& h2, const T& a2, bool conserved, const Consts& c) {
-    const T h = h1 + h2;
-    const T F = vfac(h, c.eps_h);
-    T u1, u2, q;
-    if (conserved) { q = a1 + a2; u1 = vfac(h1, c.eps_h) * a1; u2 = vfac(h2, c.eps_h) * a2; }
-    else           { q = h1 * a1 + h2 * a2; u1 = a1; u2 = a2; }
-    const T u = q * F;
-    const T cg = sqrt(c.g * h);
-    const T uu = (u1 * h2 + u2 * h1) * F;
-    const T d = u1 - u2;
-    const T aux = 1.0 - d * d * F / c.gp;
-    const T ci = sqrt(c.gp * h1 * h2 * F * fabs(aux));
-    V4<T> D{u - cg, uu - ci, uu + ci, u + cg};
+// aproximarAutovalores1D (Arista_kernel.cu:152-237) given the two layers'
+// depths, velocities (u1, u2) and the total normal discharge q:
+// external u -+ sqrt(g h), internal uu -+ sqrt(g' h1 h2 F |1 - (u1-u2)^2 F / g'|).
+inline V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c) {
+    const double h = h1 + h2;
+    const double F = vfac(h, c.eps_h);
+    const double u = q * F;
+    const double cg = sqrt(c.g * h);
+    const double uu = fmad(u1, h2, u2 * h1) * F;
+    const double d = u1 - u2;
+    const double aux = fmad(-((d * d) * F), c.inv_gp, 1.0);
+    const double ci = sqrt((((c.gp * h1) * h2) * F) * fabs(aux));
+    V4 D{u - cg, uu - ci, uu + ci, u + cg};
     sort_eig(D, c.eig_sort);
     return D;
 }
 
 // defTerminoFriccion (Arista_kernel.cu:11-58): friction coefficient mu.
-template <class T>
-inline T friction_mu(const T& h1, const T& u1, const T& h2, const T& u2, const Consts& c) {
-    if (c.law == LSH_FRICTION_COULOMB) return T(c.mu);
+inline double friction_mu(double h1, double u1, double h2, double u2, const Consts& c) {
+    if (c.law == LSH_FRICTION_COULOMB) return c.mu;
     // Pouliquen law (the reference's #ifndef COULOMB branch)
-    const T a = 10.0 * h1 / c.eps_h;
-    const T rr = 1.0 - c.r * (1.0 - exp_neg(a * a));
-    const T gp = c.g * rr;
-    const T fr1 = u1 * u1 * vfac(h1, c.eps_h) / gp;
-    const T fr2 = u2 * u2 * vfac(h2, c.eps_h) / gp;
-    const T fr = sqrt(fr1 + fr2 + (1.0 - rr) * fr1 * fr2);
+    const double a = (10.0 * h1) * c.inv_eps;
+    const double rr = 1.0 - c.r * (1.0 - exp_neg(a * a));
+    const double gp = c.g * rr;
+    const double fr1 = ((u1 * u1) * vfac(h1, c.eps_h)) / gp;
+    const double fr2 = ((u2 * u2) * vfac(h2, c.eps_h)) / gp;
+    const double fr = sqrt(fmad((1.0 - rr) * fr1, fr2, fr1 + fr2));
     const double beta = 0.136, L2 = 8.0e-4, chi = 1.0e-3;
-    const T mustop = c.tan1 + (c.tan2 - c.tan1) / (1.0 + h2 / L2);
-    const T mustart = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2);
-    T muf;
+    const double mustop = c.tan1 + (c.tan2 - c.tan1) / (1.0 + h2 / L2);
+    const double mustart = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2);
+    double muf;
     if (fr > beta) muf = c.tan1 + (c.tan2 - c.tan1) / (1.0 + beta * h2 / (fr * L2));
     else if (fabs(fr) < kEps) muf = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2);
-    else muf = mustart + lshm::pow_pos(fr / beta, chi) * (mustop - mustart);
-    return muf * c.L / c.H;
+    else muf = fmad(lshm::pow_pos(fr / beta, chi), mustop - mustart, mustart);
+    return (muf * c.L) / c.H;
 }
 
 // 1 - r (1 - exp(-(10 h1 / eps_h)^2)) (Arista_kernel.cu:136, Volumen_kernel.cu:15)
-template <class T> inline T fsc_of(const T& h1, const Consts& c) {
-    const T a = 10.0 * h1 / c.eps_h;
+inline double fsc_of(double h1, const Consts& c) {
+    const double a = (10.0 * h1) * c.inv_eps;
     return 1.0 - c.r * (1.0 - exp_neg(a * a));
 }
 
 // ---------------------------------------------------------------- edge flux
-// Inputs of one edge.  W0 / W1 are the two states facing the edge (cell
-// values at first order, reconstructed face values at second order; W1 is the
-// ghost at a boundary); hc* are the cell-average depths and acc*h the partial
+// One face state in the edge's normal frame: depth, normal and tangential
+// discharge of each layer, bottom depth.
+struct Face { double h1, qn1, qt1, h2, qn2, qt2, H; };
+
+// Inputs of one edge.  A / B are the states facing the edge (cell values at
+// first order, reconstructed face values at second order; B is the ghost at a
+// boundary); hc* are the cell-average depths and acc*h the partial
 // accumulators (h1, h2) the positivity limiter reads.
-template <class T> struct EdgeIn {
-    T W0[6], W1[6];
-    T H0, H1;
-    double nx, ny, len, area0, area1;
+struct EdgeIn {
+    Face A, B;
+    double len, area0, area1, inv_area0, inv_area1;
     bool interior;
-    T hc0[2], hc1[2];
-    T acc0h[2], acc1h[2];
+    double hc0[2], hc1[2];
+    double acc0h[2], acc1h[2];
 };
 
+// Edge output in the normal frame: per layer (mass, normal momentum,
+// tangential momentum) to subtract from cell 0 (m) and cell 1 (p).
+struct EdgeOut { double m[6], p[6]; double wave; };
+
 // procesarArista (Arista_kernel.cu:324-645).  Returns false for a dry edge
-// (no contribution at all, :397).  d0 / d1 are subtracted from the
-// accumulators of cell 0 / cell 1 (already multiplied by peso), `wave` is
-// added to their dt accumulator.
-template <class T>
-bool edge_flux(const EdgeIn<T>& e, const T& dt, const Consts& c, T d0[6], T d1[6], T& wave) {
-    const double nx = e.nx, ny = e.ny, eps = c.eps_h;
-    V4<T> A{e.W0[0], e.W0[1] * nx + e.W0[2] * ny, e.W0[3], e.W0[4] * nx + e.W0[5] * ny};
-    V4<T> B{e.W1[0], e.W1[1] * nx + e.W1[2] * ny, e.W1[3], e.W1[4] * nx + e.W1[5] * ny};
-    const T H0 = e.H0, H1 = e.H1;
+// (no contribution at all, :397).
+bool edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
+    const double eps = c.eps_h;
+    double Aq1 = e.A.qn1, Aq2 = e.A.qn2, Bq1 = e.B.qn1, Bq2 = e.B.qn2;
+    const double Ah1 = e.A.h1, Ah2 = e.A.h2, Bh1 = e.B.h1, Bh2 = e.B.h2;
+    const double H0 = e.A.H, H1 = e.B.H;
+
+    const double h1ij = 0.5 * (Ah1 + Bh1);
+    const double h2ij = 0.5 * (Ah2 + Bh2);
+    if (!((h1ij >= kEps) || (h2ij >= kEps))) return false;
 
     // tratamientoSecoMojado (Arista_kernel.cu:301-321)
-    if ((A.z < eps) && (H1 - B.z > H0)) B.w = 0.0;
-    if ((B.z < eps) && (H0 - A.z > H1)) A.w = 0.0;
-    if ((A.x < eps) && (H1 - B.x - B.z > H0 - A.z)) B.y = 0.0;
-    if ((B.x < eps) && (H0 - A.x - A.z > H1 - B.z)) A.y = 0.0;
-    if ((A.z + A.x < eps) && (H1 - B.x - B.z > H0)) { B.y = 0.0; B.w = 0.0; }
-    if ((B.z + B.x < eps) && (H0 - A.x - A.z > H1)) { A.y = 0.0; A.w = 0.0; }
+    if ((Ah2 < eps) && (H1 - Bh2 > H0)) Bq2 = 0.0;
+    if ((Bh2 < eps) && (H0 - Ah2 > H1)) Aq2 = 0.0;
+    if ((Ah1 < eps) && (H1 - Bh1 - Bh2 > H0 - Ah2)) Bq1 = 0.0;
+    if ((Bh1 < eps) && (H0 - Ah1 - Ah2 > H1 - Bh2)) Aq1 = 0.0;
+    if ((Ah2 + Ah1 < eps) && (H1 - Bh1 - Bh2 > H0)) { Bq1 = 0.0; Bq2 = 0.0; }
+    if ((Bh2 + Bh1 < eps) && (H0 - Ah1 - Ah2 > H1)) { Aq1 = 0.0; Aq2 = 0.0; }
 
     // Roe-type averages (Arista_kernel.cu:375-395)
-    const T fA1 = vfac(A.x, eps), fB1 = vfac(B.x, eps);
-    const T fA2 = vfac(A.z, eps), fB2 = vfac(B.z, eps);
-    const T h1ij = 0.5 * (A.x + B.x);
-    T sa = sqrt(A.x), sb = sqrt(B.x);
-    const T u1ij = (sa * (fA1 * A.y) + sb * (fB1 * B.y)) / (sa + sb + kEps);
-    const T h2ij = 0.5 * (A.z + B.z);
-    sa = sqrt(A.z); sb = sqrt(B.z);
-    const T u2ij = (sa * (fA2 * A.w) + sb * (fB2 * B.w)) / (sa + sb + kEps);
-
-    if (!((h1ij >= kEps) || (h2ij >= kEps))) return false;  // :397
+    const double fA1 = vfac(Ah1, eps), fB1 = vfac(Bh1, eps);
+    const double fA2 = vfac(Ah2, eps), fB2 = vfac(Bh2, eps);
+    double sa = sqrt(Ah1), sb = sqrt(Bh1);
+    const double u1ij = fmad(sa, fA1 * Aq1, sb * (fB1 * Bq1)) / (sa + sb + kEps);
+    sa = sqrt(Ah2); sb = sqrt(Bh2);
+    const double u2ij = fmad(sa, fA2 * Aq2, sb * (fB2 * Bq2)) / (sa + sb + kEps);
 
     // hydrostatic reconstruction (terminosPresion1D, :94-115)
-    const T Hm = tmin(H0, H1);
-    const T deta1 = max0(B.x + B.z - H1 + Hm) - max0(A.x + A.z - H0 + Hm);
-    const T deta2 = max0(B.z - H1 + Hm) - max0(A.z - H0 + Hm);
-    V4<T> tp{T(0.0), c.g * h1ij * deta1, T(0.0), c.g * h2ij * ((1.0 - c.r) * deta2 + c.r * deta1)};
+    const double Hm = tmin(H0, H1);
+    const double deta1 = max0(Bh1 + Bh2 - H1 + Hm) - max0(Ah1 + Ah2 - H0 + Hm);
+    const double deta2 = max0(Bh2 - H1 + Hm) - max0(Ah2 - H0 + Hm);
+    const double gh1 = c.g * h1ij, gh2 = c.g * h2ij;
+    V4 tp{0.0, gh1 * deta1, 0.0, gh2 * fmad(c.omr, deta2, c.r * deta1)};
 
     // edge Coulomb switch (terminosPresion1DMod :134-147, identityModification :259-264)
-    const T mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
-    const T sc = fsc_of(h1ij, c) * mu * c.g * h2ij;
-    const bool coul = fabs(h2ij * u2ij) < c.peso * sc * dt;
-    V4<T> tp2 = tp;
-    if (coul) tp2.w = c.g * h2ij * c.r * deta1;
+    const double mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
+    const double sc = ((fsc_of(h1ij, c) * mu) * c.g) * h2ij;
+    const bool coul = fabs(h2ij * u2ij) < (c.peso * sc) * dt;
+    V4 tp2 = tp;
+    if (coul) tp2.w = (gh2 * c.r) * deta1;
 
     // eigenvalue bounds (:427-444)
-    const V4<T> D = eig(h1ij, u1ij, h2ij, u2ij, false, c);
-    const V4<T> E0 = eig(A.x, A.y, A.z, A.w, true, c);
-    const V4<T> E1 = eig(B.x, B.y, B.z, B.w, true, c);
-    const T aut1 = tmin(D.x, tmin(E0.x, E1.x));
-    const T aut3 = tmax(D.w, tmax(E0.w, E1.w));
-    T lmax = tmax(fabs(aut3), fabs(aut1));
-    const T umax = tmax(fabs(u1ij), fabs(u2ij));
+    const V4 D = eig(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
+    const V4 E0 = eig(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, Aq1 + Aq2, c);
+    const V4 E1 = eig(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, Bq1 + Bq2, c);
+    const double aut1 = tmin(D.x, tmin(E0.x, E1.x));
+    const double aut3 = tmax(D.w, tmax(E0.w, E1.w));
+    double lmax = tmax(fabs(aut3), fabs(aut1));
+    const double umax = tmax(fabs(u1ij), fabs(u2ij));
     if (umax > lmax) lmax = umax;
-    T aut2 = tmax(fabs(D.y), fabs(D.z));
-    if (sgn(double(aut1 + aut3)) < 0) aut2 = -aut2;
+    double aut2 = tmax(fabs(D.y), fabs(D.z));
+    if (sgn(aut1 + aut3) < 0) aut2 = -aut2;
 
-    // PVM / IFCP coefficients (:446-465)
-    T a0, a1, a2;
+    // PVM / IFCP coefficients (:446-465); the three parabola weights share
+    // one reciprocal of (aut1-aut2)(aut1-aut3)(aut2-aut3)
+    double a0, a1, a2;
     if ((fabs(aut1 - aut3) >= kEps) && (fabs(aut1 - aut2) >= kEps) && (fabs(aut2 - aut3) >= kEps)) {
         if ((h1ij >= eps) && (h2ij >= eps)) {
-            const T a = fabs(aut1) / ((aut1 - aut3) * (aut1 - aut2));
-            const T b = fabs(aut2) / ((aut2 - aut1) * (aut2 - aut3));
-            const T cc = fabs(aut3) / ((aut3 - aut1) * (aut3 - aut2));
-            a0 = a * aut2 * aut3 + b * aut1 * aut3 + cc * aut1 * aut2;
-            a1 = -a * (aut2 + aut3) - b * (aut1 + aut3) - cc * (aut1 + aut2);
+            const double d12 = aut1 - aut2, d13 = aut1 - aut3, d23 = aut2 - aut3;
+            const double inv = 1.0 / ((d12 * d13) * d23);
+            const double a = (fabs(aut1) * d23) * inv;
+            const double b = -((fabs(aut2) * d13) * inv);
+            const double cc = (fabs(aut3) * d12) * inv;
+            a0 = fmad(a * aut2, aut3, fmad(b * aut1, aut3, (cc * aut1) * aut2));
+            a1 = -fmad(a, aut2 + aut3, fmad(b, aut1 + aut3, cc * (aut1 + aut2)));
             a2 = a + b + cc;
         } else {
-            a0 = (aut3 * fabs(aut1) - aut1 * fabs(aut3)) / (aut3 - aut1);
-            a1 = (fabs(aut3) - fabs(aut1)) / (aut3 - aut1);
+            const double inv = 1.0 / (aut3 - aut1);
+            a0 = fmad(aut3, fabs(aut1), -(aut1 * fabs(aut3))) * inv;
+            a1 = (fabs(aut3) - fabs(aut1)) * inv;
             a2 = 0.0;
         }
     } else {
@@ -289,88 +314,83 @@ bool edge_flux(const EdgeIn<T>& e, const T& dt, const Consts& c, T d0[6], T d1[6
     }
 
     // physical fluxes (getFlujo_1dC :62-92)
-    const V4<T> FA{A.y, (A.x < kEps) ? T(0.0) : (fA1 * A.y) * A.y, A.w, (A.z < kEps) ? T(0.0) : (fA2 * A.w) * A.w};
-    const V4<T> FB{B.y, (B.x < kEps) ? T(0.0) : (fB1 * B.y) * B.y, B.w, (B.z < kEps) ? T(0.0) : (fB2 * B.w) * B.w};
-    const V4<T> dF{FB.x - FA.x, FB.y - FA.y, FB.z - FA.z, FB.w - FA.w};
-    tp2 = V4<T>{tp2.x + dF.x, tp2.y + dF.y, tp2.z + dF.z, tp2.w + dF.w};
-    const V4<T> half{0.5 * (dF.x + tp.x), 0.5 * (dF.y + tp.y), 0.5 * (dF.z + tp.z), 0.5 * (dF.w + tp.w)};
+    const V4 FA{Aq1, (Ah1 < kEps) ? 0.0 : (fA1 * Aq1) * Aq1, Aq2, (Ah2 < kEps) ? 0.0 : (fA2 * Aq2) * Aq2};
+    const V4 FB{Bq1, (Bh1 < kEps) ? 0.0 : (fB1 * Bq1) * Bq1, Bq2, (Bh2 < kEps) ? 0.0 : (fB2 * Bq2) * Bq2};
+    const V4 dF{FB.x - FA.x, FB.y - FA.y, FB.z - FA.z, FB.w - FA.w};
+    tp2 = V4{tp2.x + dF.x, tp2.y + dF.y, tp2.z + dF.z, tp2.w + dF.w};
+    const V4 half{0.5 * (dF.x + tp.x), 0.5 * (dF.y + tp.y), 0.5 * (dF.z + tp.z), 0.5 * (dF.w + tp.w)};
 
     // A * tp2 (:476-482)
-    const T ga = c.g * h1ij, gb = c.g * h2ij;
-    const V4<T> At{tp2.y,
-                   (ga - u1ij * u1ij) * tp2.x + 2.0 * u1ij * tp2.y + ga * tp2.z,
-                   tp2.w,
-                   c.r * gb * tp2.x + (gb - u2ij * u2ij) * tp2.z + 2.0 * u2ij * tp2.w};
+    const V4 At{tp2.y, fmad(gh1, tp2.z, fmad(u1ij + u1ij, tp2.y, fmad(-u1ij, u1ij, gh1) * tp2.x)), tp2.w,
+                fmad(c.r * gh2, tp2.x, fmad(fmad(-u2ij, u2ij, gh2), tp2.z, (u2ij + u2ij) * tp2.w))};
 
     // identityModification (:239-276)
-    V4<T> I{deta1, B.y - A.y, T(0.0), B.w - A.w};
+    V4 I{deta1, Bq1 - Aq1, 0.0, Bq2 - Aq2};
     if (!coul) {
-        if ((A.x > eps) && (B.x > eps)) I.x = I.x - deta2;
+        if ((Ah1 > eps) && (Bh1 > eps)) I.x = I.x - deta2;
         I.z = deta2;
     }
 
     // viscosity and the two one-sided fluxes (:488-504)
-    const V4<T> Q{0.5 * (a0 * I.x + a1 * tp2.x + a2 * At.x), 0.5 * (a0 * I.y + a1 * tp2.y + a2 * At.y),
-                  0.5 * (a0 * I.z + a1 * tp2.z + a2 * At.z), 0.5 * (a0 * I.w + a1 * tp2.w + a2 * At.w)};
-    const V4<T> Fm{half.x + (FA.x - Q.x), half.y + (FA.y - Q.y), half.z + (FA.z - Q.z), half.w + (FA.w - Q.w)};
-    const V4<T> Fp{half.x + (Q.x - FB.x), half.y + (Q.y - FB.y), half.z + (Q.z - FB.z), half.w + (Q.w - FB.w)};
+    const V4 Q{0.5 * fmad(a0, I.x, fmad(a1, tp2.x, a2 * At.x)), 0.5 * fmad(a0, I.y, fmad(a1, tp2.y, a2 * At.y)),
+               0.5 * fmad(a0, I.z, fmad(a1, tp2.z, a2 * At.z)), 0.5 * fmad(a0, I.w, fmad(a1, tp2.w, a2 * At.w))};
+    const V4 Fm{half.x + (FA.x - Q.x), half.y + (FA.y - Q.y), half.z + (FA.z - Q.z), half.w + (FA.w - Q.w)};
+    const V4 Fp{half.x + (Q.x - FB.x), half.y + (Q.y - FB.y), half.z + (Q.z - FB.z), half.w + (Q.w - FB.w)};
 
     // upwinded tangential velocity (:506-532)
-    const T ut0 = fA1 * (e.W0[2] * nx - e.W0[1] * ny), ut1 = fB1 * (e.W1[2] * nx - e.W1[1] * ny);
-    const T u1t = (fabs(Fm.x) < kEps) ? T(0.0) : ((Fm.x > 0.0) ? ut0 : ut1);
-    const T vt0 = fA2 * (e.W0[5] * nx - e.W0[4] * ny), vt1 = fB2 * (e.W1[5] * nx - e.W1[4] * ny);
-    const T u2t = (fabs(Fm.z) < kEps) ? T(0.0) : ((Fm.z > 0.0) ? vt0 : vt1);
+    const double u1t = (fabs(Fm.x) < kEps) ? 0.0 : ((Fm.x > 0.0) ? fA1 * e.A.qt1 : fB1 * e.B.qt1);
+    const double u2t = (fabs(Fm.z) < kEps) ? 0.0 : ((Fm.z > 0.0) ? fA2 * e.A.qt2 : fB2 * e.B.qt2);
+    const double s1 = Fm.x * u1t, s2 = Fm.z * u2t;
 
-    // rotate back and scale by the edge length (:534-552)
-    const T s1 = Fm.x * u1t, s2 = Fm.z * u2t;
-    T P[6] = {Fp.x, Fp.y * nx + s1 * ny, Fp.y * ny - s1 * nx, Fp.z, Fp.w * nx + s2 * ny, Fp.w * ny - s2 * nx};
-    T M[6] = {Fm.x, Fm.y * nx - s1 * ny, Fm.y * ny + s1 * nx, Fm.z, Fm.w * nx - s2 * ny, Fm.w * ny + s2 * nx};
+    // normal-frame fluxes times the edge length: (mass, normal, tangential);
+    // the tangential part is +s for cell 0 and -s for cell 1 (:534-552)
+    double M[6] = {Fm.x, Fm.y, s1, Fm.z, Fm.w, s2};
+    double P[6] = {Fp.x, Fp.y, -s1, Fp.z, Fp.w, -s2};
     for (int k = 0; k < 6; ++k) { P[k] = e.len * P[k]; M[k] = e.len * M[k]; }
 
     // positivity limiter on the partially accumulated depths (:554-609)
-    const T b0 = dt / e.area0;
-    const T hp00 = e.hc0[0] + b0 * e.acc0h[0], hp01 = e.hc0[1] + b0 * e.acc0h[1];
-    T hp10 = 0.0, hp11 = 0.0;
+    const double b0 = dt * e.inv_area0;
+    const double hp00 = fmad(b0, e.acc0h[0], e.hc0[0]), hp01 = fmad(b0, e.acc0h[1], e.hc0[1]);
+    double hp10 = 0.0, hp11 = 0.0;
     if (e.interior) {
-        const T b1 = dt / e.area1;
-        hp10 = e.hc1[0] + b1 * e.acc1h[0]; hp11 = e.hc1[1] + b1 * e.acc1h[1];
+        const double b1 = dt * e.inv_area1;
+        hp10 = fmad(b1, e.acc1h[0], e.hc1[0]); hp11 = fmad(b1, e.acc1h[1], e.hc1[1]);
     }
     const double factor = 1.0 * c.beta;
     for (int layer = 0; layer < 2; ++layer) {
         const int k = 3 * layer;
-        T dta = kBig, dtb = kBig;
-        if (M[k] > 0.0) dta = (layer ? hp01 : hp00) * e.area0 / (factor * M[k] + kEps);
-        if (e.interior && P[k] > 0.0) dtb = (layer ? hp11 : hp10) * e.area1 / (factor * P[k] + kEps);
-        const T dtl = tmin(dta, dtb);
+        double dta = kBig, dtb = kBig;
+        if (M[k] > 0.0) dta = ((layer ? hp01 : hp00) * e.area0) / fmad(factor, M[k], kEps);
+        if (e.interior && P[k] > 0.0) dtb = ((layer ? hp11 : hp10) * e.area1) / fmad(factor, P[k], kEps);
+        const double dtl = tmin(dta, dtb);
         if (!(dt <= dtl)) {
-            const T alpha = dtl / (dt + kEps);
+            const double alpha = dtl / (dt + kEps);
             for (int q = k; q < k + 3; ++q) { M[q] = alpha * M[q]; P[q] = alpha * P[q]; }
         }
     }
 
     if (lmax < eps) lmax = lmax + eps;  // :611-612
-    wave = e.len * lmax / c.peso;
-    for (int k = 0; k < 6; ++k) { d0[k] = c.peso * M[k]; d1[k] = c.peso * P[k]; }
+    o.wave = (e.len * lmax) * c.inv_peso;
+    for (int k = 0; k < 6; ++k) { o.m[k] = c.peso * M[k]; o.p[k] = c.peso * P[k]; }
     return true;
 }
 
 // procesarAristaDeltaTInicial (Arista_kernel.cu:1040-1127): wave-speed bound
 // for the initial dt.  No wet/dry fix, no dry-edge skip, and the max of the
 // signed sorted external eigenvalues (:1107).
-template <class T>
-T edge_initial_wave(const T W0[6], const T W1[6], double nx, double ny, double len, const Consts& c) {
+double edge_initial_wave(const Face& A, const Face& B, double len, const Consts& c) {
     const double eps = c.eps_h;
-    const V4<T> A{W0[0], W0[1] * nx + W0[2] * ny, W0[3], W0[4] * nx + W0[5] * ny};
-    const V4<T> B{W1[0], W1[1] * nx + W1[2] * ny, W1[3], W1[4] * nx + W1[5] * ny};
-    const T h1ij = 0.5 * (A.x + B.x);
-    T sa = sqrt(A.x), sb = sqrt(B.x);
-    const T u1ij = (sa * (vfac(A.x, eps) * A.y) + sb * (vfac(B.x, eps) * B.y)) / (sa + sb + kEps);
-    const T h2ij = 0.5 * (A.z + B.z);
-    sa = sqrt(A.z); sb = sqrt(B.z);
-    const T u2ij = (sa * (vfac(A.z, eps) * A.w) + sb * (vfac(B.z, eps) * B.w)) / (sa + sb + kEps);
-    const V4<T> D = eig(h1ij, u1ij, h2ij, u2ij, false, c);
-    T lmax = tmax(D.x, D.w);
-    const T b = tmax(fabs(u1ij), fabs(u2ij));
+    const double h1ij = 0.5 * (A.h1 + B.h1);
+    const double fA1 = vfac(A.h1, eps), fB1 = vfac(B.h1, eps);
+    double sa = sqrt(A.h1), sb = sqrt(B.h1);
+    const double u1ij = fmad(sa, fA1 * A.qn1, sb * (fB1 * B.qn1)) / (sa + sb + kEps);
+    const double h2ij = 0.5 * (A.h2 + B.h2);
+    const double fA2 = vfac(A.h2, eps), fB2 = vfac(B.h2, eps);
+    sa = sqrt(A.h2); sb = sqrt(B.h2);
+    const double u2ij = fmad(sa, fA2 * A.qn2, sb * (fB2 * B.qn2)) / (sa + sb + kEps);
+    const V4 D = eig(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
+    double lmax = tmax(D.x, D.w);
+    const double b = tmax(fabs(u1ij), fabs(u2ij));
     if (b > lmax) lmax = b;
     if (lmax < eps) lmax = lmax + eps;
     return len * lmax;
@@ -378,15 +398,15 @@ T edge_initial_wave(const T W0[6], const T W1[6], double nx, double ny, double l
 
 // ---------------------------------------------------------------- state update
 // filtroEstado (Volumen_kernel.cu:92-180); its "complex" block is dead (cf = 0).
-template <class T> inline void filtro(T w[6], const T& dt, const Consts& c) {
+inline void filtro(double w[6], double dt, const Consts& c) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
     for (int layer = 0; layer < 2; ++layer) {
         const int k = 3 * layer;
-        const T x = w[k] / c.eps_h;
-        const T x2 = x * x;
-        const T aux0 = 1.0 / (x2 * x2 + kEps);
-        const T aux = exp_neg(dt * aux0);
+        const double x = w[k] * c.inv_eps;
+        const double x2 = x * x;
+        const double aux0 = 1.0 / fmad(x2, x2, kEps);
+        const double aux = exp_neg(dt * aux0);
         w[k + 1] = w[k + 1] * aux;
         w[k + 2] = w[k + 2] * aux;
     }
@@ -394,12 +414,13 @@ template <class T> inline void filtro(T w[6], const T& dt, const Consts& c) {
         const double vmax = layer ? c.vmax2 : c.vmax1;
         if (vmax > 0.0) {
             const int k = 3 * layer;
-            const T h = w[k];
-            const T f = vfac(h, c.eps_h);
-            T ux = f * w[k + 1], uy = f * w[k + 2];
-            const T u = sqrt(ux * ux + uy * uy);
+            const double h = w[k];
+            const double f = vfac(h, c.eps_h);
+            double ux = f * w[k + 1], uy = f * w[k + 2];
+            const double u = sqrt(fmad(ux, ux, uy * uy));
             if (u > vmax) {
-                ux = ux * (vmax / u); uy = uy * (vmax / u);
+                const double s = vmax / u;
+                ux = ux * s; uy = uy * s;
                 w[k + 1] = ux * h; w[k + 2] = uy * h;
             }
         }
@@ -408,59 +429,68 @@ template <class T> inline void filtro(T w[6], const T& dt, const Consts& c) {
 
 // disImplicita (Volumen_kernel.cu:31-90): semi-implicit interlayer and bottom
 // friction.  Speeds of the previous state `wo` enter the coefficients.
-template <class T> inline void dis_implicita(const T wo[6], T w[6], const T& dt, const Consts& c) {
+inline void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
     const double eps = c.eps_h;
-    const T h1 = w[0], h2 = w[3];
-    const T f1 = vfac(h1, eps), f2 = vfac(h2, eps);
-    T u1x = f1 * w[1], u1y = f1 * w[2], u2x = f2 * w[4], u2y = f2 * w[5];
-    const T fo1 = vfac(wo[0], eps), fo2 = vfac(wo[3], eps);
-    const T uo1x = fo1 * wo[1], uo1y = fo1 * wo[2], uo2x = fo2 * wo[4], uo2y = fo2 * wo[5];
-    const T dx = uo1x - uo2x, dy = uo1y - uo2y;
-    const T du = sqrt(dx * dx + dy * dy);
-    const T u1 = sqrt(uo1x * uo1x + uo1y * uo1y);
-    const T u2 = sqrt(uo2x * uo2x + uo2y * uo2y);
-    const T hmod = h2 + c.r * h1;
-    const T m = (hmod > eps * (1.0 + c.r)) ? hmod : T(eps * (1.0 + c.r));
-    const T hm2 = hmod * hmod, m2 = m * m;
-    const T hmodm = sqrt(hm2 * hm2 + m2 * m2);
+    const double h1 = w[0], h2 = w[3];
+    const double f1 = vfac(h1, eps), f2 = vfac(h2, eps);
+    double u1x = f1 * w[1], u1y = f1 * w[2], u2x = f2 * w[4], u2y = f2 * w[5];
+    const double fo1 = vfac(wo[0], eps), fo2 = vfac(wo[3], eps);
+    const double uo1x = fo1 * wo[1], uo1y = fo1 * wo[2], uo2x = fo2 * wo[4], uo2y = fo2 * wo[5];
+    const double dx = uo1x - uo2x, dy = uo1y - uo2y;
+    const double du = sqrt(fmad(dx, dx, dy * dy));
+    const double u1 = sqrt(fmad(uo1x, uo1x, uo1y * uo1y));
+    const double u2 = sqrt(fmad(uo2x, uo2x, uo2y * uo2y));
     if ((h1 > 0.0) && (h2 > 0.0)) {
-        const T c1 = dt * kSqrt2 * h2 * hmod / hmodm * c.mfc * du;
-        const T c2 = dt * c.r * kSqrt2 * h1 * hmod / hmodm * c.mfc * du;
-        const T c3 = dt * c.g * c.mfs * c.mfs * u2 / (pow43(h2) + kEps);
-        const T det = 1.0 / ((1.0 + c1) * (1.0 + c2 + c3) - c1 * c2);
-        w[1] = h1 * (u1x * (1.0 + c2 + c3) + c1 * u2x) * det;
-        w[4] = h2 * (u2x * (1.0 + c1) + c2 * u1x) * det;
-        w[2] = h1 * (u1y * (1.0 + c2 + c3) + c1 * u2y) * det;
-        w[5] = h2 * (u2y * (1.0 + c1) + c2 * u1y) * det;
+        const double hmod = fmad(c.r, h1, h2);
+        const double m = (hmod > c.eps_1r) ? hmod : c.eps_1r;
+        const double hm2 = hmod * hmod, m2 = m * m;
+        const double hh = hmod / sqrt(fmad(hm2, hm2, m2 * m2));
+        const double k12 = ((dt * kSqrt2) * hh) * (c.mfc * du);
+        const double c1 = k12 * h2;
+        const double c2 = (k12 * c.r) * h1;
+        const double c3 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
+        const double e1 = 1.0 + c1, e2 = 1.0 + c2 + c3;
+        const double det = 1.0 / fmad(e1, e2, -(c1 * c2));
+        w[1] = (h1 * fmad(u1x, e2, c1 * u2x)) * det;
+        w[4] = (h2 * fmad(u2x, e1, c2 * u1x)) * det;
+        w[2] = (h1 * fmad(u1y, e2, c1 * u2y)) * det;
+        w[5] = (h2 * fmad(u2y, e1, c2 * u1y)) * det;
     }
     if ((h1 > 0.0) && (h2 < eps)) {
         u1x = f1 * w[1]; u1y = f1 * w[2];
-        const T c1 = dt * c.g * c.mf0 * c.mf0 * u1 / (pow43(h1) + kEps);
-        w[1] = h1 * u1x / (1.0 + c1);
-        w[2] = h1 * u1y / (1.0 + c1);
+        const double c1 = ((dt * c.g_mf02) * u1) / (pow43(h1) + kEps);
+        const double inv = 1.0 / (1.0 + c1);
+        w[1] = (h1 * u1x) * inv;
+        w[2] = (h1 * u1y) * inv;
     }
     if ((h2 > 0.0) && (h1 < eps)) {
         u2x = f2 * w[4]; u2y = f2 * w[5];
-        const T c1 = dt * c.g * c.mfs * c.mfs * u2 / (pow43(h2) + kEps);
-        w[4] = h2 * u2x / (1.0 + c1);
-        w[5] = h2 * u2y / (1.0 + c1);
+        const double c1 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
+        const double inv = 1.0 / (1.0 + c1);
+        w[4] = (h2 * u2x) * inv;
+        w[5] = (h2 * u2y) * inv;
     }
 }
 
 // coulomb (Volumen_kernel.cu:7-26): granular stop / slow-down.
-template <class T> inline void coulomb(T w[6], const T& dt, const Consts& c) {
-    T mu = c.mu;
+inline void coulomb(double w[6], double dt, const Consts& c) {
+    if (!(w[3] > 0.0)) {  // no granular layer: the reference's factor is 0
+        w[4] = w[4] * 0.0;
+        w[5] = w[5] * 0.0;
+        return;
+    }
+    double mu = c.mu;
     if (c.law != LSH_FRICTION_COULOMB) {
-        const T u1 = sqrt(w[1] * w[1] + w[2] * w[2]) * vfac(w[0], c.eps_h);
-        const T u2 = sqrt(w[4] * w[4] + w[5] * w[5]) * vfac(w[3], c.eps_h);
+        const double u1 = sqrt(fmad(w[1], w[1], w[2] * w[2])) * vfac(w[0], c.eps_h);
+        const double u2 = sqrt(fmad(w[4], w[4], w[5] * w[5])) * vfac(w[3], c.eps_h);
         mu = friction_mu(w[0], u1, w[3], u2, c);
     }
-    const T sc = fsc_of(w[0], c) * mu * c.g * w[3] * dt * 1.0;
-    const T normq = sqrt(w[4] * w[4] + w[5] * w[5]);
-    T aux = 0.0;
-    if ((normq + sc >= kEps) && (w[3] > 0.0)) aux = (normq >= sc) ? normq / (normq + sc) : T(0.0);
+    const double sc = ((((fsc_of(w[0], c) * mu) * c.g) * w[3]) * dt);
+    const double normq = sqrt(fmad(w[4], w[4], w[5] * w[5]));
+    double aux = 0.0;
+    if ((normq + sc >= kEps) && (normq >= sc)) aux = normq / (normq + sc);
     w[4] = w[4] * aux;
     w[5] = w[5] * aux;
 }
@@ -468,18 +498,18 @@ template <class T> inline void coulomb(T w[6], const T& dt, const Consts& c) {
 // obtenerEstadoYDeltaTVolumenesGPU (Volumen_kernel.cu:231-284) for one cell:
 // per-cell dt from the wave accumulator, forward Euler stage, the spherical
 // metric source (new), then filtroEstado -> disImplicita -> coulomb.
-template <class T>
-inline void volume_update(const T wo[6], const T acc[7], T w[6], T& dti, double area, double tanR,
-                          const T& dt, const Consts& c) {
-    dti = (acc[6] < kEps) ? T(kBig) : (2.0 * c.cfl * area) / acc[6];
-    const T b = dt / area;
-    for (int k = 0; k < 6; ++k) w[k] = wo[k] + b * acc[k];
+inline void volume_update(const double wo[6], const double acc[7], double w[6], double& dti, double area,
+                          double inv_area, double tanR, double dt, const Consts& c) {
+    dti = (acc[6] < kEps) ? kBig : ((2.0 * c.cfl) * area) / acc[6];
+    const double b = dt * inv_area;
+    for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
     if (tanR != 0.0) {
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
-            const T ux = vfac(wo[k], c.eps_h) * wo[k + 1];
-            w[k + 1] = w[k + 1] + dt * (ux * wo[k + 2] * tanR);
-            w[k + 2] = w[k + 2] - dt * (ux * wo[k + 1] * tanR);
+            const double ux = vfac(wo[k], c.eps_h) * wo[k + 1];
+            const double s = dt * (ux * tanR);
+            w[k + 1] = fmad(s, wo[k + 2], w[k + 1]);
+            w[k + 2] = fmad(-s, wo[k + 1], w[k + 2]);
         }
     }
     filtro(w, dt, c);
@@ -507,24 +537,74 @@ struct Solver {
     }
 
     // Face value of cell `id` on side `side` (0 W, 1 E, 2 S (toward j-1), 3 N
-    // (toward j+1)).  First order (or a cell whose slopes were zeroed): the
-    // cell value itself.
-    void face(const double* const* W, size_t id, int side, double out[6], double& Hf) const {
-        if (p.order != 2) {
-            for (int k = 0; k < 6; ++k) out[k] = W[k][id];
-            Hf = W[6][id];
-            return;
+    // (toward j+1)) in the edge frame of normal (nx, ny): normal discharge
+    // q.n and tangential q_y nx - q_x ny (Arista_kernel.cu:363-371, 509-525).
+    // First order (or a cell whose slopes were zeroed): the cell value itself.
+    Face face(const double* const* W, size_t id, int side, double nxv, double nyv) const {
+        double w[6], Hf;
+        for (int k = 0; k < 6; ++k) w[k] = W[k][id];
+        Hf = W[6][id];
+        if (p.order == 2) {
+            const std::vector<double>* s = (side < 2) ? slope_x : slope_y;
+            const double sg = (side & 1) ? 1.0 : -1.0;
+            const double de1 = s[0][id], de2 = s[3][id], dH = s[6][id];
+            w[0] = w[0] + sg * (de1 - de2);
+            w[1] = w[1] + sg * s[1][id];
+            w[2] = w[2] + sg * s[2][id];
+            w[3] = w[3] + sg * (de2 + dH);
+            w[4] = w[4] + sg * s[4][id];
+            w[5] = w[5] + sg * s[5][id];
+            Hf = Hf + sg * dH;
         }
-        const std::vector<double>* s = (side < 2) ? slope_x : slope_y;
-        const double sg = (side & 1) ? 1.0 : -1.0;
-        const double de1 = s[0][id], de2 = s[3][id], dH = s[6][id];
-        out[0] = W[0][id] + sg * (de1 - de2);
-        out[1] = W[1][id] + sg * s[1][id];
-        out[2] = W[2][id] + sg * s[2][id];
-        out[3] = W[3][id] + sg * (de2 + dH);
-        out[4] = W[4][id] + sg * s[4][id];
-        out[5] = W[5][id] + sg * s[5][id];
-        Hf = W[6][id] + sg * dH;
+        Face f;
+        f.h1 = w[0]; f.qn1 = w[1] * nxv + w[2] * nyv; f.qt1 = w[2] * nxv - w[1] * nyv;
+        f.h2 = w[3]; f.qn2 = w[4] * nxv + w[5] * nyv; f.qt2 = w[5] * nxv - w[4] * nyv;
+        f.H = Hf;
+        return f;
+    }
+
+    // The edge of colour pass (dir, par) number (line, along): its cells,
+    // outward normal of cell 0, length and boundary factor
+    // (Arista_kernel.cu:651-838: vertical edge x between columns x-1 and x,
+    // horizontal edge y between rows y-1 and y; row 0's outer edge is "sup").
+    struct EdgeGeo { size_t id0, id1; bool interior; double nx, ny, len, bor; int side0, side1; };
+    EdgeGeo edge_geo(int dir, int e, int s) const {
+        EdgeGeo q;
+        q.id1 = 0;
+        q.bor = 0.0;
+        const size_t NX = size_t(nx);
+        if (dir == 0) {
+            const int x = s, y = e;
+            q.len = g.len_h[y]; q.nx = 0.0; q.side1 = 2;
+            if (y == 0) { q.id0 = size_t(x); q.ny = -1.0; q.interior = false; q.bor = p.borde_sup; q.side0 = 2; }
+            else if (y == ny) { q.id0 = size_t(ny - 1) * NX + x; q.ny = 1.0; q.interior = false; q.bor = p.borde_inf; q.side0 = 3; }
+            else { q.id0 = size_t(y - 1) * NX + x; q.id1 = q.id0 + NX; q.ny = 1.0; q.interior = true; q.side0 = 3; }
+        } else {
+            const int x = e, y = s;
+            q.len = g.len_v[y]; q.ny = 0.0; q.side1 = 0;
+            if (x == 0) { q.id0 = size_t(y) * NX; q.nx = -1.0; q.interior = false; q.bor = p.borde_izq; q.side0 = 0; }
+            else if (x == nx) { q.id0 = size_t(y) * NX + NX - 1; q.nx = 1.0; q.interior = false; q.bor = p.borde_der; q.side0 = 1; }
+            else { q.id0 = size_t(y) * NX + x - 1; q.id1 = q.id0 + 1; q.nx = 1.0; q.interior = true; q.side0 = 1; }
+        }
+        return q;
+    }
+
+    // ghost face: the cell's own face with the normal discharges times the
+    // boundary factor (:689-695, 776-782)
+    static Face ghost(const Face& a, double bor) {
+        Face b = a;
+        b.qn1 = a.qn1 * bor;
+        b.qn2 = a.qn2 * bor;
+        return b;
+    }
+
+    // the cell value in the edge frame (the initial-dt pass is first order)
+    static Face face_cell(const double* const* W, size_t id, double nxv, double nyv) {
+        Face f;
+        f.h1 = W[0][id]; f.qn1 = W[1][id] * nxv + W[2][id] * nyv; f.qt1 = W[2][id] * nxv - W[1][id] * nyv;
+        f.h2 = W[3][id]; f.qn2 = W[4][id] * nxv + W[5][id] * nyv; f.qt2 = W[5][id] * nxv - W[4][id] * nyv;
+        f.H = W[6][id];
+        return f;
     }
 
     static double minmod(double a, double b) {
@@ -578,55 +658,50 @@ struct Solver {
 #pragma omp parallel for schedule(static)
         for (int t = 0; t < nlines; ++t) {
             const int e = par + 2 * t;  // edge row y (dir 0) or column x (dir 1)
-            if ((dir == 0 && e > NY) || (dir == 1 && e > NX)) continue;
             for (int s = 0; s < nalong; ++s) {
-                EdgeIn<double> in;
-                size_t id0, id1 = 0;
-                double bor;
-                int side0, side1;
-                if (dir == 0) {
-                    const int x = s, y = e;
-                    in.len = g.len_h[y];
-                    if (y == 0) { id0 = size_t(x); in.nx = 0.0; in.ny = -1.0; in.interior = false; bor = p.borde_sup; side0 = 2; }
-                    else if (y == NY) { id0 = size_t(NY - 1) * NX + x; in.nx = 0.0; in.ny = 1.0; in.interior = false; bor = p.borde_inf; side0 = 3; }
-                    else { id0 = size_t(y - 1) * NX + x; id1 = id0 + NX; in.nx = 0.0; in.ny = 1.0; in.interior = true; bor = 0.0; side0 = 3; }
-                    side1 = 2;
-                } else {
-                    const int x = e, y = s;
-                    in.len = g.len_v[y];
-                    if (x == 0) { id0 = size_t(y) * NX; in.nx = -1.0; in.ny = 0.0; in.interior = false; bor = p.borde_izq; side0 = 0; }
-                    else if (x == NX) { id0 = size_t(y) * NX + NX - 1; in.nx = 1.0; in.ny = 0.0; in.interior = false; bor = p.borde_der; side0 = 1; }
-                    else { id0 = size_t(y) * NX + x - 1; id1 = id0 + 1; in.nx = 1.0; in.ny = 0.0; in.interior = true; bor = 0.0; side0 = 1; }
-                    side1 = 0;
-                }
-                const int row0 = int(id0 / NX);
-                face(W, id0, side0, in.W0, in.H0);
+                const EdgeGeo q = edge_geo(dir, e, s);
+                EdgeIn in;
+                in.len = q.len;
+                in.interior = q.interior;
+                const size_t row0 = q.id0 / NX;
+                in.A = face(W, q.id0, q.side0, q.nx, q.ny);
                 in.area0 = g.area[row0];
-                in.hc0[0] = W[0][id0]; in.hc0[1] = W[3][id0];
-                in.acc0h[0] = acc[0][id0]; in.acc0h[1] = acc[3][id0];
-                if (in.interior) {
-                    face(W, id1, side1, in.W1, in.H1);
-                    in.area1 = g.area[id1 / NX];
-                    in.hc1[0] = W[0][id1]; in.hc1[1] = W[3][id1];
-                    in.acc1h[0] = acc[0][id1]; in.acc1h[1] = acc[3][id1];
+                in.inv_area0 = g.inv_area[row0];
+                in.hc0[0] = W[0][q.id0]; in.hc0[1] = W[3][q.id0];
+                in.acc0h[0] = acc[0][q.id0]; in.acc0h[1] = acc[3][q.id0];
+                if (q.interior) {
+                    const size_t row1 = q.id1 / NX;
+                    in.B = face(W, q.id1, q.side1, q.nx, q.ny);
+                    in.area1 = g.area[row1];
+                    in.inv_area1 = g.inv_area[row1];
+                    in.hc1[0] = W[0][q.id1]; in.hc1[1] = W[3][q.id1];
+                    in.acc1h[0] = acc[0][q.id1]; in.acc1h[1] = acc[3][q.id1];
                 } else {
-                    // ghost cell: normal discharge times the boundary factor (:689-695, 776-782)
-                    for (int k = 0; k < 6; ++k) in.W1[k] = in.W0[k];
-                    const int kn = (dir == 0) ? 2 : 1;
-                    in.W1[kn] = in.W0[kn] * bor;
-                    in.W1[kn + 3] = in.W0[kn + 3] * bor;
-                    in.H1 = in.H0;
+                    in.B = ghost(in.A, q.bor);
                     in.area1 = in.area0;
+                    in.inv_area1 = in.inv_area0;
                     in.hc1[0] = in.hc1[1] = 0.0;
                     in.acc1h[0] = in.acc1h[1] = 0.0;
                 }
-                double d0[6], d1[6], wave;
-                if (!edge_flux(in, dt, c, d0, d1, wave)) continue;
-                for (int k = 0; k < 6; ++k) acc[k][id0] -= d0[k];
-                acc[6][id0] += wave;
-                if (in.interior) {
-                    for (int k = 0; k < 6; ++k) acc[k][id1] -= d1[k];
-                    acc[6][id1] += wave;
+                EdgeOut o;
+                if (!edge_flux(in, dt, c, o)) continue;
+                // rotate the normal-frame fluxes back: x = fn nx - ft ny, y = fn ny + ft nx
+                const double nxv = q.nx, nyv = q.ny;
+                double d0[6], d1[6];
+                for (int l = 0; l < 2; ++l) {
+                    const int k = 3 * l;
+                    d0[k] = o.m[k];
+                    d0[k + 1] = o.m[k + 1] * nxv - o.m[k + 2] * nyv;
+                    d0[k + 2] = o.m[k + 1] * nyv + o.m[k + 2] * nxv;
+                    d1[k] = o.p[k];
+                    d1[k + 1] = o.p[k + 1] * nxv - o.p[k + 2] * nyv;
+                    d1[k + 2] = o.p[k + 1] * nyv + o.p[k + 2] * nxv;
+                }
+                for (int k = 0; k < 6; ++k) acc[k][q.id0] -= d0[k];
+                acc[6][q.id0] += o.wave;
+                if (q.interior) {
+                    for (int k = 0; k < 6; ++k) acc[k][q.id1] -= d1[k];
+                    acc[6][q.id1] += o.wave;
                 }
             }
         }
@@ -643,10 +718,10 @@ struct Solver {
                 const double gh1 = c.g * W[0][id], gh2 = c.g * W[3][id];
                 const double e1x = 2.0 * slope_x[0][id], e2x = 2.0 * slope_x[3][id];
                 const double e1y = 2.0 * slope_y[0][id], e2y = 2.0 * slope_y[3][id];
-                acc[1][id] -= c.peso * (gh1 * e1x * g.wx[j]);
-                acc[4][id] -= c.peso * (gh2 * ((1.0 - c.r) * e2x + c.r * e1x) * g.wx[j]);
-                acc[2][id] -= c.peso * (gh1 * e1y * g.wy[j]);
-                acc[5][id] -= c.peso * (gh2 * ((1.0 - c.r) * e2y + c.r * e1y) * g.wy[j]);
+                acc[1][id] -= c.peso * ((gh1 * e1x) * g.wx[j]);
+                acc[4][id] -= c.peso * ((gh2 * fmad(c.omr, e2x, c.r * e1x)) * g.wx[j]);
+                acc[2][id] -= c.peso * ((gh1 * e1y) * g.wy[j]);
+                acc[5][id] -= c.peso * ((gh2 * fmad(c.omr, e2y, c.r * e1y)) * g.wy[j]);
             }
         }
     }
@@ -670,7 +745,7 @@ struct Solver {
                 double wo[6], a[7], w[6], d;
                 for (int k = 0; k < 6; ++k) wo[k] = W[k][id];
                 for (int k = 0; k < 7; ++k) a[k] = acc[k][id];
-                volume_update(wo, a, w, d, g.area[j], g.tanR[j], dt, c);
+                volume_update(wo, a, w, d, g.area[j], g.inv_area[j], g.tanR[j], dt, c);
                 for (int k = 0; k < 6; ++k) Wn[k][id] = w[k];
                 if (d < mn) mn = d;
             }
@@ -691,33 +766,12 @@ struct Solver {
                     const int e = par + 2 * t;
                     if ((dir == 0 && e > NY) || (dir == 1 && e > NX)) continue;
                     for (int s = 0; s < nalong; ++s) {
-                        size_t id0, id1 = 0;
-                        double nxv, nyv, bor, len;
-                        bool interior;
-                        if (dir == 0) {
-                            const int x = s, y = e;
-                            len = g.len_h[y];
-                            if (y == 0) { id0 = size_t(x); nxv = 0; nyv = -1; interior = false; bor = p.borde_sup; }
-                            else if (y == NY) { id0 = size_t(NY - 1) * NX + x; nxv = 0; nyv = 1; interior = false; bor = p.borde_inf; }
-                            else { id0 = size_t(y - 1) * NX + x; id1 = id0 + NX; nxv = 0; nyv = 1; interior = true; bor = 0; }
-                        } else {
-                            const int x = e, y = s;
-                            len = g.len_v[y];
-                            if (x == 0) { id0 = size_t(y) * NX; nxv = -1; nyv = 0; interior = false; bor = p.borde_izq; }
-                            else if (x == NX) { id0 = size_t(y) * NX + NX - 1; nxv = 1; nyv = 0; interior = false; bor = p.borde_der; }
-                            else { id0 = size_t(y) * NX + x - 1; id1 = id0 + 1; nxv = 1; nyv = 0; interior = true; bor = 0; }
-                        }
-                        double W0[6], W1[6];
-                        for (int k = 0; k < 6; ++k) W0[k] = W[k][id0];
-                        if (interior) for (int k = 0; k < 6; ++k) W1[k] = W[k][id1];
-                        else {
-                            for (int k = 0; k < 6; ++k) W1[k] = W0[k];
-                            const int kn = (dir == 0) ? 2 : 1;
-                            W1[kn] = W0[kn] * bor; W1[kn + 3] = W0[kn + 3] * bor;
-                        }
-                        const double wv = edge_initial_wave(W0, W1, nxv, nyv, len, c);
-                        aw[id0] += wv;
-                        if (interior) aw[id1] += wv;
+                        const EdgeGeo q = edge_geo(dir, e, s);
+                        const Face A = face_cell(W, q.id0, q.nx, q.ny);
+                        const Face B = q.interior ? face_cell(W, q.id1, q.nx, q.ny) : ghost(A, q.bor);
+                        const double wv = edge_initial_wave(A, B, q.len, c);
+                        aw[q.id0] += wv;
+                        if (q.interior) aw[q.id1] += wv;
                     }
                 }
             }
@@ -726,7 +780,7 @@ struct Solver {
         for (int j = 0; j < NY; ++j)
             for (int i = 0; i < NX; ++i) {
                 const double a = aw[size_t(j) * NX + i];
-                const double d = (a < kEps) ? kBig : (2.0 * c.cfl * g.area[j]) / a;  // Volumen_kernel.cu:226
+                const double d = (a < kEps) ? kBig : ((2.0 * c.cfl) * g.area[j]) / a;  // Volumen_kernel.cu:226
                 if (d < mn) mn = d;
             }
         return mn;

@@ -14,11 +14,26 @@ from datafiles import write_case
 pytestmark = pytest.mark.gpu
 
 
+def f32(x):
+    return float(np.float32(x))
+
+
+def float_params(p):
+    """shallowWater() takes its parameters as float (main.cxx:157-164 casts
+    every one); the replay must use the same rounded values."""
+    q = p.copy()
+    for name, typ in q._fields_:
+        if typ.__name__ == "c_double":
+            setattr(q, name, f32(getattr(q, name)))
+    return q
+
+
 def oracle_replay(oracle, pr):
     """Replay the reference loop on the oracle; returns the snapshot states
     (with their times), the final state and the eta1 max (as float32 after
     the shim's float conversion of the input)."""
-    p = pr.params.copy()
+    p = float_params(pr.params)
+    p.radius = pr.params.radius
     st = {v: pr.state[v].astype(np.float32).astype(np.float64) for v in VARS}
     arrs = oracle.state_arrays(st)
     em = arrs[0] + arrs[3] - arrs[6]
@@ -26,10 +41,11 @@ def oracle_replay(oracle, pr):
     t, dt = 0.0, oracle.initial_dt(p, arrs)
     nxt = 0.0
     snaps = []
-    while t < pr.tiempo_tot:
-        if pr.tiempo_guardar >= 0 and t >= nxt:
+    t_tot, t_save = f32(pr.tiempo_tot), f32(pr.tiempo_guardar)
+    while t < t_tot:
+        if t_save >= 0 and t >= nxt:
             snaps.append((t, [a.copy() for a in arrs]))
-            nxt += pr.tiempo_guardar
+            nxt += t_save
         t, dt, _ = oracle.run(p, arrs, 1, t=t, dt=dt, eta=(em, et))
     return snaps, arrs, em, et
 
@@ -50,7 +66,7 @@ def test_shallow_water_entry_point(gpu_lib, oracle, tmp_path, monkeypatch, gauge
     for k, v in enumerate(VARS[:6]):
         assert np.array_equal(out[v], arrs[k].astype(np.float32)), v
     assert np.array_equal(eta[..., 0], em.astype(np.float32))
-    H, Q, T, hmin = pr.params.H, pr.Q, pr.T, pr.hmin
+    H, Q, T, hmin = f32(pr.params.H), f32(pr.Q), f32(pr.T), f32(pr.hmin)
     if not gauges:
         from scipy.io import netcdf_file
         with netcdf_file(str(tmp_path / "out" / "run1_eta1.nc"), "r", mmap=False) as d:
