@@ -41,7 +41,7 @@ using lsh::TimeRec;
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
-constexpr unsigned long long kDtInitBits = 0x7fefffffffffffffULL;  // DBL_MAX
+constexpr unsigned long long kRateInitBits = 0ULL;  // +0.0
 constexpr int kEdgeBlock = 128;
 constexpr int kCellBlock = 256;
 constexpr int kGraphChunk = 16;
@@ -299,24 +299,26 @@ __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
     }
 }
 
-__device__ __forceinline__ void block_min_bits(unsigned long long v, TimeRec* tm) {
+// Block max of the per-cell rates (non-negative doubles order like their bit
+// patterns), then one 64-bit atomicMax per block.
+__device__ __forceinline__ void block_max_bits(unsigned long long v, TimeRec* tm) {
     __shared__ unsigned long long red[kCellBlock / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
-        v = (w < v) ? w : v;
+        v = (w > v) ? w : v;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kDtInitBits;
+        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kRateInitBits;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
-            v = (w < v) ? w : v;
+            v = (w > v) ? w : v;
         }
-        if (lane == 0) atomicMin(&tm->dtmin_bits, v);
+        if (lane == 0) atomicMax(&tm->rmax_bits, v);
     }
 }
 
@@ -328,10 +330,10 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
     const int nx = a.c.nx, ny = a.c.ny;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     const double dt = a.tm->dt;
-    unsigned long long bits = kDtInitBits;
+    unsigned long long bits = kRateInitBits;
     if (id < nx * ny) {
         const int j = id / nx;
-        double wo[6], acc[7], w[6], dti;
+        double wo[6], acc[7], w[6], rate;
 #pragma unroll
         for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
 #pragma unroll
@@ -352,7 +354,7 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
         if (still) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = wo[k];
-            dti = lsh::kBig;
+            rate = 0.0;
         } else {
             if (a.c.order == 2) {
                 // cell-midpoint integral of g h d(eta) over the reconstructed cell
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
                 acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
                 acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
             }
-            lsh::volume_update(wo, acc, w, dti, a.geo.area[j], a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
+            lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
         }
         if (MODE == 2) {
 #pragma unroll
@@ -375,19 +377,25 @@ __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
         if (bad) atomicOr(&a.tm->err, 1 << LSH_ERR_NUMERIC);
-        bits = (unsigned long long)__double_as_longlong(dti);
+        bits = (unsigned long long)__double_as_longlong(rate);
     }
-    if (MODE != 2) block_min_bits(bits, a.tm);
+    if (MODE != 2) block_max_bits(bits, a.tm);
+}
+
+// dt from the largest acc_w / area: 2 CFL / max rate, 1e30 when no cell has a wave speed
+__device__ __forceinline__ double dt_of(unsigned long long rmax_bits, double two_cfl) {
+    const double m = __longlong_as_double((long long)rmax_bits);
+    return (m > 0.0) ? two_cfl / m : lsh::kBig;
 }
 
 // Advance the device clock: t += dt, dt = min per-cell dt (ShallowWater.cu:436-442).
-__global__ void k_advance(TimeRec* tm) {
+__global__ void k_advance(TimeRec* tm, double two_cfl) {
     if (tm->done) return;
     tm->t += tm->dt;
     tm->steps += 1;
-    const double nd = __longlong_as_double((long long)tm->dtmin_bits);
+    const double nd = dt_of(tm->rmax_bits, two_cfl);
     tm->dt = nd;
-    tm->dtmin_bits = kDtInitBits;
+    tm->rmax_bits = kRateInitBits;
     if (tm->t >= tm->t_end) tm->done = 1;
     if (tm->dt_min > 0.0 && nd < tm->dt_min) { tm->err |= 1 << LSH_ERR_STALL; tm->done = 1; }
     if (tm->err) tm->done = 1;
@@ -447,19 +455,19 @@ __global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
 __global__ void __launch_bounds__(kCellBlock) k_cell_dt(KArgs a) {
     const int nx = a.c.nx, ny = a.c.ny;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long bits = kDtInitBits;
+    unsigned long long bits = kRateInitBits;
     if (id < nx * ny) {
         const int j = id / nx;
         const double w = a.acc[6][id];
-        const double d = (w < lsh::kEps) ? lsh::kBig : ((2.0 * a.c.cfl) * a.geo.area[j]) / w;
-        bits = (unsigned long long)__double_as_longlong(d);
+        const double rate = (w < lsh::kEps) ? 0.0 : w * a.geo.inv_area[j];
+        bits = (unsigned long long)__double_as_longlong(rate);
     }
-    block_min_bits(bits, a.tm);
+    block_max_bits(bits, a.tm);
 }
 
-__global__ void k_init_finish(TimeRec* tm) {
-    tm->dt = __longlong_as_double((long long)tm->dtmin_bits);
-    tm->dtmin_bits = kDtInitBits;
+__global__ void k_init_finish(TimeRec* tm, double two_cfl) {
+    tm->dt = dt_of(tm->rmax_bits, two_cfl);
+    tm->rmax_bits = kRateInitBits;
     tm->t = 0.0;
     tm->steps = 0;
     tm->done = 0;
@@ -569,6 +577,7 @@ Consts make_consts(const lsh_params& p) {
     c.eps_1r = p.eps_h * (1.0 + p.r);
     c.g_mf02 = (p.gravity * p.mf0) * p.mf0;
     c.g_mfs2 = (p.gravity * p.mfs) * p.mfs;
+    c.sqrt_g = std::sqrt(p.gravity);
     c.law = p.friction_law; c.order = p.order; c.nx = p.nx; c.ny = p.ny; c.track_eta = p.track_eta_max;
     c.eig_sort = p.eig_sort;
     return c;
@@ -652,7 +661,7 @@ int enqueue_step(const lsh_ctx* ctx, cudaStream_t s) {
         for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
         enqueue_passes<1>(ctx, a, s);
         k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
-        k_advance<<<1, 1, 0, s>>>(ctx->tm);
+        k_advance<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
         return 6;
     }
     KArgs a1 = base_args(ctx);
@@ -668,7 +677,7 @@ int enqueue_step(const lsh_ctx* ctx, cudaStream_t s) {
     k_recon<<<nb, kCellBlock, 0, s>>>(a2);
     enqueue_passes<2>(ctx, a2, s);
     k_volume<2><<<nb, kCellBlock, 0, s>>>(a2);
-    k_advance<<<1, 1, 0, s>>>(ctx->tm);
+    k_advance<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
     return 13;
 }
 
@@ -702,7 +711,7 @@ int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKin
     cudaStream_t s = ctx->stream;
     k_init_eta<<<nb, kCellBlock, 0, s>>>(a);
     TimeRec init{};
-    init.dtmin_bits = kDtInitBits;
+    init.rmax_bits = kRateInitBits;
     init.t_end = INFINITY;
     init.dt_min = ctx->p.dt_min;
     LSH_CUDA(cudaMemcpyAsync(ctx->tm, &init, sizeof(TimeRec), cudaMemcpyHostToDevice, s));
@@ -711,7 +720,7 @@ int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKin
     k_init_wave<1, false><<<dim3(((ctx->p.nx) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
     k_init_wave<1, false><<<dim3(((ctx->p.nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
     k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
-    k_init_finish<<<1, 1, 0, s>>>(ctx->tm);
+    k_init_finish<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
     ctx->launches += 7;
     LSH_CUDA(cudaGetLastError());
     LSH_CUDA(cudaMemcpyAsync(ctx->tm_host, ctx->tm, sizeof(TimeRec), cudaMemcpyDeviceToHost, s));
@@ -1024,7 +1033,7 @@ int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels) {
             mark();
         }
     }
-    k_advance<<<1, 1, 0, s>>>(ctx->tm); mark();
+    k_advance<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl); mark();
     ctx->launches += nk;
     int status = LSH_OK;
     cudaError_t e = cudaGetLastError();
@@ -1100,9 +1109,9 @@ std::mutex g_noalloc_mu;
 double g_noalloc_geo_host[7 * kNaGeoStride];
 
 // Move the running min of per-cell dt into dt (initial-dt pass of a no-alloc call).
-__global__ void k_noalloc_take_dt(TimeRec* tm) {
-    tm->dt = __longlong_as_double((long long)tm->dtmin_bits);
-    tm->dtmin_bits = kDtInitBits;
+__global__ void k_noalloc_take_dt(TimeRec* tm, double two_cfl) {
+    tm->dt = dt_of(tm->rmax_bits, two_cfl);
+    tm->rmax_bits = kRateInitBits;
 }
 
 // Same per-row formulas as make_geo, written into a caller-provided array.
@@ -1176,7 +1185,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     init.dt = *dt_io;
     init.t_end = INFINITY;
     init.dt_min = p->dt_min;
-    init.dtmin_bits = kDtInitBits;
+    init.rmax_bits = kRateInitBits;
     LSH_CUDA(cudaMemcpyAsync(tm, &init, sizeof(TimeRec), cudaMemcpyHostToDevice, s));
 
     KArgs a;
@@ -1204,7 +1213,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
         k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
         k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
         k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
-        k_noalloc_take_dt<<<1, 1, 0, s>>>(tm);
+        k_noalloc_take_dt<<<1, 1, 0, s>>>(tm, 2.0 * p->cfl);
     }
     const dim3 gh0((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535));
     const dim3 gh1((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535));
@@ -1216,7 +1225,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
         k_edges_v<1><<<gv0, kEdgeBlock, 0, s>>>(a, 0);
         k_edges_v<1><<<gv1, kEdgeBlock, 0, s>>>(a, 1);
         k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
-        k_advance<<<1, 1, 0, s>>>(tm);
+        k_advance<<<1, 1, 0, s>>>(tm, 2.0 * p->cfl);
     }
     LSH_CUDA(cudaGetLastError());
     TimeRec out{};

@@ -35,7 +35,7 @@ struct Consts {
     double g, r, gp, eps_h, peso, beta, cfl, mu, mfc, mf0, mfs, vmax1, vmax2, L, H;
     double tan1, tan2, tan3, tan4;
     // host-derived, with the same formulas as the CPU oracle's make_consts
-    double omr, inv_gp, inv_eps, inv_peso, eps_1r, g_mf02, g_mfs2;
+    double omr, inv_gp, inv_eps, inv_peso, eps_1r, g_mf02, g_mfs2, sqrt_g;
     double borde_sup, borde_inf, borde_izq, borde_der;
     int law;
     int order;
@@ -61,7 +61,7 @@ struct TimeRec {
     double dt;                       // dt of the next step
     double t_end;                    // stop once t >= t_end
     double dt_min;                   // stall guard (0: off)
-    unsigned long long dtmin_bits;   // running min of per-cell dt (bits of a positive double)
+    unsigned long long rmax_bits;    // running max of per-cell acc_w / area (bits of a double >= 0)
     long long steps;                 // steps taken
     int done;                        // 1 once t >= t_end (kernels then return at once)
     int err;                         // sticky error bits (LSH status values as bits)
@@ -75,9 +75,10 @@ __device__ __forceinline__ double max0(double a) { return (a > 0.0) ? a : 0.0; }
 __device__ __forceinline__ double fmad(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ double exp_neg(double x) { return lshm::exp_neg(x); }
 
+// sqrt(2) h / sqrt(h^4 + max(h, eps_h)^4); exactly 1/h for h > eps_h
 __device__ __forceinline__ double vfac(double h, double eps_h) {
-    const double m = (h > eps_h) ? h : eps_h;
-    const double h2 = h * h, m2 = m * m;
+    if (h > eps_h) return 1.0 / h;
+    const double h2 = h * h, m2 = eps_h * eps_h;
     return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
@@ -111,11 +112,14 @@ __device__ __forceinline__ void sort_eig(V4& D, int full) {
 // granular layer is absent (h2 = 0, u2 = 0), so the internal pair is exactly
 // zero and its square root is skipped.
 template <bool L2>
-__device__ __forceinline__ V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c) {
+__device__ __forceinline__ V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c,
+                                  double Fknown = -1.0, double sqrt_h = -1.0) {
     const double h = L2 ? h1 + h2 : h1;
-    const double F = vfac(h, c.eps_h);
+    // single layer: vfac(h1 + 0) is vfac(h1), which the caller may already hold
+    const double F = (!L2 && Fknown >= 0.0) ? Fknown : vfac(h, c.eps_h);
     const double u = q * F;
-    const double cg = sqrt(c.g * h);
+    // sqrt_h >= 0: sqrt(h1) is known and h2 == 0, so sqrt(g h) = sqrt(g) sqrt(h1)
+    const double cg = (sqrt_h >= 0.0) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     double uu = 0.0, ci = 0.0;
     if (L2) {
         uu = fmad(u1, h2, u2 * h1) * F;
@@ -199,13 +203,15 @@ __device__ __forceinline__ void edge_flux(const EdgeIn& e, double dt, const Cons
 
     const double fA1 = vfac(Ah1, eps), fB1 = vfac(Bh1, eps);
     const double fA2 = L2 ? vfac(Ah2, eps) : 0.0, fB2 = L2 ? vfac(Bh2, eps) : 0.0;
-    double sa = sqrt(Ah1), sb = sqrt(Bh1);
-    const double u1ij = fmad(sa, fA1 * Aq1, sb * (fB1 * Bq1)) / (sa + sb + kEps);
+    const double sa1 = sqrt(Ah1), sb1 = sqrt(Bh1);
+    const double u1ij = fmad(sa1, fA1 * Aq1, sb1 * (fB1 * Bq1)) / (sa1 + sb1 + kEps);
     double u2ij = 0.0;
     if (L2) {
-        sa = sqrt(Ah2); sb = sqrt(Bh2);
-        u2ij = fmad(sa, fA2 * Aq2, sb * (fB2 * Bq2)) / (sa + sb + kEps);
+        const double sa2 = sqrt(Ah2), sb2 = sqrt(Bh2);
+        u2ij = fmad(sa2, fA2 * Aq2, sb2 * (fB2 * Bq2)) / (sa2 + sb2 + kEps);
     }
+    // a face's celerity sqrt(g h) is sqrt(g) sqrt(h1) when its granular layer is empty
+    const bool oneA = !L2 || (Ah2 == 0.0), oneB = !L2 || (Bh2 == 0.0);
 
     const double Hm = tmin(H0, H1);
     const double deta1 = L2 ? max0(Bh1 + Bh2 - H1 + Hm) - max0(Ah1 + Ah2 - H0 + Hm)
@@ -224,8 +230,8 @@ __device__ __forceinline__ void edge_flux(const EdgeIn& e, double dt, const Cons
     }
 
     const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, L2 ? fmad(h1ij, u1ij, h2ij * u2ij) : h1ij * u1ij, c);
-    const V4 E0 = eig<L2>(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, L2 ? Aq1 + Aq2 : Aq1, c);
-    const V4 E1 = eig<L2>(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, L2 ? Bq1 + Bq2 : Bq1, c);
+    const V4 E0 = eig<L2>(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, L2 ? Aq1 + Aq2 : Aq1, c, fA1, oneA ? sa1 : -1.0);
+    const V4 E1 = eig<L2>(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, L2 ? Bq1 + Bq2 : Bq1, c, fB1, oneB ? sb1 : -1.0);
     const double aut1 = tmin(D.x, tmin(E0.x, E1.x));
     const double aut3 = tmax(D.w, tmax(E0.w, E1.w));
     double lmax = tmax(fabs(aut3), fabs(aut1));
@@ -361,17 +367,22 @@ __device__ __forceinline__ double edge_initial_wave(const Face& A, const Face& B
     return len * lmax;
 }
 
-// filtroEstado (Volumen_kernel.cu:92-180)
+// filtroEstado (Volumen_kernel.cu:92-180).  L2 == false: h2 = q2 = 0, so
+// the layer-2 damping (0 times a factor) is skipped.
+template <bool L2>
 __device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
 #pragma unroll
-    for (int layer = 0; layer < 2; ++layer) {
+    for (int layer = 0; layer < (L2 ? 2 : 1); ++layer) {
         const int k = 3 * layer;
         const double x = w[k] * c.inv_eps;
         const double x2 = x * x;
-        const double aux0 = 1.0 / fmad(x2, x2, kEps);
-        const double aux = exp_neg(dt * aux0);
+        const double d = fmad(x2, x2, kEps);
+        // exp(-dt/d) is exactly 1 once dt/d < 2^-54: skip the division below a
+        // bound that holds with ample margin over the roundings
+        if (dt < d * 0x1.fp-55) continue;
+        const double aux = exp_neg(dt * (1.0 / d));
         w[k + 1] = w[k + 1] * aux;
         w[k + 2] = w[k + 2] * aux;
     }
@@ -393,19 +404,41 @@ __device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) 
     }
 }
 
-// disImplicita (Volumen_kernel.cu:31-90)
-__device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c) {
+// disImplicita (Volumen_kernel.cu:31-90).  L2 == false: the new and the old
+// granular layer are empty (h2 = q2 = 0): only the water-bottom branch can run.
+// fo1 = vfac(wo[0]), the old state's water factor, computed by the caller.
+template <bool L2>
+__device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c,
+                                              double fo1) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
     const double eps = c.eps_h;
-    const double h1 = w[0], h2 = w[3];
-    const double f1 = vfac(h1, eps), f2 = vfac(h2, eps);
-    double u1x = f1 * w[1], u1y = f1 * w[2], u2x = f2 * w[4], u2y = f2 * w[5];
-    const double fo1 = vfac(wo[0], eps), fo2 = vfac(wo[3], eps);
-    const double uo1x = fo1 * wo[1], uo1y = fo1 * wo[2], uo2x = fo2 * wo[4], uo2y = fo2 * wo[5];
+    const double h1 = w[0], h2 = L2 ? w[3] : 0.0;
+    const double uo1x = fo1 * wo[1], uo1y = fo1 * wo[2];
+    const double u1 = sqrt(fmad(uo1x, uo1x, uo1y * uo1y));
+    if (!L2) {
+        // bottom friction h u / (1 + c1), 1/(1 + X/Y) = Y/(Y + X); above
+        // eps_h, h u is q itself
+        if (h1 > 0.0) {
+            const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1;
+            const double inv = Y / (Y + X);
+            if (h1 > eps) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
+            else {
+                const double f1 = vfac(h1, eps);
+                w[1] = (h1 * (f1 * w[1])) * inv;
+                w[2] = (h1 * (f1 * w[2])) * inv;
+            }
+        }
+        return;
+    }
+    const double f1 = vfac(h1, eps);
+    double u1x = f1 * w[1], u1y = f1 * w[2];
+    const double f2 = vfac(h2, eps);
+    double u2x = f2 * w[4], u2y = f2 * w[5];
+    const double fo2 = vfac(wo[3], eps);
+    const double uo2x = fo2 * wo[4], uo2y = fo2 * wo[5];
     const double dx = uo1x - uo2x, dy = uo1y - uo2y;
     const double du = sqrt(fmad(dx, dx, dy * dy));
-    const double u1 = sqrt(fmad(uo1x, uo1x, uo1y * uo1y));
     const double u2 = sqrt(fmad(uo2x, uo2x, uo2y * uo2y));
     if ((h1 > 0.0) && (h2 > 0.0)) {
         const double hmod = fmad(c.r, h1, h2);
@@ -424,18 +457,16 @@ __device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], d
         w[5] = (h2 * fmad(u2y, e1, c2 * u1y)) * det;
     }
     if ((h1 > 0.0) && (h2 < eps)) {
-        u1x = f1 * w[1]; u1y = f1 * w[2];
-        const double c1 = ((dt * c.g_mf02) * u1) / (pow43(h1) + kEps);
-        const double inv = 1.0 / (1.0 + c1);
-        w[1] = (h1 * u1x) * inv;
-        w[2] = (h1 * u1y) * inv;
+        const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1;
+        const double inv = Y / (Y + X);
+        if (h1 > eps) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
+        else { w[1] = (h1 * (f1 * w[1])) * inv; w[2] = (h1 * (f1 * w[2])) * inv; }
     }
     if ((h2 > 0.0) && (h1 < eps)) {
-        u2x = f2 * w[4]; u2y = f2 * w[5];
-        const double c1 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
-        const double inv = 1.0 / (1.0 + c1);
-        w[4] = (h2 * u2x) * inv;
-        w[5] = (h2 * u2y) * inv;
+        const double Y = pow43(h2) + kEps, X = (dt * c.g_mfs2) * u2;
+        const double inv = Y / (Y + X);
+        if (h2 > eps) { w[4] = w[4] * inv; w[5] = w[5] * inv; }
+        else { w[4] = (h2 * (f2 * w[4])) * inv; w[5] = (h2 * (f2 * w[5])) * inv; }
     }
 }
 
@@ -462,26 +493,39 @@ __device__ __forceinline__ void coulomb(double w[6], double dt, const Consts& c)
 
 // One cell of obtenerEstadoYDeltaTVolumenesGPU (Volumen_kernel.cu:231-284),
 // plus the spherical metric source (tanR = tan(lat)/R, 0 for Cartesian).
-__device__ __forceinline__ void volume_update(const double wo[6], const double acc[7], double w[6], double& dti,
-                                              double area, double inv_area, double tanR, double dt,
-                                              const Consts& c) {
-    dti = (acc[6] < kEps) ? kBig : ((2.0 * c.cfl) * area) / acc[6];
+// `rate` gets acc_w / area (0 below EPSILON): the step's dt is
+// 2 CFL / max(rate), the min over cells of 2 CFL area / acc_w
+// (Volumen_kernel.cu:256) with one division per step.
+__device__ __forceinline__ void volume_update(const double wo[6], const double acc[7], double w[6], double& rate,
+                                              double inv_area, double tanR, double dt, const Consts& c) {
+    rate = (acc[6] < kEps) ? 0.0 : acc[6] * inv_area;
     const double b = dt * inv_area;
 #pragma unroll
     for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
+    const double fo1 = vfac(wo[0], c.eps_h);
     if (tanR != 0.0) {
 #pragma unroll
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
-            const double ux = vfac(wo[k], c.eps_h) * wo[k + 1];
+            if (is_zero(wo[k]) && is_zero(wo[k + 1]) && is_zero(wo[k + 2])) continue;  // adds exactly 0
+            const double ux = (layer ? vfac(wo[k], c.eps_h) : fo1) * wo[k + 1];
             const double s = dt * (ux * tanR);
             w[k + 1] = fmad(s, wo[k + 2], w[k + 1]);
             w[k + 2] = fmad(-s, wo[k + 1], w[k + 2]);
         }
     }
-    filtro(w, dt, c);
-    dis_implicita(wo, w, dt, c);
-    coulomb(w, dt, c);
+    // single layer: the granular layer is empty before and after the Euler
+    // update (h2 = q2 = 0 in both), so its friction and Coulomb terms are zeros
+    if (is_zero(wo[3]) && is_zero(wo[4]) && is_zero(wo[5]) && is_zero(w[3]) && is_zero(w[4]) && is_zero(w[5])) {
+        filtro<false>(w, dt, c);
+        dis_implicita<false>(wo, w, dt, c, fo1);
+        w[4] = w[4] * 0.0;  // coulomb() with h2 = 0
+        w[5] = w[5] * 0.0;
+    } else {
+        filtro<true>(w, dt, c);
+        dis_implicita<true>(wo, w, dt, c, fo1);
+        coulomb(w, dt, c);
+    }
 }
 
 }  // namespace lsh

@@ -69,6 +69,7 @@ struct Consts {
     double eps_1r;    // eps_h (1 + r)
     double g_mf02;    // g mf0^2
     double g_mfs2;    // g mfs^2
+    double sqrt_g;    // sqrt(g)
     int law;
     int eig_sort;
 };
@@ -99,6 +100,7 @@ static Consts make_consts(const lsh_params& p) {
     c.eps_1r = p.eps_h * (1.0 + p.r);
     c.g_mf02 = (p.gravity * p.mf0) * p.mf0;
     c.g_mfs2 = (p.gravity * p.mfs) * p.mfs;
+    c.sqrt_g = std::sqrt(p.gravity);
     c.law = p.friction_law;
     c.eig_sort = p.eig_sort;
     return c;
@@ -148,10 +150,11 @@ inline double fmad(double a, double b, double c) { return lshm::fmad(a, b, c); }
 inline double exp_neg(double x) { return lshm::exp_neg(x); }
 
 // sqrt(2) h / sqrt(h^4 + max(h, eps_h)^4): the desingularised 1/h factor
-// (Arista_kernel.cu:74,380; Volumen_kernel.cu:13,44,48)
+// (Arista_kernel.cu:74,380; Volumen_kernel.cu:13,44,48).  For h > eps_h the
+// expression is exactly 1/h, which is how it is evaluated there.
 inline double vfac(double h, double eps_h) {
-    const double m = (h > eps_h) ? h : eps_h;
-    const double h2 = h * h, m2 = m * m;
+    if (h > eps_h) return 1.0 / h;
+    const double h2 = h * h, m2 = eps_h * eps_h;
     return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
@@ -175,11 +178,12 @@ inline void sort_eig(V4& D, int full) {
 // aproximarAutovalores1D (Arista_kernel.cu:152-237) given the two layers'
 // depths, velocities (u1, u2) and the total normal discharge q:
 // external u -+ sqrt(g h), internal uu -+ sqrt(g' h1 h2 F |1 - (u1-u2)^2 F / g'|).
-inline V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c) {
+// sqrt_h >= 0: sqrt(h1) is known and h2 == 0, so sqrt(g h) = sqrt(g) sqrt(h1).
+inline V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c, double sqrt_h = -1.0) {
     const double h = h1 + h2;
     const double F = vfac(h, c.eps_h);
     const double u = q * F;
-    const double cg = sqrt(c.g * h);
+    const double cg = (sqrt_h >= 0.0) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     const double uu = fmad(u1, h2, u2 * h1) * F;
     const double d = u1 - u2;
     const double aux = fmad(-((d * d) * F), c.inv_gp, 1.0);
@@ -259,10 +263,12 @@ bool edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     // Roe-type averages (Arista_kernel.cu:375-395)
     const double fA1 = vfac(Ah1, eps), fB1 = vfac(Bh1, eps);
     const double fA2 = vfac(Ah2, eps), fB2 = vfac(Bh2, eps);
-    double sa = sqrt(Ah1), sb = sqrt(Bh1);
-    const double u1ij = fmad(sa, fA1 * Aq1, sb * (fB1 * Bq1)) / (sa + sb + kEps);
-    sa = sqrt(Ah2); sb = sqrt(Bh2);
-    const double u2ij = fmad(sa, fA2 * Aq2, sb * (fB2 * Bq2)) / (sa + sb + kEps);
+    const double sa1 = sqrt(Ah1), sb1 = sqrt(Bh1);
+    const double u1ij = fmad(sa1, fA1 * Aq1, sb1 * (fB1 * Bq1)) / (sa1 + sb1 + kEps);
+    const double sa2 = sqrt(Ah2), sb2 = sqrt(Bh2);
+    const double u2ij = fmad(sa2, fA2 * Aq2, sb2 * (fB2 * Bq2)) / (sa2 + sb2 + kEps);
+    // a cell's celerity sqrt(g h) is sqrt(g) sqrt(h1) when its granular layer is empty
+    const bool oneA = (Ah2 == 0.0), oneB = (Bh2 == 0.0);
 
     // hydrostatic reconstruction (terminosPresion1D, :94-115)
     const double Hm = tmin(H0, H1);
@@ -280,8 +286,8 @@ bool edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
 
     // eigenvalue bounds (:427-444)
     const V4 D = eig(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
-    const V4 E0 = eig(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, Aq1 + Aq2, c);
-    const V4 E1 = eig(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, Bq1 + Bq2, c);
+    const V4 E0 = eig(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, Aq1 + Aq2, c, oneA ? sa1 : -1.0);
+    const V4 E1 = eig(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, Bq1 + Bq2, c, oneB ? sb1 : -1.0);
     const double aut1 = tmin(D.x, tmin(E0.x, E1.x));
     const double aut3 = tmax(D.w, tmax(E0.w, E1.w));
     double lmax = tmax(fabs(aut3), fabs(aut1));
@@ -405,8 +411,12 @@ inline void filtro(double w[6], double dt, const Consts& c) {
         const int k = 3 * layer;
         const double x = w[k] * c.inv_eps;
         const double x2 = x * x;
-        const double aux0 = 1.0 / fmad(x2, x2, kEps);
-        const double aux = exp_neg(dt * aux0);
+        const double d = fmad(x2, x2, kEps);
+        // exp(-dt / d) is exactly 1 once dt / d < 2^-54; below this bound
+        // (conservative by far more than the roundings of 1/d and dt*(1/d))
+        // the factor is 1 and the division is not needed
+        if (dt < d * 0x1.fp-55) continue;
+        const double aux = exp_neg(dt * (1.0 / d));
         w[k + 1] = w[k + 1] * aux;
         w[k + 2] = w[k + 2] * aux;
     }
@@ -458,19 +468,20 @@ inline void dis_implicita(const double wo[6], double w[6], double dt, const Cons
         w[2] = (h1 * fmad(u1y, e2, c1 * u2y)) * det;
         w[5] = (h2 * fmad(u2y, e1, c2 * u1y)) * det;
     }
+    // bottom friction: h u / (1 + c1) with u = vfac(h) q; above eps_h,
+    // vfac(h) = 1/h and h u is q itself
+    // 1 / (1 + c1) with c1 = X / Y is Y / (Y + X): one division
     if ((h1 > 0.0) && (h2 < eps)) {
-        u1x = f1 * w[1]; u1y = f1 * w[2];
-        const double c1 = ((dt * c.g_mf02) * u1) / (pow43(h1) + kEps);
-        const double inv = 1.0 / (1.0 + c1);
-        w[1] = (h1 * u1x) * inv;
-        w[2] = (h1 * u1y) * inv;
+        const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1;
+        const double inv = Y / (Y + X);
+        if (h1 > eps) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
+        else { w[1] = (h1 * (f1 * w[1])) * inv; w[2] = (h1 * (f1 * w[2])) * inv; }
     }
     if ((h2 > 0.0) && (h1 < eps)) {
-        u2x = f2 * w[4]; u2y = f2 * w[5];
-        const double c1 = ((dt * c.g_mfs2) * u2) / (pow43(h2) + kEps);
-        const double inv = 1.0 / (1.0 + c1);
-        w[4] = (h2 * u2x) * inv;
-        w[5] = (h2 * u2y) * inv;
+        const double Y = pow43(h2) + kEps, X = (dt * c.g_mfs2) * u2;
+        const double inv = Y / (Y + X);
+        if (h2 > eps) { w[4] = w[4] * inv; w[5] = w[5] * inv; }
+        else { w[4] = (h2 * (f2 * w[4])) * inv; w[5] = (h2 * (f2 * w[5])) * inv; }
     }
 }
 
@@ -498,14 +509,19 @@ inline void coulomb(double w[6], double dt, const Consts& c) {
 // obtenerEstadoYDeltaTVolumenesGPU (Volumen_kernel.cu:231-284) for one cell:
 // per-cell dt from the wave accumulator, forward Euler stage, the spherical
 // metric source (new), then filtroEstado -> disImplicita -> coulomb.
-inline void volume_update(const double wo[6], const double acc[7], double w[6], double& dti, double area,
+// `rate` gets acc_w / area (0 below EPSILON): the step's dt is
+// 2 CFL / max(rate), i.e. min over cells of 2 CFL area / acc_w
+// (Volumen_kernel.cu:256) with one division per step.
+inline void volume_update(const double wo[6], const double acc[7], double w[6], double& rate, double area,
                           double inv_area, double tanR, double dt, const Consts& c) {
-    dti = (acc[6] < kEps) ? kBig : ((2.0 * c.cfl) * area) / acc[6];
+    (void)area;
+    rate = (acc[6] < kEps) ? 0.0 : acc[6] * inv_area;
     const double b = dt * inv_area;
     for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
     if (tanR != 0.0) {
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
+            if (wo[k] == 0.0 && wo[k + 1] == 0.0 && wo[k + 2] == 0.0) continue;  // adds exactly 0
             const double ux = vfac(wo[k], c.eps_h) * wo[k + 1];
             const double s = dt * (ux * tanR);
             w[k + 1] = fmad(s, wo[k + 2], w[k + 1]);
@@ -737,21 +753,24 @@ struct Solver {
         pass(W, 1, 1, dt);
         if (p.order == 2) volume_integral(W);
         const int NX = nx, NY = ny;
-        double mn = kBig;
-#pragma omp parallel for schedule(static) reduction(min : mn)
+        double mx = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : mx)
         for (int j = 0; j < NY; ++j) {
             for (int i = 0; i < NX; ++i) {
                 const size_t id = size_t(j) * NX + i;
-                double wo[6], a[7], w[6], d;
+                double wo[6], a[7], w[6], rate;
                 for (int k = 0; k < 6; ++k) wo[k] = W[k][id];
                 for (int k = 0; k < 7; ++k) a[k] = acc[k][id];
-                volume_update(wo, a, w, d, g.area[j], g.inv_area[j], g.tanR[j], dt, c);
+                volume_update(wo, a, w, rate, g.area[j], g.inv_area[j], g.tanR[j], dt, c);
                 for (int k = 0; k < 6; ++k) Wn[k][id] = w[k];
-                if (d < mn) mn = d;
+                if (rate > mx) mx = rate;
             }
         }
-        return mn;
+        return dt_of(mx);
     }
+
+    // dt from the largest acc_w / area; 1e30 when no cell has a wave speed
+    double dt_of(double max_rate) const { return (max_rate > 0.0) ? (2.0 * c.cfl) / max_rate : kBig; }
 
     double initial_dt(const double* const* W) {
         std::vector<double>& aw = acc[6];
@@ -776,14 +795,14 @@ struct Solver {
                 }
             }
         }
-        double mn = kBig;
+        double mx = 0.0;
         for (int j = 0; j < NY; ++j)
             for (int i = 0; i < NX; ++i) {
                 const double a = aw[size_t(j) * NX + i];
-                const double d = (a < kEps) ? kBig : ((2.0 * c.cfl) * g.area[j]) / a;  // Volumen_kernel.cu:226
-                if (d < mn) mn = d;
+                const double rate = (a < kEps) ? 0.0 : a * g.inv_area[j];  // Volumen_kernel.cu:226
+                if (rate > mx) mx = rate;
             }
-        return mn;
+        return dt_of(mx);
     }
 };
 
