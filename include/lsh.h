@@ -189,6 +189,35 @@ int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], in
 int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels);
 int lsh_probe_fp64_peak(int device, double* gflops);
 
+/* ---------------------------------------------------------------------------
+ * Batched ensemble (no counterpart in the reference): n scenarios with their
+ * own parameters and uneven grids (all of one `order`) advanced together.
+ * Each pass of a step is one persistent launch whose CTAs pull (scenario,
+ * tile) work items from a device counter; a run of steps is a CUDA graph.
+ * Every scenario stays bit-identical to its single-grid run (lsh_create...). */
+typedef struct lsh_batch lsh_batch;
+typedef struct lsh_tune {
+    int32_t edge_tile;          /* edges per work item, in units of 128        */
+    int32_t edge_ctas_per_sm;   /* persistent CTAs per SM for the edge passes  */
+    int32_t cell_tile;          /* cells per work item, in units of 256        */
+    int32_t cell_ctas_per_sm;   /* persistent CTAs per SM for the cell passes  */
+    double ms_per_step;         /* measured by lsh_batch_autotune              */
+} lsh_tune;
+int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** out);
+int lsh_batch_destroy(lsh_batch* b);
+/* upload scenario `s` from host arrays and run its initial-dt pass */
+int lsh_batch_set_state(lsh_batch* b, int s, const double* const host_state[LSH_NVARS], double* dt0_out);
+int lsh_batch_step(lsh_batch* b, int nsteps);              /* asynchronous */
+int lsh_batch_synchronize(lsh_batch* b);
+int lsh_batch_get_state(lsh_batch* b, int s, double* const host_state[LSH_NVARS]);
+int lsh_batch_get_time(lsh_batch* b, int s, double* t, double* dt_next, long long* steps);
+/* autotuner: time the candidate tile lengths and CTA counts on live steps and
+ * keep the fastest (the trial steps advance the simulation) */
+int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best);
+int lsh_batch_set_tune(lsh_batch* b, const lsh_tune* tune);
+int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune);
+int lsh_batch_get_launch_count(lsh_batch* b, long long* launches);
+
 /* Human-readable text for a status code. */
 const char* lsh_status_string(int status);
 

@@ -31,7 +31,9 @@
 #include <vector>
 
 #include "../../include/lsh.h"
+#include "lsh_passes.cuh"
 #include "lsh_scheme.cuh"
+#include "lsh_setup.h"
 
 using lsh::Consts;
 using lsh::EdgeIn;
@@ -40,184 +42,16 @@ using lsh::TimeRec;
 
 namespace {
 
-constexpr double kPi = 3.14159265358979323846;
-constexpr unsigned long long kRateInitBits = 0ULL;  // +0.0
-constexpr int kEdgeBlock = 128;
-constexpr int kCellBlock = 256;
+using lsh::kCellBlock;
+using lsh::kEdgeBlock;
+using lsh::kRateInitBits;
+using lsh::KArgs;
+using lsh::dt_of;
+using lsh::do_edge;
+using lsh::face_rest;
 constexpr int kGraphChunk = 16;
 
 thread_local std::string g_last_error;
-
-struct KArgs {
-    Consts c;
-    Geo geo;
-    const double* W[7];   // input state (face values are W + slopes at order 2)
-    double* Wout[6];      // output state of the volume kernel
-    const double* Xavg[6];  // order 2, stage 2: the step's initial state for the average
-    double* acc[7];
-    const double* sx[7];
-    const double* sy[7];
-    double* sxw[7];       // reconstruction kernel outputs
-    double* syw[7];
-    double* eta_max;
-    double* eta_time;
-    TimeRec* tm;
-};
-
-// ------------------------------------------------------------------ kernels
-
-// Depths of a face (first order: the cell's; second order: reconstructed).
-template <int ORDER>
-__device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, double& h1, double& h2) {
-    h1 = a.W[0][id];
-    h2 = a.W[3][id];
-    if (ORDER == 2) {
-        const double* const* s = (side < 2) ? a.sx : a.sy;
-        const double d1 = s[0][id] - s[3][id], d2 = s[3][id] + s[6][id];
-        // side & 1: the +slope face (E or N); the sign is a negation, not a multiply
-        h1 = h1 + ((side & 1) ? d1 : -d1);
-        h2 = h2 + ((side & 1) ? d2 : -d2);
-    }
-}
-
-// The rest of a face in the edge frame.  DIR 1 (vertical edge, normal
-// (sg, 0)): qn = sg qx, qt = sg qy; DIR 0 (horizontal, normal (0, sg)):
-// qn = sg qy, qt = -sg qx (Arista_kernel.cu:363-371, 509-525) -- selections
-// and negations, no FP64 arithmetic.
-template <int DIR, int ORDER>
-__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Face& f) {
-    double qx1 = a.W[1][id], qy1 = a.W[2][id], qx2 = a.W[4][id], qy2 = a.W[5][id], H = a.W[6][id];
-    if (ORDER == 2) {
-        const double* const* s = (side < 2) ? a.sx : a.sy;
-        const bool pos = (side & 1);
-        const double s1 = s[1][id], s2 = s[2][id], s4 = s[4][id], s5 = s[5][id], sH = s[6][id];
-        qx1 = qx1 + (pos ? s1 : -s1);
-        qy1 = qy1 + (pos ? s2 : -s2);
-        qx2 = qx2 + (pos ? s4 : -s4);
-        qy2 = qy2 + (pos ? s5 : -s5);
-        H = H + (pos ? sH : -sH);
-    }
-    if (DIR == 1) {
-        f.qn1 = pos_normal ? qx1 : -qx1; f.qt1 = pos_normal ? qy1 : -qy1;
-        f.qn2 = pos_normal ? qx2 : -qx2; f.qt2 = pos_normal ? qy2 : -qy2;
-    } else {
-        f.qn1 = pos_normal ? qy1 : -qy1; f.qt1 = pos_normal ? -qx1 : qx1;
-        f.qn2 = pos_normal ? qy2 : -qy2; f.qt2 = pos_normal ? -qx2 : qx2;
-    }
-    f.H = H;
-}
-
-// One edge: gather both sides, evaluate, scatter to the accumulators.
-// dir 0: horizontal edge row y between rows y-1 and y, column x.
-// dir 1: vertical edge column x between columns x-1 and x, row y.
-template <int DIR, bool FIRST, int ORDER>
-__device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt) {
-    const int nx = a.c.nx, ny = a.c.ny;
-    lsh::EdgeIn e;
-    int id0, id1 = -1, side0, row0, row1 = 0;
-    double bor = 0.0;
-    bool pos_normal = true;
-    if (DIR == 0) {
-        e.len = a.geo.len_h[y];
-        if (y == 0) { id0 = x; row0 = 0; pos_normal = false; bor = a.c.borde_sup; side0 = 2; }
-        else if (y == ny) { id0 = (ny - 1) * nx + x; row0 = ny - 1; bor = a.c.borde_inf; side0 = 3; }
-        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; row0 = y - 1; row1 = y; side0 = 3; }
-    } else {
-        e.len = a.geo.len_v[y];
-        row0 = row1 = y;
-        if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; side0 = 0; }
-        else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; side0 = 1; }
-        else { id0 = y * nx + x - 1; id1 = id0 + 1; side0 = 1; }
-    }
-    e.interior = (id1 >= 0);
-    const int side1 = (DIR == 0) ? 2 : 0;
-    face_depths<ORDER>(a, id0, side0, e.A.h1, e.A.h2);
-    if (e.interior) face_depths<ORDER>(a, id1, side1, e.B.h1, e.B.h2);
-    else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
-    // dry edge (Arista_kernel.cu:397): nothing to add; the first pass still
-    // writes the zeros that initialise the accumulators
-    if (!((0.5 * (e.A.h1 + e.B.h1) >= lsh::kEps) || (0.5 * (e.A.h2 + e.B.h2) >= lsh::kEps))) {
-        if (FIRST) {
-#pragma unroll
-            for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
-            if (e.interior) {
-#pragma unroll
-                for (int k = 0; k < 7; ++k) a.acc[k][id1] = 0.0;
-            }
-        }
-        return;
-    }
-    face_rest<DIR, ORDER>(a, id0, side0, pos_normal, e.A);
-    e.area0 = a.geo.area[row0];
-    e.inv_area0 = a.geo.inv_area[row0];
-    e.hc0[0] = a.W[0][id0];
-    e.hc0[1] = a.W[3][id0];
-    if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
-    else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
-    if (e.interior) {
-        face_rest<DIR, ORDER>(a, id1, side1, pos_normal, e.B);
-        e.area1 = a.geo.area[row1];
-        e.inv_area1 = a.geo.inv_area[row1];
-        e.hc1[0] = a.W[0][id1];
-        e.hc1[1] = a.W[3][id1];
-        if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
-        else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
-    } else {
-        // ghost: the cell's face with the normal discharges times the boundary factor
-        e.B = e.A;
-        e.B.qn1 = e.A.qn1 * bor;
-        e.B.qn2 = e.A.qn2 * bor;
-        e.area1 = e.area0;
-        e.inv_area1 = e.inv_area0;
-        e.hc1[0] = e.hc1[1] = 0.0;
-        e.acc1h[0] = e.acc1h[1] = 0.0;
-    }
-    lsh::EdgeOut o;
-    using lsh::is_zero;
-    if (is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2))
-        lsh::edge_flux<false>(e, dt, a.c, o);
-    else
-        lsh::edge_flux<true>(e, dt, a.c, o);
-    // back to x/y: DIR 1: (qx, qy) = sg (fn, ft); DIR 0: qx = -sg ft, qy = sg fn
-    double d0[6], d1[6];
-#pragma unroll
-    for (int l = 0; l < 2; ++l) {
-        const int k = 3 * l;
-        d0[k] = o.m[k];
-        d1[k] = o.p[k];
-        if (DIR == 1) {
-            d0[k + 1] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
-            d0[k + 2] = pos_normal ? o.m[k + 2] : -o.m[k + 2];
-            d1[k + 1] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
-            d1[k + 2] = pos_normal ? o.p[k + 2] : -o.p[k + 2];
-        } else {
-            d0[k + 1] = pos_normal ? -o.m[k + 2] : o.m[k + 2];
-            d0[k + 2] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
-            d1[k + 1] = pos_normal ? -o.p[k + 2] : o.p[k + 2];
-            d1[k + 2] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
-        }
-    }
-    if (FIRST) {
-        // every cell meets exactly one hor-even edge: write, do not accumulate
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a.acc[k][id0] = 0.0 - d0[k];
-        a.acc[6][id0] = 0.0 + o.wave;
-        if (e.interior) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.acc[k][id1] = 0.0 - d1[k];
-            a.acc[6][id1] = 0.0 + o.wave;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a.acc[k][id0] -= d0[k];
-        a.acc[6][id0] += o.wave;
-        if (e.interior) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.acc[k][id1] -= d1[k];
-            a.acc[6][id1] += o.wave;
-        }
-    }
-}
 
 // Horizontal edges of parity `par`: x along threads, edge rows along blocks.
 template <bool FIRST, int ORDER>
@@ -243,83 +77,13 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
     for (int y = blockIdx.y; y < ny; y += gridDim.y) do_edge<1, false, ORDER>(a, x, y, dt);
 }
 
-__device__ __forceinline__ double minmod(double a, double b) {
-    if (a > 0.0 && b > 0.0) return (a < b) ? a : b;
-    if (a < 0.0 && b < 0.0) return (a > b) ? a : b;
-    return 0.0;
-}
-
-__device__ __forceinline__ double recon_var(const KArgs& a, int id, int k) {
-    if (k == 0) return (a.W[0][id] + a.W[3][id]) - a.W[6][id];
-    if (k == 3) return a.W[3][id] - a.W[6][id];
-    return a.W[k][id];
-}
-
 // Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
 // with a first-order fallback where a reconstructed depth would be negative.
 __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
     if (a.tm->done) return;
-    const int nx = a.c.nx, ny = a.c.ny;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= nx * ny) return;
-    const int j = id / nx, i = id - j * nx;
-    // A cell whose own and 4 neighbours' depths are all zero only meets dry
-    // edges (a dry cell's faces always have zero depth: any nonzero depth
-    // slope would make one face negative and trigger the fallback), so its
-    // slopes are never read: store zeros and skip the FP64 work.
-    {
-        using lsh::is_zero;
-        bool dry = is_zero(a.W[0][id]) && is_zero(a.W[3][id]);
-        if (dry && i > 0) dry = is_zero(a.W[0][id - 1]) && is_zero(a.W[3][id - 1]);
-        if (dry && i < nx - 1) dry = is_zero(a.W[0][id + 1]) && is_zero(a.W[3][id + 1]);
-        if (dry && j > 0) dry = is_zero(a.W[0][id - nx]) && is_zero(a.W[3][id - nx]);
-        if (dry && j < ny - 1) dry = is_zero(a.W[0][id + nx]) && is_zero(a.W[3][id + nx]);
-        if (dry) {
-#pragma unroll
-            for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
-            return;
-        }
-    }
-    double sx[7], sy[7];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-        const double pc = recon_var(a, id, k);
-        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - recon_var(a, id - 1, k), recon_var(a, id + 1, k) - pc) : 0.0;
-        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - recon_var(a, id - nx, k), recon_var(a, id + nx, k) - pc) : 0.0;
-    }
-    const double h1 = a.W[0][id], h2 = a.W[3][id];
-    const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
-    const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
-    const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
-                     (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-        a.sxw[k][id] = bad ? 0.0 : sx[k];
-        a.syw[k][id] = bad ? 0.0 : sy[k];
-    }
-}
-
-// Block max of the per-cell rates (non-negative doubles order like their bit
-// patterns), then one 64-bit atomicMax per block.
-__device__ __forceinline__ void block_max_bits(unsigned long long v, TimeRec* tm) {
-    __shared__ unsigned long long red[kCellBlock / 32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
-        v = (w > v) ? w : v;
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kRateInitBits;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
-            v = (w > v) ? w : v;
-        }
-        if (lane == 0) atomicMax(&tm->rmax_bits, v);
-    }
+    if (id >= a.c.nx * a.c.ny) return;
+    lsh::recon_cell(a, id);
 }
 
 // MODE 0: order 1, in place; per-cell dt min.  MODE 1: order 2 stage 1
@@ -327,66 +91,13 @@ __device__ __forceinline__ void block_max_bits(unsigned long long v, TimeRec* tm
 template <int MODE>
 __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
     if (a.tm->done) return;
-    const int nx = a.c.nx, ny = a.c.ny;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     const double dt = a.tm->dt;
     unsigned long long bits = kRateInitBits;
-    if (id < nx * ny) {
-        const int j = id / nx;
-        double wo[6], acc[7], w[6], rate;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
-#pragma unroll
-        for (int k = 0; k < 7; ++k) acc[k] = a.acc[k][id];
-        if (MODE != 2 && a.c.track_eta) {
-            // actualizarEta1MaximaGPU (Volumen_kernel.cu:182-213): state before the step
-            const double v = wo[0] - a.W[6][id];
-            if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
-        }
-        // a dry, still cell with nothing flowing in maps to itself through the
-        // whole update (dt contribution 1e30; its second-order pressure
-        // integral is g*0*... = 0): skip the FP64 work
-        bool still = true;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) still &= lsh::is_zero(wo[k]);
-#pragma unroll
-        for (int k = 0; k < 7; ++k) still &= lsh::is_zero(acc[k]);
-        if (still) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) w[k] = wo[k];
-            rate = 0.0;
-        } else {
-            if (a.c.order == 2) {
-                // cell-midpoint integral of g h d(eta) over the reconstructed cell
-                const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
-                const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
-                const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
-                const double wx = a.geo.wx[j], wy = a.geo.wy[j];
-                acc[1] -= a.c.peso * ((gh1 * e1x) * wx);
-                acc[4] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2x, a.c.r * e1x)) * wx);
-                acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
-                acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
-            }
-            lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
-        }
-        if (MODE == 2) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) w[k] = 0.5 * (a.Xavg[k][id] + w[k]);
-        }
-        bool bad = false;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
-        if (bad) atomicOr(&a.tm->err, 1 << LSH_ERR_NUMERIC);
-        bits = (unsigned long long)__double_as_longlong(rate);
-    }
-    if (MODE != 2) block_max_bits(bits, a.tm);
+    if (id < a.c.nx * a.c.ny) bits = lsh::volume_cell<MODE>(a, id, dt);
+    if (MODE != 2) lsh::block_max_bits<kCellBlock>(bits, &a.tm->rmax_bits);
 }
 
-// dt from the largest acc_w / area: 2 CFL / max rate, 1e30 when no cell has a wave speed
-__device__ __forceinline__ double dt_of(unsigned long long rmax_bits, double two_cfl) {
-    const double m = __longlong_as_double((long long)rmax_bits);
-    return (m > 0.0) ? two_cfl / m : lsh::kBig;
-}
 
 // Advance the device clock: t += dt, dt = min per-cell dt (ShallowWater.cu:436-442).
 __global__ void k_advance(TimeRec* tm, double two_cfl) {
@@ -410,59 +121,17 @@ __global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
     const int nalong = (DIR == 0) ? nx : ny;
     // DIR 0: threads along x, lines along blocks.y; DIR 1: threads along edge columns
     for (int bl = blockIdx.y; bl < ((DIR == 0) ? nlines : nalong); bl += gridDim.y) {
-        int x, y;
-        if (DIR == 0) { x = tid; y = par + 2 * bl; if (x >= nx) return; }
-        else { x = par + 2 * tid; y = bl; if (tid >= nlines) return; }
-        int id0, id1 = -1;
-        double bor = 0.0, len;
-        bool pos_normal = true;
-        if (DIR == 0) {
-            len = a.geo.len_h[y];
-            if (y == 0) { id0 = x; pos_normal = false; bor = a.c.borde_sup; }
-            else if (y == ny) { id0 = (ny - 1) * nx + x; bor = a.c.borde_inf; }
-            else { id0 = (y - 1) * nx + x; id1 = id0 + nx; }
-        } else {
-            len = a.geo.len_v[y];
-            if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; }
-            else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; }
-            else { id0 = y * nx + x - 1; id1 = id0 + 1; }
-        }
-        lsh::Face A, B;
-        A.h1 = a.W[0][id0];
-        A.h2 = a.W[3][id0];
-        face_rest<DIR, 1>(a, id0, 0, pos_normal, A);
-        if (id1 >= 0) {
-            B.h1 = a.W[0][id1];
-            B.h2 = a.W[3][id1];
-            face_rest<DIR, 1>(a, id1, 0, pos_normal, B);
-        } else {
-            B = A;
-            B.qn1 = A.qn1 * bor;
-            B.qn2 = A.qn2 * bor;
-        }
-        const double wv = lsh::edge_initial_wave(A, B, len, a.c);
-        if (FIRST) {
-            a.acc[6][id0] = 0.0 + wv;
-            if (id1 >= 0) a.acc[6][id1] = 0.0 + wv;
-        } else {
-            a.acc[6][id0] += wv;
-            if (id1 >= 0) a.acc[6][id1] += wv;
-        }
+        if (DIR == 0) { if (tid >= nx) return; lsh::init_wave_edge<0, FIRST>(a, tid, par + 2 * bl); }
+        else { if (tid >= nlines) return; lsh::init_wave_edge<1, FIRST>(a, par + 2 * tid, bl); }
     }
 }
 
-// Per-cell dt of the initial wave pass (obtenerDeltaTVolumenesGPU) and its min.
+// Per-cell rate of the initial wave pass (obtenerDeltaTVolumenesGPU) and its max.
 __global__ void __launch_bounds__(kCellBlock) k_cell_dt(KArgs a) {
-    const int nx = a.c.nx, ny = a.c.ny;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long bits = kRateInitBits;
-    if (id < nx * ny) {
-        const int j = id / nx;
-        const double w = a.acc[6][id];
-        const double rate = (w < lsh::kEps) ? 0.0 : w * a.geo.inv_area[j];
-        bits = (unsigned long long)__double_as_longlong(rate);
-    }
-    block_max_bits(bits, a.tm);
+    if (id < a.c.nx * a.c.ny) bits = lsh::init_cell_rate(a, id);
+    lsh::block_max_bits<kCellBlock>(bits, &a.tm->rmax_bits);
 }
 
 __global__ void k_init_finish(TimeRec* tm, double two_cfl) {
@@ -541,79 +210,11 @@ int fail_cuda(cudaError_t e, const char* what) {
     } while (0)
 
 int check_params(const lsh_params* p) {
-    if (!p) return LSH_ERR_INVALID;
-    if (p->nx < 1 || p->ny < 1) { g_last_error = "nx and ny must be >= 1"; return LSH_ERR_INVALID; }
-    if ((long long)p->nx * p->ny >= (1LL << 31) - 1024) { g_last_error = "grid too large for 32-bit indexing"; return LSH_ERR_INVALID; }
-    if (p->order != 1 && p->order != 2) { g_last_error = "order must be 1 or 2"; return LSH_ERR_INVALID; }
-    if (p->coords != LSH_COORDS_CARTESIAN && p->coords != LSH_COORDS_SPHERICAL) { g_last_error = "bad coords"; return LSH_ERR_INVALID; }
-    if (p->friction_law != LSH_FRICTION_COULOMB && p->friction_law != LSH_FRICTION_POULIQUEN) { g_last_error = "bad friction law"; return LSH_ERR_INVALID; }
-    if (p->eig_sort != 0 && p->eig_sort != 1) { g_last_error = "eig_sort must be 0 or 1"; return LSH_ERR_INVALID; }
-    if (!(p->eps_h > 0) || !(p->gravity > 0) || !(p->r >= 0 && p->r < 1) || !(p->peso > 0) || !(p->cfl > 0) || !(p->H > 0) || !(p->L > 0)) {
-        g_last_error = "eps_h, gravity, peso, cfl, L, H must be > 0 and 0 <= r < 1";
-        return LSH_ERR_INVALID;
-    }
-    if (p->coords == LSH_COORDS_CARTESIAN && !(p->dx > 0 && p->dy > 0)) { g_last_error = "dx, dy must be > 0"; return LSH_ERR_INVALID; }
-    if (p->coords == LSH_COORDS_SPHERICAL &&
-        !(p->dlon > 0 && p->dlat > 0 && p->radius > 0 && std::fabs(p->lat0) < 90 && std::fabs(p->lat0 + p->ny * p->dlat) < 90)) {
-        g_last_error = "spherical grid needs dlon, dlat, radius > 0 and latitudes inside (-90, 90)";
+    if (const char* why = lsh::params_problem(p)) {
+        g_last_error = why;
         return LSH_ERR_INVALID;
     }
     return LSH_OK;
-}
-
-Consts make_consts(const lsh_params& p) {
-    Consts c{};
-    c.g = p.gravity; c.r = p.r; c.gp = p.gravity * (1.0 - p.r);
-    c.eps_h = p.eps_h; c.peso = p.peso; c.beta = p.beta; c.cfl = p.cfl;
-    c.mu = std::fabs(std::tan(p.angle1)) * (p.L / p.H);  // defTerminoFriccion, Coulomb
-    c.mfc = p.mfc; c.mf0 = p.mf0; c.mfs = p.mfs; c.vmax1 = p.vmax1; c.vmax2 = p.vmax2;
-    c.L = p.L; c.H = p.H;
-    c.tan1 = std::tan(p.angle1); c.tan2 = std::tan(p.angle2); c.tan3 = std::tan(p.angle3); c.tan4 = std::tan(p.angle4);
-    c.borde_sup = p.borde_sup; c.borde_inf = p.borde_inf; c.borde_izq = p.borde_izq; c.borde_der = p.borde_der;
-    c.omr = 1.0 - p.r;
-    c.inv_gp = 1.0 / c.gp;
-    c.inv_eps = 1.0 / p.eps_h;
-    c.inv_peso = 1.0 / p.peso;
-    c.eps_1r = p.eps_h * (1.0 + p.r);
-    c.g_mf02 = (p.gravity * p.mf0) * p.mf0;
-    c.g_mfs2 = (p.gravity * p.mfs) * p.mfs;
-    c.sqrt_g = std::sqrt(p.gravity);
-    c.law = p.friction_law; c.order = p.order; c.nx = p.nx; c.ny = p.ny; c.track_eta = p.track_eta_max;
-    c.eig_sort = p.eig_sort;
-    return c;
-}
-
-// Per-row geometry on the host (same formulas as the CPU oracle).
-void make_geo(const lsh_params& p, std::vector<double>& area, std::vector<double>& len_v, std::vector<double>& len_h,
-              std::vector<double>& tanR, std::vector<double>& wx, std::vector<double>& wy,
-              std::vector<double>& inv_area) {
-    const int ny = p.ny;
-    area.resize(ny); len_v.resize(ny); len_h.resize(ny + 1); tanR.resize(ny); wx.resize(ny); wy.resize(ny);
-    if (p.coords == LSH_COORDS_SPHERICAL) {
-        const double d2r = kPi / 180.0;
-        const double R = p.radius, dl = p.dlon * d2r, dp = p.dlat * d2r;
-        for (int y = 0; y <= ny; ++y) len_h[y] = R * std::cos((p.lat0 + y * p.dlat) * d2r) * dl;
-        for (int j = 0; j < ny; ++j) {
-            const double ps = (p.lat0 + j * p.dlat) * d2r, pn = (p.lat0 + (j + 1) * p.dlat) * d2r;
-            const double pc = (p.lat0 + (j + 0.5) * p.dlat) * d2r;
-            area[j] = R * R * dl * (std::sin(pn) - std::sin(ps));
-            len_v[j] = R * dp;
-            tanR[j] = std::tan(pc) / R;
-            wx[j] = area[j] / (R * std::cos(pc) * dl);
-            wy[j] = area[j] / (R * dp);
-        }
-    } else {
-        for (int y = 0; y <= ny; ++y) len_h[y] = p.dx;
-        for (int j = 0; j < ny; ++j) {
-            area[j] = p.dx * p.dy;  // Problema.cxx:296
-            len_v[j] = p.dy;
-            tanR[j] = 0.0;
-            wx[j] = p.dy;
-            wy[j] = p.dx;
-        }
-    }
-    inv_area.resize(ny);
-    for (int j = 0; j < ny; ++j) inv_area[j] = 1.0 / area[j];
 }
 
 KArgs base_args(const lsh_ctx* ctx) {
@@ -806,7 +407,7 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     lsh_ctx* ctx = new (std::nothrow) lsh_ctx();
     if (!ctx) return LSH_ERR_HOST_OOM;
     ctx->p = *p;
-    ctx->c = make_consts(*p);
+    ctx->c = lsh::make_consts(*p);
     ctx->N = size_t(p->nx) * p->ny;
     auto bail = [&](int s) { lsh_destroy(ctx); return s; };
     if (device >= 0) {
@@ -845,17 +446,9 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     cur += (geo_n + 31) & ~size_t(31);
     ctx->tm = reinterpret_cast<TimeRec*>(cur);
 
-    std::vector<double> area, len_v, len_h, tanR, wx, wy, inv_area;
-    make_geo(*p, area, len_v, len_h, tanR, wx, wy, inv_area);
-    std::vector<double> g(geo_n, 0.0);
     const size_t st = size_t(p->ny + 1);
-    std::copy(area.begin(), area.end(), g.begin());
-    std::copy(len_v.begin(), len_v.end(), g.begin() + st);
-    std::copy(len_h.begin(), len_h.end(), g.begin() + 2 * st);
-    std::copy(tanR.begin(), tanR.end(), g.begin() + 3 * st);
-    std::copy(wx.begin(), wx.end(), g.begin() + 4 * st);
-    std::copy(wy.begin(), wy.end(), g.begin() + 5 * st);
-    std::copy(inv_area.begin(), inv_area.end(), g.begin() + 6 * st);
+    std::vector<double> g(geo_n, 0.0);
+    lsh::fill_geo(*p, g.data(), st);
     {
         cudaError_t e = cudaMemcpy(ctx->geo_buf, g.data(), geo_n * sizeof(double), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy geometry"));
@@ -1114,42 +707,6 @@ __global__ void k_noalloc_take_dt(TimeRec* tm, double two_cfl) {
     tm->rmax_bits = kRateInitBits;
 }
 
-// Same per-row formulas as make_geo, written into a caller-provided array.
-void noalloc_fill_geo(const lsh_params& p, double* g) {
-    double* area = g;
-    double* len_v = g + kNaGeoStride;
-    double* len_h = g + 2 * kNaGeoStride;
-    double* tanR = g + 3 * kNaGeoStride;
-    double* wx = g + 4 * kNaGeoStride;
-    double* wy = g + 5 * kNaGeoStride;
-    double* inv_area = g + 6 * kNaGeoStride;
-    const int ny = p.ny;
-    if (p.coords == LSH_COORDS_SPHERICAL) {
-        const double d2r = kPi / 180.0;
-        const double R = p.radius, dl = p.dlon * d2r, dp = p.dlat * d2r;
-        for (int y = 0; y <= ny; ++y) len_h[y] = R * std::cos((p.lat0 + y * p.dlat) * d2r) * dl;
-        for (int j = 0; j < ny; ++j) {
-            const double ps = (p.lat0 + j * p.dlat) * d2r, pn = (p.lat0 + (j + 1) * p.dlat) * d2r;
-            const double pc = (p.lat0 + (j + 0.5) * p.dlat) * d2r;
-            area[j] = R * R * dl * (std::sin(pn) - std::sin(ps));
-            len_v[j] = R * dp;
-            tanR[j] = std::tan(pc) / R;
-            wx[j] = area[j] / (R * std::cos(pc) * dl);
-            wy[j] = area[j] / (R * dp);
-        }
-    } else {
-        for (int y = 0; y <= ny; ++y) len_h[y] = p.dx;
-        for (int j = 0; j < ny; ++j) {
-            area[j] = p.dx * p.dy;
-            len_v[j] = p.dy;
-            tanR[j] = 0.0;
-            wx[j] = p.dy;
-            wy[j] = p.dx;
-        }
-    }
-    for (int j = 0; j < ny; ++j) inv_area[j] = 1.0 / area[j];
-}
-
 }  // namespace
 
 extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], int nsteps,
@@ -1176,7 +733,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     }
     double* base = g_noalloc_base[dev];
 
-    noalloc_fill_geo(*p, g_noalloc_geo_host);
+    lsh::fill_geo(*p, g_noalloc_geo_host, kNaGeoStride);
     LSH_CUDA(cudaMemcpyAsync(base + kNaGeoOffset, g_noalloc_geo_host, 7 * kNaGeoStride * sizeof(double),
                              cudaMemcpyHostToDevice, s));
     TimeRec* tm = reinterpret_cast<TimeRec*>(base + kNaTimeOffset);
@@ -1190,7 +747,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
 
     KArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.c = make_consts(*p);
+    a.c = lsh::make_consts(*p);
     a.c.track_eta = 0;
     const double* g = base + kNaGeoOffset;
     a.geo.area = g;
@@ -1235,3 +792,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     *dt_io = out.dt;
     return err_bits_to_status(out.err);
 }
+
+namespace lsh {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace lsh

@@ -1,0 +1,374 @@
+// lsh_passes.cuh -- per-edge and per-cell device functions of the step,
+// shared by the single-grid kernels (lsh_core.cu) and the batched ensemble
+// kernels (lsh_batch.cu), so both evaluate exactly the same arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/lsh.h"
+#include "lsh_scheme.cuh"
+
+namespace lsh {
+
+constexpr unsigned long long kRateInitBits = 0ULL;  // +0.0
+constexpr int kEdgeBlock = 128;
+constexpr int kCellBlock = 256;
+
+struct KArgs {
+    Consts c;
+    Geo geo;
+    const double* W[7];   // input state (face values are W + slopes at order 2)
+    double* Wout[6];      // output state of the volume kernel
+    const double* Xavg[6];  // order 2, stage 2: the step's initial state for the average
+    double* acc[7];
+    const double* sx[7];
+    const double* sy[7];
+    double* sxw[7];       // reconstruction kernel outputs
+    double* syw[7];
+    double* eta_max;
+    double* eta_time;
+    TimeRec* tm;
+};
+
+// Depths of a face (first order: the cell's; second order: reconstructed).
+template <int ORDER>
+__device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, double& h1, double& h2) {
+    h1 = a.W[0][id];
+    h2 = a.W[3][id];
+    if (ORDER == 2) {
+        const double* const* s = (side < 2) ? a.sx : a.sy;
+        const double d1 = s[0][id] - s[3][id], d2 = s[3][id] + s[6][id];
+        // side & 1: the +slope face (E or N); the sign is a negation, not a multiply
+        h1 = h1 + ((side & 1) ? d1 : -d1);
+        h2 = h2 + ((side & 1) ? d2 : -d2);
+    }
+}
+
+// The rest of a face in the edge frame.  DIR 1 (vertical edge, normal
+// (sg, 0)): qn = sg qx, qt = sg qy; DIR 0 (horizontal, normal (0, sg)):
+// qn = sg qy, qt = -sg qx (Arista_kernel.cu:363-371, 509-525) -- selections
+// and negations, no FP64 arithmetic.
+template <int DIR, int ORDER>
+__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Face& f) {
+    double qx1 = a.W[1][id], qy1 = a.W[2][id], qx2 = a.W[4][id], qy2 = a.W[5][id], H = a.W[6][id];
+    if (ORDER == 2) {
+        const double* const* s = (side < 2) ? a.sx : a.sy;
+        const bool pos = (side & 1);
+        const double s1 = s[1][id], s2 = s[2][id], s4 = s[4][id], s5 = s[5][id], sH = s[6][id];
+        qx1 = qx1 + (pos ? s1 : -s1);
+        qy1 = qy1 + (pos ? s2 : -s2);
+        qx2 = qx2 + (pos ? s4 : -s4);
+        qy2 = qy2 + (pos ? s5 : -s5);
+        H = H + (pos ? sH : -sH);
+    }
+    if (DIR == 1) {
+        f.qn1 = pos_normal ? qx1 : -qx1; f.qt1 = pos_normal ? qy1 : -qy1;
+        f.qn2 = pos_normal ? qx2 : -qx2; f.qt2 = pos_normal ? qy2 : -qy2;
+    } else {
+        f.qn1 = pos_normal ? qy1 : -qy1; f.qt1 = pos_normal ? -qx1 : qx1;
+        f.qn2 = pos_normal ? qy2 : -qy2; f.qt2 = pos_normal ? -qx2 : qx2;
+    }
+    f.H = H;
+}
+
+// One edge: gather both sides, evaluate, scatter to the accumulators.
+// dir 0: horizontal edge row y between rows y-1 and y, column x.
+// dir 1: vertical edge column x between columns x-1 and x, row y.
+template <int DIR, bool FIRST, int ORDER>
+__device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    lsh::EdgeIn e;
+    int id0, id1 = -1, side0, row0, row1 = 0;
+    double bor = 0.0;
+    bool pos_normal = true;
+    if (DIR == 0) {
+        e.len = a.geo.len_h[y];
+        if (y == 0) { id0 = x; row0 = 0; pos_normal = false; bor = a.c.borde_sup; side0 = 2; }
+        else if (y == ny) { id0 = (ny - 1) * nx + x; row0 = ny - 1; bor = a.c.borde_inf; side0 = 3; }
+        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; row0 = y - 1; row1 = y; side0 = 3; }
+    } else {
+        e.len = a.geo.len_v[y];
+        row0 = row1 = y;
+        if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; side0 = 0; }
+        else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; side0 = 1; }
+        else { id0 = y * nx + x - 1; id1 = id0 + 1; side0 = 1; }
+    }
+    e.interior = (id1 >= 0);
+    const int side1 = (DIR == 0) ? 2 : 0;
+    face_depths<ORDER>(a, id0, side0, e.A.h1, e.A.h2);
+    if (e.interior) face_depths<ORDER>(a, id1, side1, e.B.h1, e.B.h2);
+    else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
+    // dry edge (Arista_kernel.cu:397): nothing to add; the first pass still
+    // writes the zeros that initialise the accumulators
+    if (!((0.5 * (e.A.h1 + e.B.h1) >= lsh::kEps) || (0.5 * (e.A.h2 + e.B.h2) >= lsh::kEps))) {
+        if (FIRST) {
+#pragma unroll
+            for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
+            if (e.interior) {
+#pragma unroll
+                for (int k = 0; k < 7; ++k) a.acc[k][id1] = 0.0;
+            }
+        }
+        return;
+    }
+    face_rest<DIR, ORDER>(a, id0, side0, pos_normal, e.A);
+    e.area0 = a.geo.area[row0];
+    e.inv_area0 = a.geo.inv_area[row0];
+    e.hc0[0] = a.W[0][id0];
+    e.hc0[1] = a.W[3][id0];
+    if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
+    else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
+    if (e.interior) {
+        face_rest<DIR, ORDER>(a, id1, side1, pos_normal, e.B);
+        e.area1 = a.geo.area[row1];
+        e.inv_area1 = a.geo.inv_area[row1];
+        e.hc1[0] = a.W[0][id1];
+        e.hc1[1] = a.W[3][id1];
+        if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
+        else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
+    } else {
+        // ghost: the cell's face with the normal discharges times the boundary factor
+        e.B = e.A;
+        e.B.qn1 = e.A.qn1 * bor;
+        e.B.qn2 = e.A.qn2 * bor;
+        e.area1 = e.area0;
+        e.inv_area1 = e.inv_area0;
+        e.hc1[0] = e.hc1[1] = 0.0;
+        e.acc1h[0] = e.acc1h[1] = 0.0;
+    }
+    lsh::EdgeOut o;
+    using lsh::is_zero;
+    if (is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2))
+        lsh::edge_flux<false>(e, dt, a.c, o);
+    else
+        lsh::edge_flux<true>(e, dt, a.c, o);
+    // back to x/y: DIR 1: (qx, qy) = sg (fn, ft); DIR 0: qx = -sg ft, qy = sg fn
+    double d0[6], d1[6];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const int k = 3 * l;
+        d0[k] = o.m[k];
+        d1[k] = o.p[k];
+        if (DIR == 1) {
+            d0[k + 1] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
+            d0[k + 2] = pos_normal ? o.m[k + 2] : -o.m[k + 2];
+            d1[k + 1] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
+            d1[k + 2] = pos_normal ? o.p[k + 2] : -o.p[k + 2];
+        } else {
+            d0[k + 1] = pos_normal ? -o.m[k + 2] : o.m[k + 2];
+            d0[k + 2] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
+            d1[k + 1] = pos_normal ? -o.p[k + 2] : o.p[k + 2];
+            d1[k + 2] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
+        }
+    }
+    if (FIRST) {
+        // every cell meets exactly one hor-even edge: write, do not accumulate
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] = 0.0 - d0[k];
+        a.acc[6][id0] = 0.0 + o.wave;
+        if (e.interior) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] = 0.0 - d1[k];
+            a.acc[6][id1] = 0.0 + o.wave;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] -= d0[k];
+        a.acc[6][id0] += o.wave;
+        if (e.interior) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] -= d1[k];
+            a.acc[6][id1] += o.wave;
+        }
+    }
+}
+
+__device__ __forceinline__ double minmod(double a, double b) {
+    if (a > 0.0 && b > 0.0) return (a < b) ? a : b;
+    if (a < 0.0 && b < 0.0) return (a > b) ? a : b;
+    return 0.0;
+}
+
+__device__ __forceinline__ double recon_var(const KArgs& a, int id, int k) {
+    if (k == 0) return (a.W[0][id] + a.W[3][id]) - a.W[6][id];
+    if (k == 3) return a.W[3][id] - a.W[6][id];
+    return a.W[k][id];
+}
+
+// One cell of the second-order reconstruction (k_recon).
+__device__ __forceinline__ void recon_cell(const KArgs& a, int id) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int j = id / nx, i = id - j * nx;
+    // A cell whose own and 4 neighbours' depths are all zero only meets dry
+    // edges (a dry cell's faces always have zero depth: any nonzero depth
+    // slope would make one face negative and trigger the fallback), so its
+    // slopes are never read: store zeros and skip the FP64 work.
+    {
+        using lsh::is_zero;
+        bool dry = is_zero(a.W[0][id]) && is_zero(a.W[3][id]);
+        if (dry && i > 0) dry = is_zero(a.W[0][id - 1]) && is_zero(a.W[3][id - 1]);
+        if (dry && i < nx - 1) dry = is_zero(a.W[0][id + 1]) && is_zero(a.W[3][id + 1]);
+        if (dry && j > 0) dry = is_zero(a.W[0][id - nx]) && is_zero(a.W[3][id - nx]);
+        if (dry && j < ny - 1) dry = is_zero(a.W[0][id + nx]) && is_zero(a.W[3][id + nx]);
+        if (dry) {
+#pragma unroll
+            for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
+            return;
+        }
+    }
+    double sx[7], sy[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const double pc = recon_var(a, id, k);
+        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - recon_var(a, id - 1, k), recon_var(a, id + 1, k) - pc) : 0.0;
+        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - recon_var(a, id - nx, k), recon_var(a, id + nx, k) - pc) : 0.0;
+    }
+    const double h1 = a.W[0][id], h2 = a.W[3][id];
+    const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
+    const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
+    const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
+                     (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        a.sxw[k][id] = bad ? 0.0 : sx[k];
+        a.syw[k][id] = bad ? 0.0 : sy[k];
+    }
+}
+
+// Block max of the per-cell rates (non-negative doubles order like their bit
+// patterns), then one 64-bit atomicMax per block.
+template <int BLOCK>
+__device__ __forceinline__ void block_max_bits(unsigned long long v, unsigned long long* target) {
+    __shared__ unsigned long long red[BLOCK / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kRateInitBits;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+            v = (w > v) ? w : v;
+        }
+        if (lane == 0) atomicMax(target, v);
+    }
+}
+
+// One cell of the Euler-stage update (k_volume); returns the bits of the
+// cell's acc_w / area for the dt reduction.
+// MODE 0: order 1, in place.  MODE 1: order 2 stage 1 (W -> Wout).
+// MODE 2: order 2 stage 2, Wout = (Xavg + E(W)) / 2.
+template <int MODE>
+__device__ __forceinline__ unsigned long long volume_cell(const KArgs& a, int id, double dt) {
+    const int nx = a.c.nx;
+    const int j = id / nx;
+    double wo[6], acc[7], w[6], rate;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) acc[k] = a.acc[k][id];
+    if (MODE != 2 && a.c.track_eta) {
+        // actualizarEta1MaximaGPU (Volumen_kernel.cu:182-213): state before the step
+        const double v = wo[0] - a.W[6][id];
+        if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
+    }
+    // a dry, still cell with nothing flowing in maps to itself through the
+    // whole update (dt contribution 1e30; its second-order pressure
+    // integral is g*0*... = 0): skip the FP64 work
+    bool still = true;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) still &= lsh::is_zero(wo[k]);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) still &= lsh::is_zero(acc[k]);
+    if (still) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = wo[k];
+        rate = 0.0;
+    } else {
+        if (a.c.order == 2) {
+            // cell-midpoint integral of g h d(eta) over the reconstructed cell
+            const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
+            const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
+            const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
+            const double wx = a.geo.wx[j], wy = a.geo.wy[j];
+            acc[1] -= a.c.peso * ((gh1 * e1x) * wx);
+            acc[4] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2x, a.c.r * e1x)) * wx);
+            acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
+            acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
+        }
+        lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
+    }
+    if (MODE == 2) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = 0.5 * (a.Xavg[k][id] + w[k]);
+    }
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
+    if (bad) atomicOr(&a.tm->err, 1 << LSH_ERR_NUMERIC);
+    return (unsigned long long)__double_as_longlong(rate);
+}
+
+// dt from the largest acc_w / area: 2 CFL / max rate, 1e30 when no cell has a wave speed
+__device__ __forceinline__ double dt_of(unsigned long long rmax_bits, double two_cfl) {
+    const double m = __longlong_as_double((long long)rmax_bits);
+    return (m > 0.0) ? two_cfl / m : lsh::kBig;
+}
+
+// One edge of the initial-dt pass (procesarAristasDeltaTInicialGPU,
+// Arista_kernel.cu:1129-1308): its wave-speed bound into acc[6].
+template <int DIR, bool FIRST>
+__device__ __forceinline__ void init_wave_edge(const KArgs& a, int x, int y) {
+    const int nx = a.c.nx, ny = a.c.ny;
+    int id0, id1 = -1;
+    double bor = 0.0, len;
+    bool pos_normal = true;
+    if (DIR == 0) {
+        len = a.geo.len_h[y];
+        if (y == 0) { id0 = x; pos_normal = false; bor = a.c.borde_sup; }
+        else if (y == ny) { id0 = (ny - 1) * nx + x; bor = a.c.borde_inf; }
+        else { id0 = (y - 1) * nx + x; id1 = id0 + nx; }
+    } else {
+        len = a.geo.len_v[y];
+        if (x == 0) { id0 = y * nx; pos_normal = false; bor = a.c.borde_izq; }
+        else if (x == nx) { id0 = y * nx + nx - 1; bor = a.c.borde_der; }
+        else { id0 = y * nx + x - 1; id1 = id0 + 1; }
+    }
+    lsh::Face A, B;
+    A.h1 = a.W[0][id0];
+    A.h2 = a.W[3][id0];
+    face_rest<DIR, 1>(a, id0, 0, pos_normal, A);
+    if (id1 >= 0) {
+        B.h1 = a.W[0][id1];
+        B.h2 = a.W[3][id1];
+        face_rest<DIR, 1>(a, id1, 0, pos_normal, B);
+    } else {
+        B = A;
+        B.qn1 = A.qn1 * bor;
+        B.qn2 = A.qn2 * bor;
+    }
+    const double wv = lsh::edge_initial_wave(A, B, len, a.c);
+    if (FIRST) {
+        a.acc[6][id0] = 0.0 + wv;
+        if (id1 >= 0) a.acc[6][id1] = 0.0 + wv;
+    } else {
+        a.acc[6][id0] += wv;
+        if (id1 >= 0) a.acc[6][id1] += wv;
+    }
+
+}
+
+// acc_w / area of one cell after the initial wave pass (obtenerDeltaTVolumenesGPU)
+__device__ __forceinline__ unsigned long long init_cell_rate(const KArgs& a, int id) {
+    const int j = id / a.c.nx;
+    const double w = a.acc[6][id];
+    const double rate = (w < lsh::kEps) ? 0.0 : w * a.geo.inv_area[j];
+    return (unsigned long long)__double_as_longlong(rate);
+}
+
+}  // namespace lsh

@@ -52,6 +52,17 @@ SIGNATURES = {
     "lsh_profile_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsh_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, DP]),
     "lsh_step_noalloc": (ctypes.c_int, [P, P, ctypes.c_int, DP, DP, P]),
+    "lsh_batch_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]),
+    "lsh_batch_destroy": (ctypes.c_int, [P]),
+    "lsh_batch_set_state": (ctypes.c_int, [P, ctypes.c_int, P, DP]),
+    "lsh_batch_step": (ctypes.c_int, [P, ctypes.c_int]),
+    "lsh_batch_synchronize": (ctypes.c_int, [P]),
+    "lsh_batch_get_state": (ctypes.c_int, [P, ctypes.c_int, P]),
+    "lsh_batch_get_time": (ctypes.c_int, [P, ctypes.c_int, DP, DP, ctypes.POINTER(ctypes.c_longlong)]),
+    "lsh_batch_autotune": (ctypes.c_int, [P, ctypes.c_int, P]),
+    "lsh_batch_set_tune": (ctypes.c_int, [P, P]),
+    "lsh_batch_get_tune": (ctypes.c_int, [P, P]),
+    "lsh_batch_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "lsh_last_error": (ctypes.c_char_p, []),
 }
@@ -194,4 +205,91 @@ class Solver:
         _check(self.lib.lsh_set_stream(self._ctx, ctypes.c_void_p(stream_ptr)), "lsh_set_stream")
 
 
-__all__ = ["Solver", "LshError", "load", "device_available", "SIGNATURES", "_abi"]
+class Tune(ctypes.Structure):
+    """Mirror of lsh_tune."""
+    _fields_ = [("edge_tile", ctypes.c_int32), ("edge_ctas_per_sm", ctypes.c_int32),
+                ("cell_tile", ctypes.c_int32), ("cell_ctas_per_sm", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Batch:
+    """A batched ensemble (wraps lsh_batch): scenarios with their own
+    parameters and grid sizes, advanced together."""
+
+    def __init__(self, params_list, device: int = 0):
+        self.lib = load()
+        self.params = [p.copy() for p in params_list]
+        arr = (LshParams * len(self.params))(*self.params)
+        self._b = ctypes.c_void_p()
+        _check(self.lib.lsh_batch_create(arr, len(self.params), int(device), ctypes.byref(self._b)),
+               "lsh_batch_create")
+
+    def close(self):
+        if self._b:
+            self.lib.lsh_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, s, state):
+        p = self.params[s]
+        arrs = [np.ascontiguousarray(state[v] if isinstance(state, dict) else state[i], dtype=np.float64)
+                for i, v in enumerate(VARS)]
+        for a in arrs:
+            if a.size != p.nx * p.ny:
+                raise ValueError("state array size does not match nx*ny")
+        dt = ctypes.c_double()
+        _check(self.lib.lsh_batch_set_state(self._b, int(s), _ptr_array([a.ctypes.data for a in arrs]),
+                                            ctypes.byref(dt)), "lsh_batch_set_state")
+        return dt.value
+
+    def step(self, n=1):
+        _check(self.lib.lsh_batch_step(self._b, int(n)), "lsh_batch_step")
+
+    def synchronize(self):
+        _check(self.lib.lsh_batch_synchronize(self._b), "lsh_batch_synchronize")
+
+    def get_state(self, s):
+        p = self.params[s]
+        out = {v: np.empty((p.ny, p.nx), dtype=np.float64) for v in VARS}
+        _check(self.lib.lsh_batch_get_state(self._b, int(s), _ptr_array([out[v].ctypes.data for v in VARS])),
+               "lsh_batch_get_state")
+        return out
+
+    def time(self, s):
+        t, dt, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        _check(self.lib.lsh_batch_get_time(self._b, int(s), ctypes.byref(t), ctypes.byref(dt), ctypes.byref(n)),
+               "lsh_batch_get_time")
+        return t.value, dt.value, n.value
+
+    def autotune(self, trial_steps=8):
+        t = Tune()
+        _check(self.lib.lsh_batch_autotune(self._b, int(trial_steps), ctypes.byref(t)), "lsh_batch_autotune")
+        return t.as_dict()
+
+    def set_tune(self, **kw):
+        t = Tune()
+        _check(self.lib.lsh_batch_get_tune(self._b, ctypes.byref(t)), "lsh_batch_get_tune")
+        for k, v in kw.items():
+            setattr(t, k, v)
+        _check(self.lib.lsh_batch_set_tune(self._b, ctypes.byref(t)), "lsh_batch_set_tune")
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        _check(self.lib.lsh_batch_get_launch_count(self._b, ctypes.byref(n)), "lsh_batch_get_launch_count")
+        return n.value
+
+
+__all__ = ["Solver", "Batch", "Tune", "LshError", "load", "device_available", "SIGNATURES", "_abi"]
