@@ -3,7 +3,9 @@
 // kernels (lsh_batch.cu), so both evaluate exactly the same arithmetic.
 #pragma once
 
+#if defined(__CUDACC__)
 #include <cuda_runtime.h>
+#endif
 
 #include "../../include/lsh.h"
 #include "lsh_scheme.cuh"
@@ -13,6 +15,15 @@ namespace lsh {
 constexpr unsigned long long kRateInitBits = 0ULL;  // +0.0
 constexpr int kEdgeBlock = 128;
 constexpr int kCellBlock = 256;
+
+// Sticky error bit: an atomic OR on the device, a plain OR in host code.
+LSH_HD void err_or(int* word, int bit) {
+#if defined(__CUDA_ARCH__)
+    atomicOr(word, bit);
+#else
+    *word |= bit;
+#endif
+}
 
 struct KArgs {
     Consts c;
@@ -32,7 +43,7 @@ struct KArgs {
 
 // Depths of a face (first order: the cell's; second order: reconstructed).
 template <int ORDER>
-__device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, double& h1, double& h2) {
+LSH_HD void face_depths(const KArgs& a, int id, int side, double& h1, double& h2) {
     h1 = a.W[0][id];
     h2 = a.W[3][id];
     if (ORDER == 2) {
@@ -49,7 +60,7 @@ __device__ __forceinline__ void face_depths(const KArgs& a, int id, int side, do
 // qn = sg qy, qt = -sg qx (Arista_kernel.cu:363-371, 509-525) -- selections
 // and negations, no FP64 arithmetic.
 template <int DIR, int ORDER>
-__device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Face& f) {
+LSH_HD void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Face& f) {
     double qx1 = a.W[1][id], qy1 = a.W[2][id], qx2 = a.W[4][id], qy2 = a.W[5][id], H = a.W[6][id];
     if (ORDER == 2) {
         const double* const* s = (side < 2) ? a.sx : a.sy;
@@ -75,7 +86,7 @@ __device__ __forceinline__ void face_rest(const KArgs& a, int id, int side, bool
 // dir 0: horizontal edge row y between rows y-1 and y, column x.
 // dir 1: vertical edge column x between columns x-1 and x, row y.
 template <int DIR, bool FIRST, int ORDER>
-__device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt) {
+LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
     const int nx = a.c.nx, ny = a.c.ny;
     lsh::EdgeIn e;
     int id0, id1 = -1, side0, row0, row1 = 0;
@@ -183,20 +194,20 @@ __device__ __forceinline__ void do_edge(const KArgs& a, int x, int y, double dt)
     }
 }
 
-__device__ __forceinline__ double minmod(double a, double b) {
+LSH_HD double minmod(double a, double b) {
     if (a > 0.0 && b > 0.0) return (a < b) ? a : b;
     if (a < 0.0 && b < 0.0) return (a > b) ? a : b;
     return 0.0;
 }
 
-__device__ __forceinline__ double recon_var(const KArgs& a, int id, int k) {
+LSH_HD double recon_var(const KArgs& a, int id, int k) {
     if (k == 0) return (a.W[0][id] + a.W[3][id]) - a.W[6][id];
     if (k == 3) return a.W[3][id] - a.W[6][id];
     return a.W[k][id];
 }
 
 // One cell of the second-order reconstruction (k_recon).
-__device__ __forceinline__ void recon_cell(const KArgs& a, int id) {
+LSH_HD void recon_cell(const KArgs& a, int id) {
     const int nx = a.c.nx, ny = a.c.ny;
     const int j = id / nx, i = id - j * nx;
     // A cell whose own and 4 neighbours' depths are all zero only meets dry
@@ -235,6 +246,7 @@ __device__ __forceinline__ void recon_cell(const KArgs& a, int id) {
     }
 }
 
+#if defined(__CUDACC__)
 // Block max of the per-cell rates (non-negative doubles order like their bit
 // patterns), then one 64-bit atomicMax per block.
 template <int BLOCK>
@@ -258,13 +270,14 @@ __device__ __forceinline__ void block_max_bits(unsigned long long v, unsigned lo
         if (lane == 0) atomicMax(target, v);
     }
 }
+#endif
 
 // One cell of the Euler-stage update (k_volume); returns the bits of the
 // cell's acc_w / area for the dt reduction.
 // MODE 0: order 1, in place.  MODE 1: order 2 stage 1 (W -> Wout).
 // MODE 2: order 2 stage 2, Wout = (Xavg + E(W)) / 2.
 template <int MODE>
-__device__ __forceinline__ unsigned long long volume_cell(const KArgs& a, int id, double dt) {
+LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
     const int nx = a.c.nx;
     const int j = id / nx;
     double wo[6], acc[7], w[6], rate;
@@ -310,20 +323,20 @@ __device__ __forceinline__ unsigned long long volume_cell(const KArgs& a, int id
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
-    if (bad) atomicOr(&a.tm->err, 1 << LSH_ERR_NUMERIC);
-    return (unsigned long long)__double_as_longlong(rate);
+    if (bad) err_or(&a.tm->err, 1 << LSH_ERR_NUMERIC);
+    return (unsigned long long)lshm::bits_of(rate);
 }
 
 // dt from the largest acc_w / area: 2 CFL / max rate, 1e30 when no cell has a wave speed
-__device__ __forceinline__ double dt_of(unsigned long long rmax_bits, double two_cfl) {
-    const double m = __longlong_as_double((long long)rmax_bits);
+LSH_HD double dt_of(unsigned long long rmax_bits, double two_cfl) {
+    const double m = lshm::from_bits(rmax_bits);
     return (m > 0.0) ? two_cfl / m : lsh::kBig;
 }
 
 // One edge of the initial-dt pass (procesarAristasDeltaTInicialGPU,
 // Arista_kernel.cu:1129-1308): its wave-speed bound into acc[6].
 template <int DIR, bool FIRST>
-__device__ __forceinline__ void init_wave_edge(const KArgs& a, int x, int y) {
+LSH_HD void init_wave_edge(const KArgs& a, int x, int y) {
     const int nx = a.c.nx, ny = a.c.ny;
     int id0, id1 = -1;
     double bor = 0.0, len;
@@ -364,11 +377,11 @@ __device__ __forceinline__ void init_wave_edge(const KArgs& a, int x, int y) {
 }
 
 // acc_w / area of one cell after the initial wave pass (obtenerDeltaTVolumenesGPU)
-__device__ __forceinline__ unsigned long long init_cell_rate(const KArgs& a, int id) {
+LSH_HD unsigned long long init_cell_rate(const KArgs& a, int id) {
     const int j = id / a.c.nx;
     const double w = a.acc[6][id];
     const double rate = (w < lsh::kEps) ? 0.0 : w * a.geo.inv_area[j];
-    return (unsigned long long)__double_as_longlong(rate);
+    return (unsigned long long)lshm::bits_of(rate);
 }
 
 }  // namespace lsh

@@ -26,6 +26,11 @@
 
 namespace lsh {
 
+#if !defined(__CUDA_ARCH__)
+using std::fabs;
+using std::sqrt;
+#endif
+
 constexpr double kEps = 1.1920928955078125e-07;  // FLT_EPSILON (Constantes.hxx:13)
 constexpr double kSqrt2 = 1.41421356237309504880;
 constexpr double kBig = 1e30;
@@ -69,34 +74,34 @@ struct TimeRec {
 
 struct V4 { double x, y, z, w; };
 
-__device__ __forceinline__ double tmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double tmax(double a, double b) { return (b > a) ? b : a; }
-__device__ __forceinline__ double max0(double a) { return (a > 0.0) ? a : 0.0; }
-__device__ __forceinline__ double fmad(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ double exp_neg(double x) { return lshm::exp_neg(x); }
+LSH_HD double tmin(double a, double b) { return (b < a) ? b : a; }
+LSH_HD double tmax(double a, double b) { return (b > a) ? b : a; }
+LSH_HD double max0(double a) { return (a > 0.0) ? a : 0.0; }
+LSH_HD double fmad(double a, double b, double c) { return lshm::fmad(a, b, c); }
+LSH_HD double exp_neg(double x) { return lshm::exp_neg(x); }
 
 // sqrt(2) h / sqrt(h^4 + max(h, eps_h)^4); exactly 1/h for h > eps_h
-__device__ __forceinline__ double vfac(double h, double eps_h) {
+LSH_HD double vfac(double h, double eps_h) {
     if (h > eps_h) return 1.0 / h;
     const double h2 = h * h, m2 = eps_h * eps_h;
     return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
-__device__ __forceinline__ double pow43(double h) { return h * lshm::cbrt_pos(h); }
+LSH_HD double pow43(double h) { return h * lshm::cbrt_pos(h); }
 
-__device__ __forceinline__ int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }
+LSH_HD int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }
 
 // x == +0 or -0, by bit pattern (integer pipe)
-__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+LSH_HD bool is_zero(double x) { return (lshm::bits_of(x) << 1) == 0; }
 
-__device__ __forceinline__ bool is_bad(double x) {
+LSH_HD bool is_bad(double x) {
     // NaN or Inf by bit pattern (integer pipe, no FP64 compare)
-    return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
+    return (lshm::bits_of(x) & 0x7ff0000000000000ULL) == 0x7ff0000000000000ULL;
 }
 
 // Compare-and-swap sequence of Arista_kernel.cu:193-234 (with its (2,1)
 // compare) or, with `full`, the same sequence made a true sort.
-__device__ __forceinline__ void sort_eig(V4& D, int full) {
+LSH_HD void sort_eig(V4& D, int full) {
     double t;
     if (D.x > D.y) { t = D.y; D.y = D.x; D.x = t; }
     if (D.x > D.z) { t = D.z; D.z = D.x; D.x = t; }
@@ -112,7 +117,7 @@ __device__ __forceinline__ void sort_eig(V4& D, int full) {
 // granular layer is absent (h2 = 0, u2 = 0), so the internal pair is exactly
 // zero and its square root is skipped.
 template <bool L2>
-__device__ __forceinline__ V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c,
+LSH_HD V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c,
                                   double Fknown = -1.0, double sqrt_h = -1.0) {
     const double h = L2 ? h1 + h2 : h1;
     // single layer: vfac(h1 + 0) is vfac(h1), which the caller may already hold
@@ -133,7 +138,7 @@ __device__ __forceinline__ V4 eig(double h1, double h2, double u1, double u2, do
 }
 
 // defTerminoFriccion (Arista_kernel.cu:11-58)
-__device__ __forceinline__ double friction_mu(double h1, double u1, double h2, double u2, const Consts& c) {
+LSH_HD double friction_mu(double h1, double u1, double h2, double u2, const Consts& c) {
     if (c.law == 0) return c.mu;
     const double a = (10.0 * h1) * c.inv_eps;
     const double rr = 1.0 - c.r * (1.0 - exp_neg(a * a));
@@ -151,7 +156,7 @@ __device__ __forceinline__ double friction_mu(double h1, double u1, double h2, d
     return (muf * c.L) / c.H;
 }
 
-__device__ __forceinline__ double fsc_of(double h1, const Consts& c) {
+LSH_HD double fsc_of(double h1, const Consts& c) {
     const double a = (10.0 * h1) * c.inv_eps;
     return 1.0 - c.r * (1.0 - exp_neg(a * a));
 }
@@ -179,7 +184,7 @@ struct EdgeOut { double m[6], p[6]; double wave; };
 // granular layer (h2 = qn2 = 0); every layer-1 value is then the same as in
 // the general path and every layer-2 output is zero, so that work is skipped.
 template <bool L2>
-__device__ __forceinline__ void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
+LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     const double eps = c.eps_h;
     double Aq1 = e.A.qn1, Aq2 = L2 ? e.A.qn2 : 0.0, Bq1 = e.B.qn1, Bq2 = L2 ? e.B.qn2 : 0.0;
     const double Ah1 = e.A.h1, Bh1 = e.B.h1;
@@ -349,7 +354,7 @@ __device__ __forceinline__ void edge_flux(const EdgeIn& e, double dt, const Cons
 }
 
 // procesarAristaDeltaTInicial: wave-speed bound for the initial dt.
-__device__ __forceinline__ double edge_initial_wave(const Face& A, const Face& B, double len, const Consts& c) {
+LSH_HD double edge_initial_wave(const Face& A, const Face& B, double len, const Consts& c) {
     const double eps = c.eps_h;
     const double h1ij = 0.5 * (A.h1 + B.h1);
     const double fA1 = vfac(A.h1, eps), fB1 = vfac(B.h1, eps);
@@ -370,7 +375,7 @@ __device__ __forceinline__ double edge_initial_wave(const Face& A, const Face& B
 // filtroEstado (Volumen_kernel.cu:92-180).  L2 == false: h2 = q2 = 0, so
 // the layer-2 damping (0 times a factor) is skipped.
 template <bool L2>
-__device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) {
+LSH_HD void filtro(double w[6], double dt, const Consts& c) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
 #pragma unroll
@@ -408,7 +413,7 @@ __device__ __forceinline__ void filtro(double w[6], double dt, const Consts& c) 
 // granular layer are empty (h2 = q2 = 0): only the water-bottom branch can run.
 // fo1 = vfac(wo[0]), the old state's water factor, computed by the caller.
 template <bool L2>
-__device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c,
+LSH_HD void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c,
                                               double fo1) {
     if (w[0] < 0.0) w[0] = 0.0;
     if (w[3] < 0.0) w[3] = 0.0;
@@ -471,7 +476,7 @@ __device__ __forceinline__ void dis_implicita(const double wo[6], double w[6], d
 }
 
 // coulomb (Volumen_kernel.cu:7-26)
-__device__ __forceinline__ void coulomb(double w[6], double dt, const Consts& c) {
+LSH_HD void coulomb(double w[6], double dt, const Consts& c) {
     if (!(w[3] > 0.0)) {
         w[4] = w[4] * 0.0;
         w[5] = w[5] * 0.0;
@@ -496,7 +501,7 @@ __device__ __forceinline__ void coulomb(double w[6], double dt, const Consts& c)
 // `rate` gets acc_w / area (0 below EPSILON): the step's dt is
 // 2 CFL / max(rate), the min over cells of 2 CFL area / acc_w
 // (Volumen_kernel.cu:256) with one division per step.
-__device__ __forceinline__ void volume_update(const double wo[6], const double acc[7], double w[6], double& rate,
+LSH_HD void volume_update(const double wo[6], const double acc[7], double w[6], double& rate,
                                               double inv_area, double tanR, double dt, const Consts& c) {
     rate = (acc[6] < kEps) ? 0.0 : acc[6] * inv_area;
     const double b = dt * inv_area;

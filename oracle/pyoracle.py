@@ -23,8 +23,10 @@ _ref = None
 
 def build(force=False):
     """Compile the oracle (a second or two)."""
+    srcs = [os.path.join(HERE, "lsh_oracle.cpp"), os.path.join(HERE, "dual.h"),
+            os.path.join(HERE, "..", "landslidehysea_gb300", "csrc", "lsh_fpmath.h")]
     if force or not os.path.exists(ORACLE_SO) or \
-            os.path.getmtime(ORACLE_SO) < os.path.getmtime(os.path.join(HERE, "lsh_oracle.cpp")):
+            os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["sh", os.path.join(HERE, "build_oracle.sh")], check=True)
     return ORACLE_SO
 
@@ -47,6 +49,9 @@ def lib():
         _lib.orc_masks.argtypes = [P, P, P]
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_fpmath.argtypes = [ctypes.c_int, P, P, ctypes.c_longlong]
+        D = ctypes.POINTER(ctypes.c_double)
+        _lib.orc_misfit_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, D, ctypes.c_int, P, P, D, P]
+        _lib.orc_tl_run.argtypes = [P, P, P, P, ctypes.c_longlong, ctypes.c_int, D, D, ctypes.c_int, P, P, D, D, P]
     return _lib
 
 
@@ -139,3 +144,50 @@ def ref_run(params, state, nsteps, eta=None):
                           p.vmax1, p.vmax2, p.gravity, p.eps_h, p.L, p.H, int(nsteps), trace.ctypes.data,
                           ctypes.byref(t), em, et)
     return arrs, trace, t.value
+
+
+def _gauge_args(gauges, target, nsteps):
+    g = np.ascontiguousarray(gauges if gauges is not None else np.zeros(0), dtype=np.int32)
+    t = None if target is None else np.ascontiguousarray(target, dtype=np.float64).reshape(nsteps, len(g))
+    return g, t
+
+
+def misfit_run(params, arrs, nsteps, dt=None, gauges=None, target=None):
+    """Forward run of `nsteps` with the gauge misfit (oracle).  `arrs` (7
+    arrays) is advanced in place.  dt None: the initial-dt pass.  Returns
+    (J, dt_next, eta series [nsteps, n_gauges])."""
+    g, t = _gauge_args(gauges, target, nsteps)
+    eta = np.zeros((nsteps, len(g)))
+    d = ctypes.c_double(0.0 if dt is None else dt)
+    J = ctypes.c_double()
+    st = lib().orc_misfit_run(ctypes.byref(params), _ptrs(arrs), int(nsteps), int(dt is None), ctypes.byref(d),
+                              len(g), g.ctypes.data if len(g) else None, t.ctypes.data if t is not None else None,
+                              ctypes.byref(J), eta.ctypes.data if len(g) else None)
+    if st:
+        raise RuntimeError(f"orc_misfit_run: status {st}")
+    return J.value, d.value, eta
+
+
+def tl_run(params, arrs, darrs, dpar, nsteps, dt=None, ddt=0.0, gauges=None, target=None):
+    """Tangent-linear run (oracle on dual numbers).  darrs: 6 tangent arrays
+    (h1..q2y, None = 0), advanced in place with `arrs`; dpar: tangents of
+    (angle1, mf0, mfs, r).  Returns (J, dJ, dt_next, ddt_next)."""
+    g, t = _gauge_args(gauges, target, nsteps)
+    N = arrs[0].size
+    dd = [np.zeros(N) if a is None else a for a in darrs]
+    for a in dd:
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    dp = np.ascontiguousarray(dpar, dtype=np.float64)
+    d = ctypes.c_double(0.0 if dt is None else dt)
+    dd_t = ctypes.c_double(ddt)
+    J = ctypes.c_double()
+    dJ = ctypes.c_double()
+    st = lib().orc_tl_run(ctypes.byref(params), _ptrs(arrs), _ptrs(dd), dp.ctypes.data, int(nsteps), int(dt is None),
+                          ctypes.byref(d), ctypes.byref(dd_t), len(g), g.ctypes.data if len(g) else None,
+                          t.ctypes.data if t is not None else None, ctypes.byref(J), ctypes.byref(dJ), None)
+    if st:
+        raise RuntimeError(f"orc_tl_run: status {st}")
+    for a, b in zip(darrs, dd):
+        if a is not None and a is not b:
+            a[...] = b
+    return J.value, dJ.value, d.value, dd_t.value
