@@ -272,6 +272,19 @@ struct EdgeIn {
 template <class T>
 struct EdgeOut { T m[6], p[6]; T wave; };
 
+// A face pair with no granular layer (h2 = qn2 = 0 on both faces): the
+// two-layer formulas then reduce to the water layer's, but their derivatives
+// with respect to h2 contain sqrt'(0) and are undefined.  The derivative
+// taken is that of the single-layer branch (the CUDA kernels evaluate such
+// edges with a single-layer specialisation): no sensitivity to h2 or q2.
+// Values are untouched, so the double oracle is unchanged.
+inline void single_layer_branch(Face<double>&, Face<double>&) {}
+inline void single_layer_branch(Face<Dual>& A, Face<Dual>& B) {
+    if (A.h2 == 0.0 && B.h2 == 0.0 && A.qn2 == 0.0 && B.qn2 == 0.0) {
+        A.h2.d = B.h2.d = A.qn2.d = B.qn2.d = A.qt2.d = B.qt2.d = 0.0;
+    }
+}
+
 // procesarArista (Arista_kernel.cu:324-645).  Returns false for a dry edge
 // (no contribution at all, :397).
 template <class T>
@@ -743,6 +756,7 @@ struct Solver {
                     in.acc1h[0] = in.acc1h[1] = 0.0;
                 }
                 EdgeOut<T> o;
+                single_layer_branch(in.A, in.B);
                 if (!edge_flux(in, dt, c, o)) continue;
                 // rotate the normal-frame fluxes back: x = fn nx - ft ny, y = fn ny + ft nx
                 const T nxv = q.nx, nyv = q.ny;

@@ -74,3 +74,73 @@ def test_tl_matches_central_fd(order, spherical, what):
     fd = _fd(p, arrs, gauges, tgt, n, dirs, dpar, scale)
     assert abs(dJ) > 0
     assert abs(fd - dJ) <= 2e-6 * abs(dJ), (fd, dJ)
+
+
+# ---------------------------------------------------------------- local adjoints vs FD
+from adj_cases import host_adjoint, native_lib, scenario_case, wet_direction  # noqa: E402
+
+
+def _worst(fn, modes, seeds=30):
+    import ctypes
+    fd, ad = ctypes.c_double(), ctypes.c_double()
+    out = {}
+    for m in modes:
+        errs = sorted(fn(s, m, 6, ctypes.byref(fd), ctypes.byref(ad)) for s in range(seeds))
+        out[m] = (errs[len(errs) // 2], errs[-1])
+    return out
+
+
+def test_local_edge_adjoint_vs_fd():
+    lib = native_lib("adj_local")
+    lib.adjl_set_component(-1)
+    # bit0 granular layer, bit1 limiter active, bit2 boundary edge, bit3 Coulomb regime
+    for bor in (0.5, 1.0, -1.0):
+        lib.adjl_set_bor(bor)
+        for mode, (med, worst) in _worst(lib.adjl_edge, [0, 1, 2, 3, 4, 5, 7, 9, 11]).items():
+            assert med < 1e-7 and worst < 5e-5, (bor, mode, med, worst)
+
+
+def test_local_volume_adjoint_vs_fd():
+    lib = native_lib("adj_local")
+    lib.adjl_set_component(-1)
+    # bit0 granular layer, bit1 spherical, bit2 thin layers, bit3 vmax caps
+    for mode, (med, worst) in _worst(lib.adjl_volume, [0, 1, 2, 3, 4, 5, 8, 9]).items():
+        assert med < 1e-7 and worst < 5e-5, (mode, med, worst)
+
+
+def test_local_initial_wave_adjoint_vs_fd():
+    import ctypes
+    lib = native_lib("adj_local")
+    fd, ad = ctypes.c_double(), ctypes.c_double()
+    errs = sorted(lib.adjl_initial_wave(s, 6, ctypes.byref(fd), ctypes.byref(ad)) for s in range(30))
+    assert errs[15] < 1e-6 and errs[-1] < 1e-4
+
+
+# ---------------------------------------------------------------- the whole sweep vs the tangent-linear
+def _dot_check(p, arrs, gauges, n, dirs_list, tol):
+    _, _, eta = pyoracle.misfit_run(p, copy_arrs(arrs), n, gauges=gauges)
+    tgt = eta + 0.01 * np.random.default_rng(5).standard_normal(eta.shape)
+    J, grad, gpar = host_adjoint(p, copy_arrs(arrs), n, gauges, tgt)
+    Jo, _, _ = pyoracle.misfit_run(p, copy_arrs(arrs), n, gauges=gauges, target=tgt)
+    assert J == Jo
+    for dirs, dpar in dirs_list:
+        dd = [None if x is None else x.copy() for x in dirs]
+        _, dJ, _, _ = pyoracle.tl_run(p, copy_arrs(arrs), dd, dpar, n, gauges=gauges, target=tgt)
+        ad = sum(float(np.dot(grad[k], dirs[k])) for k in range(6) if dirs[k] is not None) + float(np.dot(gpar, dpar))
+        assert abs(ad - dJ) <= tol * max(abs(dJ), 1e-300), (dpar, dJ, ad)
+
+
+@pytest.mark.parametrize("order,spherical", [(1, False), (2, False), (2, True)])
+def test_host_adjoint_equals_tangent_linear_smooth(order, spherical):
+    p, arrs, gauges = smooth_case(order=order, spherical=spherical)
+    dl = [(smooth_direction(p.nx, p.ny, 3, which=w), [0, 0, 0, 0]) for w in ((3,), (0,), (1, 2), (4, 5))]
+    dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
+    _dot_check(p, arrs, gauges, 4, dl, 1e-11)
+
+
+@pytest.mark.parametrize("kind,order", [("shelf", 1), ("shelf", 2), ("fjord", 2)])
+def test_host_adjoint_equals_tangent_linear_scenarios(kind, order):
+    p, arrs, gauges = scenario_case(kind, order)
+    dl = [(wet_direction(arrs, w, 7), [0, 0, 0, 0]) for w in ((3,), (0,), (1, 2), (4, 5))]
+    dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
+    _dot_check(p, arrs, gauges, 5, dl, 1e-11)
