@@ -48,8 +48,12 @@ def parse():
     ap.add_argument("--n", type=int, default=2048, help="grid size (n x n); the headline is 2048")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("fjord", "ensemble"), default="fjord",
-                    help="fjord: the 2048^2 headline; ensemble: the batched 256-scenario ensemble vs serial")
+    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint"), default="fjord",
+                    help="fjord: the 2048^2 headline; ensemble: the batched 256-scenario ensemble vs serial; "
+                         "adjoint: gradient of the 16-gauge misfit on the 1024^2 fjord vs its forward")
+    ap.add_argument("--adj-n", type=int, default=1024, help="adjoint workload grid size")
+    ap.add_argument("--adj-steps", type=int, default=4000, help="adjoint workload steps")
+    ap.add_argument("--adj-budget-gb", type=float, default=None, help="checkpoint budget (default 180 GB or free)")
     ap.add_argument("--count", type=int, default=256, help="ensemble scenarios")
     return ap.parse_args()
 
@@ -427,10 +431,76 @@ def run_ensemble(args):
     return 0
 
 
+def run_adjoint(args):
+    """Adjoint workload: the 16-gauge misfit of an N-step run of the n^2
+    second-order spherical fjord against a twin run whose Coulomb angle,
+    Manning coefficients and density ratio are perturbed by seeded +-5%;
+    gradient with respect to the initial h2 field and (angle1, mf0, mfs, r).
+    Reports the wall time of lsh_adjoint_forward + lsh_adjoint_gradient
+    (recomputation included) over the wall time of the same N steps through
+    lsh_step (the product's forward, CUDA graphs)."""
+    import copy
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from landslidehysea_gb300 import build as B
+    B.build()
+    from landslidehysea_gb300 import scenarios
+    from landslidehysea_gb300.solver import Adjoint, Solver
+    sc = scenarios.fjord(n=args.adj_n)
+    p = sc.params
+    ij = [(int(i), int(j)) for i, j in sc.gauges if i >= 0 and j >= 0]
+    gauges = np.array([j * p.nx + i for i, j in ij], dtype=np.int32)
+    nsteps = args.adj_steps
+    rng = np.random.default_rng(2024)
+    twin = copy.copy(p)
+    f = 1.0 + 0.05 * rng.choice([-1.0, 1.0], 4)
+    twin.angle1, twin.mf0, twin.mfs, twin.r = p.angle1 * f[0], p.mf0 * f[1], p.mfs * f[2], p.r * f[3]
+    with Adjoint(twin, gauges) as T:
+        T.set_budget(0.0 + 6 * 8 * (p.nx * p.ny + 32) + 1.0)
+        _, target = T.forward(sc.state, nsteps)
+    # the forward alone: N steps through lsh_step
+    s = Solver(p, device=local)
+    s.set_state(sc.state)
+    s.synchronize()
+    t0 = time.perf_counter()
+    s.step(nsteps)
+    s.synchronize()
+    t_fwd = time.perf_counter() - t0
+    s.close()
+    with Adjoint(p, gauges, device=local) as A:
+        if args.adj_budget_gb is not None:
+            A.set_budget(args.adj_budget_gb * 1e9)
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            J, _ = A.forward(sc.state, nsteps, target)
+            t1 = time.perf_counter()
+            g, gp = A.gradient()
+            t2 = time.perf_counter()
+        st = A.stats()
+    ratio = (t2 - t0) / t_fwd
+    line = {"metric": "adjoint/forward wall time, 16-gauge misfit gradient", "value": ratio, "unit": "x",
+            "n_gpus": 1, "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * (t2 - t0) / nsteps,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"fjord{args.adj_n}x{args.adj_n}_order2_spherical_adjoint", "steps": nsteps,
+                       "gauges": int(gauges.size), "twin_perturbation": [float(x) for x in f],
+                       "gradient": ["h2 field", "angle1", "mf0", "mfs", "r"]},
+            "forward_s": t_fwd, "adjoint_forward_s": t1 - t0, "adjoint_gradient_s": t2 - t1, "misfit": J,
+            "grad_params": gp, "grad_h2_l2": float(np.linalg.norm(g["h2"])), "stats": st,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "ours" and args.workload == "ensemble":
         return run_ensemble(args)
+    if args.impl == "ours" and args.workload == "adjoint":
+        return run_adjoint(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -218,6 +218,52 @@ int lsh_batch_set_tune(lsh_batch* b, const lsh_tune* tune);
 int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune);
 int lsh_batch_get_launch_count(lsh_batch* b, long long* launches);
 
+/* ------------------------------------------------------------------------
+ * Discrete adjoint (no counterpart in the reference, which has no
+ * differentiation): the gradient of
+ *   J = w * sum_{n=1..N} sum_g (eta1_n[g] - target[n-1][g])^2 + <bar_final, X_N>,
+ * eta1 = h1 + h2 - H at gauge cells after each step, with respect to the
+ * initial h1, q1x, q1y, h2, q2x, q2y of every cell and to (angle1, mf0, mfs, r).
+ * dt is the CFL step of the previous state and is differentiated as such.
+ * Checkpoints follow a binomial (revolve) schedule in as many state slots as
+ * the memory budget holds (default 180 GB, capped by free device memory).
+ * Coulomb friction law only.
+ * ------------------------------------------------------------------------ */
+typedef struct lsh_adjoint lsh_adjoint;
+
+typedef struct lsh_adjoint_stats {
+    int32_t slots;              /* checkpoint slots (states) held              */
+    int32_t nsteps;             /* steps of the recorded forward run           */
+    int64_t forward_steps;      /* steps run by lsh_adjoint_forward            */
+    int64_t recompute_steps;    /* steps re-advanced by the schedule           */
+    int64_t reversed_steps;     /* steps reversed (each recomputed once more)  */
+    double ms_forward;          /* wall time of the last lsh_adjoint_forward   */
+    double ms_gradient;         /* wall time of the last lsh_adjoint_gradient  */
+    double slot_bytes;          /* device bytes per checkpoint slot            */
+} lsh_adjoint_stats;
+
+int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const int* gauge_cells,
+                       lsh_adjoint** out);
+int lsh_adjoint_destroy(lsh_adjoint* a);
+/* device bytes the checkpoint slots may take */
+int lsh_adjoint_set_budget(lsh_adjoint* a, double bytes);
+/* run nsteps from host_state (7 arrays); target: nsteps x n_gauges (NULL: no
+ * misfit); misfit: J without the weight; gauge_series: nsteps x n_gauges (may be NULL) */
+int lsh_adjoint_forward(lsh_adjoint* a, const double* const host_state[LSH_NVARS], int nsteps, const double* target,
+                        double* misfit, double* gauge_series);
+/* gradient of misfit_weight * J + <bar_final, X_N> (bar_final: 6 arrays or
+ * NULL); grad_state: 6 host arrays (entries may be NULL); grad_params[4]:
+ * d/d(angle1 [rad], mf0, mfs, r) */
+int lsh_adjoint_gradient(lsh_adjoint* a, double misfit_weight, const double* const bar_final[6],
+                         double* grad_state[6], double grad_params[4]);
+int lsh_adjoint_get_stats(lsh_adjoint* a, lsh_adjoint_stats* out);
+/* the checkpoint schedule alone (no device work): the forward steps it takes
+ * to reverse nsteps with `slots` slots (its first descent included; the
+ * forward run's remaining steps to X_N not) and the optimum
+ * r n - beta(s + 1, r - 1); status 0 when every step is reversed once, in
+ * order, from the right state */
+int lsh_revolve_plan(int nsteps, int slots, long long* forward_steps, long long* optimal);
+
 /* Human-readable text for a status code. */
 const char* lsh_status_string(int status);
 

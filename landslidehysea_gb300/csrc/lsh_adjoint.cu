@@ -1,0 +1,834 @@
+// lsh_adjoint.cu -- the discrete adjoint of the time loop on the GPU (C ABI
+// in include/lsh.h, lsh_adjoint_*).
+//
+// Gradient of  J = w * sum_{n=1..N} sum_g (eta1_n[g] - target[n][g])^2 + <bar_final, X_N>
+// (eta1 = h1 + h2 - H at the gauge cells after each step) with respect to
+// the initial state (h1, q1, h2, q2 of every cell) and to the Coulomb angle,
+// the Manning coefficients mf0, mfs and the density ratio r.  The step's dt
+// is the CFL step of the previous state and is differentiated as such.
+//
+// lsh_adjoint_forward runs the N steps once, recording dt, the largest
+// rate's bits and the gauge series, and stores the checkpoints of the
+// binomial schedule's first descent (lsh_revolve.h) in as many state slots
+// as the memory budget allows.  lsh_adjoint_gradient then walks the schedule
+// backwards.  Reversing step n recomputes it from X_n with the very kernels
+// of the forward (lsh_kernels.cuh), keeping what the adjoint reads: slopes,
+// accumulators after each colour pass, the stage-1 state, the
+// reconstruction's branch tape.  The adjoint kernels then run each stage's
+// operators in reverse: volume update, the four colour passes (last first),
+// reconstruction.  They use the hand-written bodies of lsh_adjoint.cuh.
+// Every branch (wet/dry, Coulomb stop, limiter, eigenvalue order, minmod)
+// takes the forward's direction, because the recomputation is bit-identical.
+// Parameter and dt adjoints are summed per block, then in a fixed order:
+// the gradient is bit-reproducible.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lsh.h"
+#include "lsh_adjoint.cuh"
+#include "lsh_kernels.cuh"
+#include "lsh_revolve.h"
+#include "lsh_setup.h"
+
+using lsh::AdjArgs;
+using lsh::ConstBar;
+using lsh::Consts;
+using lsh::Geo;
+
+namespace {
+
+constexpr int kAdjEdgeBlock = 128;
+constexpr int kAdjCellBlock = 128;
+constexpr int kRed = 9;        // dt adjoint + the 8 constant adjoints
+constexpr int kPartSlots = 11;  // partial-sum launches per reversed step (2 stages x 5, + initial dt)
+
+// ------------------------------------------------------------------ device helpers
+
+template <int BLOCK>
+__device__ void block_sum9(double v[kRed], double* out) {
+    __shared__ double sh[BLOCK / 32][kRed];
+#pragma unroll
+    for (int k = 0; k < kRed; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kRed; ++k) sh[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < kRed) {
+        double s = 0.0;
+        for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+__device__ void pack9(double dtb, const ConstBar& cb, double v[kRed]) {
+    v[0] = dtb; v[1] = cb.r; v[2] = cb.omr; v[3] = cb.gp; v[4] = cb.inv_gp;
+    v[5] = cb.mu; v[6] = cb.g_mf02; v[7] = cb.g_mfs2; v[8] = cb.eps_1r;
+}
+
+// Where the stage-1 dt rate peaks and the adjoint of that rate.
+struct RateSel {
+    long long cell;
+    double bar;
+};
+
+template <int DIR, bool FIRST, int ORDER>
+__global__ void __launch_bounds__(kAdjEdgeBlock) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
+    a.rate_cell = rs ? rs->cell : -1;
+    a.rate_bar = rs ? rs->bar : 0.0;
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int nlines = (DIR == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
+    const long long E = (DIR == 0) ? (long long)nlines * nx : (long long)nlines * ny;
+    double dtb = 0.0;
+    ConstBar cb;
+    lsh::cb_zero(cb);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < E;
+         idx += (long long)gridDim.x * blockDim.x) {
+        if (DIR == 0) {
+            const int t = (int)(idx / nx), x = (int)(idx - (long long)t * nx);
+            lsh::edge_adj_body<0, FIRST, ORDER>(a, x, par + 2 * t, dtb, cb);
+        } else {
+            const int y = (int)(idx / nlines), t = (int)(idx - (long long)y * nlines);
+            lsh::edge_adj_body<1, false, ORDER>(a, par + 2 * t, y, dtb, cb);
+        }
+    }
+    double v[kRed];
+    pack9(dtb, cb, v);
+    block_sum9<kAdjEdgeBlock>(v, part + (size_t)blockIdx.x * kRed);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kAdjCellBlock) k_adj_volume(AdjArgs a, const RateSel* rs, double* part) {
+    a.rate_cell = rs ? rs->cell : -1;
+    a.rate_bar = rs ? rs->bar : 0.0;
+    const long long N = (long long)a.c.nx * a.c.ny;
+    double dtb = 0.0;
+    ConstBar cb;
+    lsh::cb_zero(cb);
+    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
+        lsh::volume_adj_body<MODE>(a, (int)id, dtb, cb);
+    double v[kRed];
+    pack9(dtb, cb, v);
+    block_sum9<kAdjCellBlock>(v, part + (size_t)blockIdx.x * kRed);
+}
+
+__global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
+    const long long N = (long long)a.c.nx * a.c.ny;
+    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
+        lsh::recon_adj_cell(a, (int)id);
+}
+
+struct P7 {
+    const double* p[7];
+};
+
+__global__ void __launch_bounds__(kAdjCellBlock) k_adj_tape(P7 W, int nx, int ny, unsigned* tape) {
+    const long long N = (long long)nx * ny;
+    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
+        tape[id] = lsh::recon_tape_cell(W.p, nx, ny, (int)id);
+}
+
+// Max and arg-max (lowest cell on ties) of acc_w / area (0 below EPSILON).
+__global__ void __launch_bounds__(kCellBlock) k_adj_rate_max(const double* acc6, Geo geo, int nx, long long N,
+                                                             unsigned long long* rmax) {
+    unsigned long long bits = 0;
+    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x) {
+        const double w = acc6[id];
+        const double rate = (w < lsh::kEps) ? 0.0 : w * geo.inv_area[id / nx];
+        const unsigned long long b = lshm::bits_of(rate);
+        bits = (b > bits) ? b : bits;
+    }
+    lsh::block_max_bits<kCellBlock>(bits, rmax);
+}
+
+__global__ void __launch_bounds__(kCellBlock) k_adj_argmax(const double* acc6, Geo geo, int nx, long long N,
+                                                           const unsigned long long* rmax, long long* cell) {
+    const unsigned long long m = *rmax;
+    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x) {
+        const double w = acc6[id];
+        const double rate = (w < lsh::kEps) ? 0.0 : w * geo.inv_area[id / nx];
+        if (m != 0 && lshm::bits_of(rate) == m) atomicMin((unsigned long long*)cell, (unsigned long long)id);
+    }
+}
+
+// dt' = 2 CFL / R: the adjoint of the largest rate R is -dt'bar dt' / R (the
+// volume adjoint turns it into acc_w's, times 1 / area, at the arg-max cell).
+__global__ void k_adj_ratebar(const unsigned long long* rmax, const long long* cell, const double* red,
+                              const double* dt_next, RateSel* out) {
+    const double R = lshm::from_bits(*rmax);
+    const long long c = *cell;
+    const double dtb = red[0];
+    if (!(R > 0.0) || c < 0 || c == 0x7fffffffffffffffLL || dtb == 0.0) {
+        out->cell = -1;
+        out->bar = 0.0;
+        return;
+    }
+    out->cell = c;
+    out->bar = -dtb * (*dt_next / R);
+}
+
+// The misfit's adjoint at the state after a step: 2 w (eta - target) at each gauge.
+__global__ void k_adj_gauges(double* hb1, double* hb2, const int* gauges, int ng, const double* eta, const double* tgt,
+                             double w) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int id = gauges[g];
+    // several gauges may share a cell: one thread adds them all, in order
+    if (g > 0) {
+        for (int h = 0; h < g; ++h)
+            if (gauges[h] == id) return;
+    }
+    double s = 0.0;
+    for (int h = g; h < ng; ++h)
+        if (gauges[h] == id) s += w * (2.0 * (eta[h] - tgt[h]));
+    hb1[id] += s;
+    hb2[id] += s;
+}
+
+__global__ void k_adj_init(AdjArgs a, const RateSel* rs, double* part) {
+    double v[kRed] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (threadIdx.x == 0 && rs->cell >= 0) {
+        ConstBar cb;
+        lsh::cb_zero(cb);
+        // rate = acc_w / area at the arg-max cell
+        lsh::init_wave_adj_cell(a, (int)rs->cell, rs->bar * a.geo.inv_area[rs->cell / a.c.nx], cb);
+        pack9(0.0, cb, v);
+    }
+    block_sum9<32>(v, part);
+}
+
+// Sum the step's partials in a fixed order: red[0] = the dt adjoint of the
+// step's input dt; red[1..8] += the constant adjoints.
+__global__ void k_adj_reduce(const double* part, int nparts, double* red) {
+    const int k = threadIdx.x;
+    if (k >= kRed) return;
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += part[(size_t)i * kRed + k];
+    if (k == 0) red[0] = s;
+    else red[k] += s;
+}
+
+__global__ void k_set_dt(lsh::TimeRec* tm, const double* dt) {
+    tm->dt = *dt;
+    tm->rmax_bits = kRateInitBits;
+    tm->done = 0;
+    tm->err = 0;
+    tm->t_end = INFINITY;
+}
+
+__global__ void k_record(const lsh::TimeRec* tm, double* dt_out) { *dt_out = tm->dt; }
+
+__global__ void k_gauge_eta(const double* h1, const double* h2, const double* H, const int* gauges, int ng, double* eta) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int id = gauges[g];
+    eta[g] = (h1[id] + h2[id]) - H[id];
+}
+
+__global__ void k_init_cell(long long* cell) { *cell = 0x7fffffffffffffffLL; }
+
+int afail(cudaError_t e, const char* what) {
+    lsh::set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+    (void)cudaGetLastError();
+    return (e == cudaErrorMemoryAllocation) ? LSH_ERR_GPU_OOM : LSH_ERR_CUDA;
+}
+
+#define A_CUDA(call)                                        \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return afail(e_, #call);     \
+    } while (0)
+
+}  // namespace
+
+// ------------------------------------------------------------------ object
+
+struct lsh_adjoint {
+    lsh_params p;
+    Consts c;
+    int device = 0;
+    int sms = 152;
+    cudaStream_t stream = nullptr;
+    size_t N = 0, npad = 0;
+    int order = 1;
+    // one slab for the working arrays
+    void* slab = nullptr;
+    double* X[7] = {};         // current state (X[6] = H)
+    double* Y[6] = {};         // stage-1 output (order 2)
+    double* s1x[7] = {}, *s1y[7] = {}, *s2x[7] = {}, *s2y[7] = {};
+    double* acc1[7] = {}, *acc2[7] = {};
+    double* snap1[3][2] = {}, *snap2[3][2] = {};
+    double* Xb[6] = {}, *Xbn[6] = {}, *Yb[6] = {};
+    double* sxb[7] = {}, *syb[7] = {}, *accb[7] = {};
+    double* eta_dummy = nullptr;
+    unsigned* tape1 = nullptr, *tape2 = nullptr;
+    double* geo_buf = nullptr;
+    Geo geo{};
+    lsh::TimeRec* tm = nullptr;
+    unsigned long long* rmax = nullptr;  // scratch for the arg-max
+    long long* argmax = nullptr;
+    RateSel* rsel = nullptr;
+    double* part = nullptr;    // kPartSlots x grid x kRed
+    double* red = nullptr;     // kRed
+    // checkpoints
+    double* slots = nullptr;
+    int n_slots = 0;
+    double budget = 180e9;
+    // the recorded forward
+    int nsteps = 0;
+    double* d_dts = nullptr;               // nsteps + 1
+    int ng = 0;
+    int* d_gauges = nullptr;
+    double* d_eta = nullptr;               // nsteps * ng
+    double* d_tgt = nullptr;               // nsteps * ng
+    bool have_target = false;
+    double misfit_weight = 1.0;
+    std::vector<double> h_dts;
+    bool have_forward = false;
+    bool spine_stored = false;  // slots 1.. hold the first descent (until a reverse sweep reuses them)
+    int cur_step = -1;          // step of the state in X
+    int grid = 0;
+    lsh_adjoint_stats stats{};
+    std::vector<int> spine;  // steps stored in slots 1, 2, ... by the forward sweep
+};
+
+namespace {
+
+KArgs fwd_args(const lsh_adjoint* A, const double* const* W, double* const* Wout, const double* const* Xavg,
+               double* const* acc, double* const* sx, double* const* sy) {
+    KArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.c = A->c;
+    a.geo = A->geo;
+    for (int k = 0; k < 7; ++k) {
+        a.W[k] = W[k];
+        a.acc[k] = acc[k];
+        a.sx[k] = sx ? sx[k] : nullptr;
+        a.sy[k] = sy ? sy[k] : nullptr;
+        a.sxw[k] = sx ? sx[k] : nullptr;
+        a.syw[k] = sy ? sy[k] : nullptr;
+    }
+    for (int k = 0; k < 6; ++k) { a.Wout[k] = Wout ? Wout[k] : nullptr; a.Xavg[k] = Xavg ? Xavg[k] : nullptr; }
+    a.eta_max = A->eta_dummy;
+    a.eta_time = A->eta_dummy;
+    a.tm = A->tm;
+    return a;
+}
+
+dim3 grid_h(const lsh_adjoint* A, int par) {
+    const int nlines = (A->p.ny - par) / 2 + 1;
+    return dim3((A->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min(nlines, 65535));
+}
+dim3 grid_v(const lsh_adjoint* A, int par) {
+    const int nlines = (A->p.nx - par) / 2 + 1;
+    return dim3((nlines + kEdgeBlock - 1) / kEdgeBlock, std::min(A->p.ny, 65535));
+}
+unsigned cell_blocks(const lsh_adjoint* A) { return unsigned((A->N + kCellBlock - 1) / kCellBlock); }
+
+// The four colour passes of one stage; snaps (may be null) get acc[0], acc[3]
+// after the first three.
+template <int ORDER>
+void fwd_passes(const lsh_adjoint* A, const KArgs& a, double* snaps[3][2], double* const* acc, cudaStream_t s) {
+    const size_t bytes = A->N * sizeof(double);
+    k_edges_h<true, ORDER><<<grid_h(A, 0), kEdgeBlock, 0, s>>>(a, 0);
+    if (snaps) { cudaMemcpyAsync(snaps[0][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[0][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
+    k_edges_h<false, ORDER><<<grid_h(A, 1), kEdgeBlock, 0, s>>>(a, 1);
+    if (snaps) { cudaMemcpyAsync(snaps[1][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[1][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
+    k_edges_v<ORDER><<<grid_v(A, 0), kEdgeBlock, 0, s>>>(a, 0);
+    if (snaps) { cudaMemcpyAsync(snaps[2][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[2][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
+    k_edges_v<ORDER><<<grid_v(A, 1), kEdgeBlock, 0, s>>>(a, 1);
+}
+
+// One forward step X -> X (the product's step: the same kernels and order),
+// with the time record's dt; k_advance leaves the next dt in the record.
+void fwd_step(const lsh_adjoint* A, cudaStream_t s) {
+    const unsigned nb = cell_blocks(A);
+    double* const* X = A->X;
+    if (A->order == 1) {
+        const KArgs a = fwd_args(A, X, X, nullptr, A->acc1, nullptr, nullptr);
+        fwd_passes<1>(A, a, nullptr, A->acc1, s);
+        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+    } else {
+        double* Y7[7];
+        for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+        Y7[6] = A->X[6];
+        const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+        k_recon<<<nb, kCellBlock, 0, s>>>(a1);
+        fwd_passes<2>(A, a1, nullptr, A->acc1, s);
+        k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+        const KArgs a2 = fwd_args(A, Y7, X, X, A->acc2, A->s2x, A->s2y);
+        k_recon<<<nb, kCellBlock, 0, s>>>(a2);
+        fwd_passes<2>(A, a2, nullptr, A->acc2, s);
+        k_volume<2><<<nb, kCellBlock, 0, s>>>(a2);
+    }
+    k_advance<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
+}
+
+AdjArgs adj_args(const lsh_adjoint* A, const double* const* W, const double* const* sx, const double* const* sy,
+                 double* const* acc, double* const* Wbar, const double* const* wbar, double* const* Xbar,
+                 const unsigned* tape, double dt) {
+    AdjArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.c = A->c;
+    a.geo = A->geo;
+    for (int k = 0; k < 7; ++k) {
+        a.W[k] = W[k];
+        a.sx[k] = sx ? sx[k] : nullptr;
+        a.sy[k] = sy ? sy[k] : nullptr;
+        a.acc[k] = acc ? acc[k] : nullptr;
+        a.sxb[k] = A->sxb[k];
+        a.syb[k] = A->syb[k];
+        a.accb[k] = A->accb[k];
+    }
+    for (int k = 0; k < 6; ++k) {
+        a.Wbar[k] = Wbar[k];
+        a.wbar[k] = wbar ? wbar[k] : nullptr;
+        a.Xbar[k] = Xbar ? Xbar[k] : nullptr;
+    }
+    a.tape = tape;
+    a.rate_cell = -1;
+    a.dt = dt;
+    return a;
+}
+
+// Reverse of one stage: volume (MODE), passes last-first, reconstruction.
+template <int ORDER, int MODE>
+void rev_stage(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, int part_slot, cudaStream_t s) {
+    const int G = A->grid;
+    double* part = A->part + (size_t)part_slot * G * kRed;
+    k_adj_volume<MODE><<<G, kAdjCellBlock, 0, s>>>(a, rs, part);
+    part += (size_t)G * kRed;
+    a.snap[0] = snaps[2][0]; a.snap[1] = snaps[2][1];
+    k_adj_edges<1, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 1, part);
+    part += (size_t)G * kRed;
+    a.snap[0] = snaps[1][0]; a.snap[1] = snaps[1][1];
+    k_adj_edges<1, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 0, part);
+    part += (size_t)G * kRed;
+    a.snap[0] = snaps[0][0]; a.snap[1] = snaps[0][1];
+    k_adj_edges<0, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 1, part);
+    part += (size_t)G * kRed;
+    a.snap[0] = a.snap[1] = nullptr;
+    k_adj_edges<0, true, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 0, part);
+    if (ORDER == 2) k_adj_recon<<<G, kAdjCellBlock, 0, s>>>(a);
+}
+
+void zero6(double* const* v, size_t N, cudaStream_t s) {
+    for (int k = 0; k < 6; ++k) cudaMemsetAsync(v[k], 0, N * sizeof(double), s);
+}
+
+struct Ops : lsh::RevolveOps {
+    lsh_adjoint* A;
+    int status = 0;
+    explicit Ops(lsh_adjoint* a) : A(a) {}
+    double* slot(int k, int v) const { return A->slots + ((size_t)k * 6 + v) * A->npad; }
+    int advance(int from, int to) override {
+        for (int n = from; n < to; ++n) {
+            k_set_dt<<<1, 1, 0, A->stream>>>(A->tm, A->d_dts + n);
+            fwd_step(A, A->stream);
+            A->stats.recompute_steps += 1;
+        }
+        A_CUDA(cudaGetLastError());
+        return 0;
+    }
+    int store(int k) override {
+        for (int v = 0; v < 6; ++v)
+            A_CUDA(cudaMemcpyAsync(slot(k, v), A->X[v], A->N * sizeof(double), cudaMemcpyDeviceToDevice, A->stream));
+        return 0;
+    }
+    int restore(int k, int) override {
+        for (int v = 0; v < 6; ++v)
+            A_CUDA(cudaMemcpyAsync(A->X[v], slot(k, v), A->N * sizeof(double), cudaMemcpyDeviceToDevice, A->stream));
+        return 0;
+    }
+    int reverse_step(int n) override;
+};
+
+// Adjoint of step n; the current state is X_n, A->Xb holds the adjoint of
+// X_{n+1}, A->red[0] the adjoint of dt_{n+1}.  Leaves the adjoint of X_n in
+// A->Xb and of dt_n in A->red[0].
+int Ops::reverse_step(int n) {
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    const unsigned nb = cell_blocks(A);
+    const int G = A->grid;
+    // misfit term of X_{n+1}
+    if (A->have_target && A->ng > 0)
+        k_adj_gauges<<<(A->ng + 127) / 128, 128, 0, s>>>(A->Xb[0], A->Xb[3], A->d_gauges, A->ng,
+                                                         A->d_eta + (size_t)n * A->ng, A->d_tgt + (size_t)n * A->ng,
+                                                         A->misfit_weight);
+    // recompute step n's intermediates
+    k_set_dt<<<1, 1, 0, s>>>(A->tm, A->d_dts + n);
+    double* const* X = A->X;
+    const double dt = A->h_dts[n];
+    if (A->order == 1) {
+        const KArgs a = fwd_args(A, X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+        fwd_passes<1>(A, a, A->snap1, A->acc1, s);
+    } else {
+        double* Y7[7];
+        for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+        Y7[6] = A->X[6];
+        const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+        k_recon<<<nb, kCellBlock, 0, s>>>(a1);
+        k_adj_tape<<<G, kAdjCellBlock, 0, s>>>(P7{{X[0], X[1], X[2], X[3], X[4], X[5], X[6]}}, A->p.nx, A->p.ny, A->tape1);
+        fwd_passes<2>(A, a1, A->snap1, A->acc1, s);
+        k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+        const KArgs a2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
+        k_recon<<<nb, kCellBlock, 0, s>>>(a2);
+        k_adj_tape<<<G, kAdjCellBlock, 0, s>>>(P7{{Y7[0], Y7[1], Y7[2], Y7[3], Y7[4], Y7[5], Y7[6]}}, A->p.nx, A->p.ny,
+                                               A->tape2);
+        fwd_passes<2>(A, a2, A->snap2, A->acc2, s);
+    }
+    // the stage-1 rate's arg-max and the adjoint of the rate
+    cudaMemsetAsync(A->rmax, 0, sizeof(unsigned long long), s);
+    k_init_cell<<<1, 1, 0, s>>>(A->argmax);
+    k_adj_rate_max<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax);
+    k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
+    k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts + n + 1, A->rsel);
+    zero6(A->Xbn, N, s);
+    if (A->order == 1) {
+        AdjArgs a = adj_args(A, X, nullptr, nullptr, A->acc1, A->Xbn, A->Xb, nullptr, nullptr, dt);
+        rev_stage<1, 0>(A, a, A->snap1, A->rsel, 0, s);
+    } else {
+        double* Y7[7];
+        for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+        Y7[6] = A->X[6];
+        zero6(A->Yb, N, s);
+        AdjArgs a2 = adj_args(A, Y7, A->s2x, A->s2y, A->acc2, A->Yb, A->Xb, A->Xbn, A->tape2, dt);
+        rev_stage<2, 2>(A, a2, A->snap2, nullptr, 0, s);
+        AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
+        rev_stage<2, 1>(A, a1, A->snap1, A->rsel, 5, s);
+    }
+    k_adj_reduce<<<1, 32, 0, s>>>(A->part, (A->order == 1 ? 5 : 10) * G, A->red);
+    for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
+    A->stats.reversed_steps += 1;
+    A_CUDA(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const int* gauge_cells, lsh_adjoint** out) {
+    if (!out || !params || n_gauges < 0 || (n_gauges > 0 && !gauge_cells)) return LSH_ERR_INVALID;
+    *out = nullptr;
+    if (const char* why = lsh::params_problem(params)) { lsh::set_last_error(why); return LSH_ERR_INVALID; }
+    if (params->friction_law != LSH_FRICTION_COULOMB) {
+        lsh::set_last_error("lsh_adjoint: the Coulomb friction law only");
+        return LSH_ERR_INVALID;
+    }
+    const long long N = (long long)params->nx * params->ny;
+    for (int g = 0; g < n_gauges; ++g)
+        if (gauge_cells[g] < 0 || gauge_cells[g] >= N) { lsh::set_last_error("lsh_adjoint: gauge cell out of range"); return LSH_ERR_INVALID; }
+    if (lsh_check_device() != 0) return LSH_ERR_NO_DEVICE;
+    lsh_adjoint* A = new (std::nothrow) lsh_adjoint();
+    if (!A) return LSH_ERR_HOST_OOM;
+    auto bail = [&](int st) { lsh_adjoint_destroy(A); return st; };
+    A->p = *params;
+    A->p.track_eta_max = 0;
+    A->c = lsh::make_consts(A->p);
+    A->order = params->order;
+    A->N = (size_t)N;
+    A->npad = (A->N + 31) & ~size_t(31);
+    if (device >= 0) { cudaError_t e = cudaSetDevice(device); if (e != cudaSuccess) return bail(afail(e, "cudaSetDevice")); }
+    cudaGetDevice(&A->device);
+    cudaDeviceGetAttribute(&A->sms, cudaDevAttrMultiProcessorCount, A->device);
+    A->grid = 2 * A->sms;
+    { cudaError_t e = cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking); if (e != cudaSuccess) return bail(afail(e, "cudaStreamCreate")); }
+    // working arrays: X 7, Y 6, s1/s2 28, acc 14, snaps 12, Xb/Xbn/Yb 18, sxb/syb/accb 21, eta dummy 1
+    const int narr = 7 + 6 + 28 + 14 + 12 + 18 + 21 + 1;
+    const size_t geo_n = 7 * size_t(params->ny + 1);
+    const size_t bytes = (size_t(narr) * A->npad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) +
+                         2 * A->npad * sizeof(unsigned);
+    { cudaError_t e = cudaMalloc(&A->slab, bytes); if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint work arrays")); }
+    cudaMemsetAsync(A->slab, 0, bytes, A->stream);
+    double* cur = static_cast<double*>(A->slab);
+    auto take = [&](double*& p) { p = cur; cur += A->npad; };
+    for (int k = 0; k < 7; ++k) take(A->X[k]);
+    for (int k = 0; k < 6; ++k) take(A->Y[k]);
+    for (int k = 0; k < 7; ++k) { take(A->s1x[k]); take(A->s1y[k]); take(A->s2x[k]); take(A->s2y[k]); }
+    for (int k = 0; k < 7; ++k) { take(A->acc1[k]); take(A->acc2[k]); }
+    for (int q = 0; q < 3; ++q) for (int v = 0; v < 2; ++v) { take(A->snap1[q][v]); take(A->snap2[q][v]); }
+    for (int k = 0; k < 6; ++k) { take(A->Xb[k]); take(A->Xbn[k]); take(A->Yb[k]); }
+    for (int k = 0; k < 7; ++k) { take(A->sxb[k]); take(A->syb[k]); take(A->accb[k]); }
+    take(A->eta_dummy);
+    A->geo_buf = cur;
+    cur += (geo_n + 31) & ~size_t(31);
+    A->tape1 = reinterpret_cast<unsigned*>(cur);
+    A->tape2 = A->tape1 + A->npad;
+    {
+        std::vector<double> g(geo_n, 0.0);
+        const size_t st = size_t(params->ny + 1);
+        lsh::fill_geo(A->p, g.data(), st);
+        cudaError_t e = cudaMemcpy(A->geo_buf, g.data(), geo_n * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(afail(e, "geometry"));
+        A->geo.area = A->geo_buf; A->geo.len_v = A->geo_buf + st; A->geo.len_h = A->geo_buf + 2 * st;
+        A->geo.tanR = A->geo_buf + 3 * st; A->geo.wx = A->geo_buf + 4 * st; A->geo.wy = A->geo_buf + 5 * st;
+        A->geo.inv_area = A->geo_buf + 6 * st;
+    }
+    {
+        cudaError_t e = cudaMalloc(&A->tm, sizeof(lsh::TimeRec));
+        if (e == cudaSuccess) e = cudaMalloc(&A->rmax, sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&A->argmax, sizeof(long long));
+        if (e == cudaSuccess) e = cudaMalloc(&A->rsel, sizeof(RateSel));
+        if (e == cudaSuccess) e = cudaMalloc(&A->part, sizeof(double) * kRed * kPartSlots * A->grid);
+        if (e == cudaSuccess) e = cudaMalloc(&A->red, sizeof(double) * kRed);
+        if (e == cudaSuccess && n_gauges > 0) e = cudaMalloc(&A->d_gauges, sizeof(int) * n_gauges);
+        if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint scalars"));
+    }
+    A->ng = n_gauges;
+    if (n_gauges > 0) { cudaError_t e = cudaMemcpy(A->d_gauges, gauge_cells, sizeof(int) * n_gauges, cudaMemcpyHostToDevice); if (e != cudaSuccess) return bail(afail(e, "gauges")); }
+    // default checkpoint budget: 180 GB, capped by what is free (leaving 4 GB)
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    A->budget = std::min(180e9, std::max(0.0, (double)fr - 4e9));
+    A->stats.slot_bytes = 6.0 * A->npad * sizeof(double);
+    { cudaError_t e = cudaStreamSynchronize(A->stream); if (e != cudaSuccess) return bail(afail(e, "init")); }
+    *out = A;
+    return LSH_OK;
+}
+
+int lsh_adjoint_destroy(lsh_adjoint* A) {
+    if (!A) return LSH_OK;
+    if (A->stream) cudaStreamSynchronize(A->stream);
+    cudaFree(A->slab);
+    cudaFree(A->tm); cudaFree(A->rmax); cudaFree(A->argmax); cudaFree(A->rsel); cudaFree(A->part); cudaFree(A->red);
+    cudaFree(A->d_gauges); cudaFree(A->d_eta); cudaFree(A->d_tgt); cudaFree(A->d_dts);
+    cudaFree(A->slots);
+    if (A->stream) cudaStreamDestroy(A->stream);
+    (void)cudaGetLastError();
+    delete A;
+    return LSH_OK;
+}
+
+int lsh_adjoint_set_budget(lsh_adjoint* A, double bytes) {
+    if (!A || !(bytes >= 0.0)) return LSH_ERR_INVALID;
+    A->budget = bytes;
+    return LSH_OK;
+}
+
+int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS], int nsteps, const double* target,
+                        double* misfit, double* gauge_series) {
+    if (!A || !host_state || nsteps < 1) return LSH_ERR_INVALID;
+    for (int k = 0; k < LSH_NVARS; ++k) if (!host_state[k]) return LSH_ERR_INVALID;
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    // (re)allocate the per-step records and the checkpoint slots
+    if (nsteps != A->nsteps) {
+        cudaFree(A->d_dts); cudaFree(A->d_eta); cudaFree(A->d_tgt);
+        A->d_dts = nullptr; A->d_eta = nullptr; A->d_tgt = nullptr;
+        A_CUDA(cudaMalloc(&A->d_dts, sizeof(double) * (nsteps + 1)));
+        if (A->ng > 0) {
+            A_CUDA(cudaMalloc(&A->d_eta, sizeof(double) * (size_t)nsteps * A->ng));
+            A_CUDA(cudaMalloc(&A->d_tgt, sizeof(double) * (size_t)nsteps * A->ng));
+        }
+        A->nsteps = nsteps;
+    }
+    const double slot_bytes = 6.0 * A->npad * sizeof(double);
+    int want = (int)std::min<double>((double)nsteps, std::floor(A->budget / slot_bytes));
+    if (want < 1) { lsh::set_last_error("lsh_adjoint: the checkpoint budget holds no state"); return LSH_ERR_INVALID; }
+    if (want != A->n_slots) {
+        cudaFree(A->slots);
+        A->slots = nullptr;
+        A->n_slots = 0;
+        cudaError_t e = cudaMalloc(&A->slots, (size_t)want * (size_t)slot_bytes);
+        while (e == cudaErrorMemoryAllocation && want > 1) {
+            (void)cudaGetLastError();
+            want = want / 2;
+            e = cudaMalloc(&A->slots, (size_t)want * (size_t)slot_bytes);
+        }
+        if (e != cudaSuccess) return afail(e, "cudaMalloc checkpoint slots");
+        A->n_slots = want;
+    }
+    A->have_target = (target != nullptr) && A->ng > 0;
+    if (A->have_target)
+        A_CUDA(cudaMemcpyAsync(A->d_tgt, target, sizeof(double) * (size_t)nsteps * A->ng, cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < 7; ++k)
+        A_CUDA(cudaMemcpyAsync(A->X[k], host_state[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
+    // initial dt (the same kernels as lsh_set_state)
+    {
+        lsh::TimeRec init{};
+        init.t_end = INFINITY;
+        A_CUDA(cudaMemcpyAsync(A->tm, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+        const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+        const int nx = A->p.nx, ny = A->p.ny;
+        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        k_cell_dt<<<cell_blocks(A), kCellBlock, 0, s>>>(a);
+        k_init_finish<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
+        k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts);
+    }
+    Ops ops(A);
+    A->stats = lsh_adjoint_stats{};
+    A->stats.slots = A->n_slots;
+    A->stats.nsteps = nsteps;
+    A->stats.slot_bytes = slot_bytes;
+    if (int st = ops.store(0)) return st;
+    A->spine.clear();
+    // the schedule's first descent, with the gauge series and dt records
+    int a = 0, free = A->n_slots - 1, slot = 0;
+    auto run = [&](int from, int to) {
+        for (int n = from; n < to; ++n) {
+            fwd_step(A, s);
+            k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts + n + 1);
+            if (A->ng > 0)
+                k_gauge_eta<<<(A->ng + 127) / 128, 128, 0, s>>>(A->X[0], A->X[3], A->X[6], A->d_gauges, A->ng,
+                                                               A->d_eta + (size_t)n * A->ng);
+        }
+        A->stats.forward_steps += to - from;
+    };
+    while (nsteps - a > 1 && free > 0) {
+        const int m = a + (int)lsh::revolve_split(nsteps - a, free + 1);
+        run(a, m);
+        ++slot;
+        if (int st = ops.store(slot)) return st;
+        A->spine.push_back(m);
+        a = m;
+        --free;
+    }
+    run(a, nsteps);
+    A_CUDA(cudaGetLastError());
+    A->h_dts.resize(nsteps + 1);
+    A_CUDA(cudaMemcpyAsync(A->h_dts.data(), A->d_dts, sizeof(double) * (nsteps + 1), cudaMemcpyDeviceToHost, s));
+    std::vector<double> eta((size_t)nsteps * A->ng);
+    if (A->ng > 0)
+        A_CUDA(cudaMemcpyAsync(eta.data(), A->d_eta, sizeof(double) * eta.size(), cudaMemcpyDeviceToHost, s));
+    A_CUDA(cudaStreamSynchronize(s));
+    double J = 0.0;
+    if (A->have_target)
+        for (size_t i = 0; i < eta.size(); ++i) { const double d = eta[i] - target[i]; J = lshm::fmad(d, d, J); }
+    if (misfit) *misfit = J;
+    if (gauge_series && A->ng > 0) std::memcpy(gauge_series, eta.data(), sizeof(double) * eta.size());
+    A->have_forward = true;
+    A->spine_stored = true;
+    A->cur_step = nsteps;
+    A->stats.ms_forward = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return LSH_OK;
+}
+
+int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* const bar_final[6], double* grad_state[6],
+                         double grad_params[4]) {
+    if (!A || !A->have_forward) return LSH_ERR_INVALID;
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    A->misfit_weight = misfit_weight;
+    for (int k = 0; k < 6; ++k) {
+        if (bar_final && bar_final[k]) A_CUDA(cudaMemcpyAsync(A->Xb[k], bar_final[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
+        else A_CUDA(cudaMemsetAsync(A->Xb[k], 0, N * sizeof(double), s));
+    }
+    A_CUDA(cudaMemsetAsync(A->red, 0, sizeof(double) * kRed, s));
+    Ops ops(A);
+    ops.cur = A->cur_step;
+    A->stats.recompute_steps = 0;
+    A->stats.reversed_steps = 0;
+    const bool pre = A->spine_stored;
+    A->spine_stored = false;  // the sweep below reuses the slots
+    A->cur_step = -1;
+    if (int st = lsh::revolve_reverse(ops, 0, A->nsteps, 0, A->n_slots - 1, pre)) return st;
+    // dt_0 from the initial pass of X_0
+    {
+        if (ops.cur != 0) { if (int st = ops.restore(0, 0)) return st; ops.cur = 0; }
+        const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+        const int nx = A->p.nx, ny = A->p.ny;
+        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        const int G = A->grid;
+        cudaMemsetAsync(A->rmax, 0, sizeof(unsigned long long), s);
+        k_init_cell<<<1, 1, 0, s>>>(A->argmax);
+        k_adj_rate_max<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax);
+        k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
+        k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts, A->rsel);
+        AdjArgs aa = adj_args(A, A->X, nullptr, nullptr, nullptr, A->Xb, nullptr, nullptr, nullptr, A->h_dts[0]);
+        double* part = A->part + (size_t)10 * A->grid * kRed;
+        k_adj_init<<<1, 32, 0, s>>>(aa, A->rsel, part);
+        k_adj_reduce<<<1, 32, 0, s>>>(part, 1, A->red);
+    }
+    A_CUDA(cudaGetLastError());
+    for (int k = 0; k < 6; ++k)
+        if (grad_state && grad_state[k])
+            A_CUDA(cudaMemcpyAsync(grad_state[k], A->Xb[k], N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    double red[kRed];
+    A_CUDA(cudaMemcpyAsync(red, A->red, sizeof(red), cudaMemcpyDeviceToHost, s));
+    A_CUDA(cudaStreamSynchronize(s));
+    ConstBar cb{red[1], red[2], red[3], red[4], red[5], red[6], red[7], red[8]};
+    double gp[4];
+    lsh::param_grads(A->p.angle1, A->p.mf0, A->p.mfs, A->p.r, A->p.gravity, A->p.eps_h, A->p.L, A->p.H, cb, gp);
+    if (grad_params) for (int k = 0; k < 4; ++k) grad_params[k] = gp[k];
+    A->cur_step = ops.cur;
+    A->stats.ms_gradient = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return LSH_OK;
+}
+
+int lsh_adjoint_get_stats(lsh_adjoint* A, lsh_adjoint_stats* out) {
+    if (!A || !out) return LSH_ERR_INVALID;
+    *out = A->stats;
+    return LSH_OK;
+}
+
+int lsh_revolve_plan(int nsteps, int slots, long long* forward_steps, long long* optimal) {
+    if (nsteps < 1 || slots < 1) return LSH_ERR_INVALID;
+    // run the schedule with counting operations (no device work)
+    struct Count : lsh::RevolveOps {
+        long long fw = 0;
+        int next = 0;
+        std::vector<int> slot_step;
+        int bad = 0;
+        int advance(int from, int to) override { fw += to - from; return 0; }
+        int store(int k) override {
+            if (k >= (int)slot_step.size()) slot_step.resize(k + 1, -1);
+            slot_step[k] = cur;
+            return 0;
+        }
+        int restore(int k, int step) override {
+            if (k >= (int)slot_step.size() || slot_step[k] != step) bad = 1;
+            return 0;
+        }
+        int reverse_step(int step) override {
+            if (step != next || cur != step) bad = 1;
+            --next;
+            return 0;
+        }
+    } c;
+    c.slot_step.assign(1, 0);
+    c.cur = 0;
+    // the first descent, as lsh_adjoint_forward runs it
+    int a = 0, free = slots - 1, slot = 0;
+    while (nsteps - a > 1 && free > 0) {
+        const int m = a + (int)lsh::revolve_split(nsteps - a, free + 1);
+        c.cur = m;
+        ++slot;
+        c.store(slot);
+        a = m;
+        --free;
+    }
+    const long long descent = a;  // the spine's advances, counted as the schedule counts them
+    c.cur = nsteps;
+    c.next = nsteps - 1;
+    if (lsh::revolve_reverse(c, 0, nsteps, 0, slots - 1, true)) return LSH_ERR_INVALID;
+    if (c.bad || c.next != -1) return LSH_ERR_INVALID;
+    if (forward_steps) *forward_steps = descent + c.fw;
+    if (optimal) *optimal = lsh::revolve_cost(nsteps, slots);
+    return LSH_OK;
+}
+
+}  // extern "C"

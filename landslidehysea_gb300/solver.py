@@ -63,6 +63,14 @@ SIGNATURES = {
     "lsh_batch_set_tune": (ctypes.c_int, [P, P]),
     "lsh_batch_get_tune": (ctypes.c_int, [P, P]),
     "lsh_batch_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
+    "lsh_adjoint_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(P)]),
+    "lsh_adjoint_destroy": (ctypes.c_int, [P]),
+    "lsh_adjoint_set_budget": (ctypes.c_int, [P, ctypes.c_double]),
+    "lsh_adjoint_forward": (ctypes.c_int, [P, P, ctypes.c_int, P, DP, P]),
+    "lsh_adjoint_gradient": (ctypes.c_int, [P, ctypes.c_double, P, P, P]),
+    "lsh_adjoint_get_stats": (ctypes.c_int, [P, P]),
+    "lsh_revolve_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                        ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "lsh_last_error": (ctypes.c_char_p, []),
 }
@@ -292,4 +300,99 @@ class Batch:
         return n.value
 
 
-__all__ = ["Solver", "Batch", "Tune", "LshError", "load", "device_available", "SIGNATURES", "_abi"]
+class AdjointStats(ctypes.Structure):
+    """Mirror of lsh_adjoint_stats."""
+    _fields_ = [("slots", ctypes.c_int32), ("nsteps", ctypes.c_int32), ("forward_steps", ctypes.c_int64),
+                ("recompute_steps", ctypes.c_int64), ("reversed_steps", ctypes.c_int64), ("ms_forward", ctypes.c_double),
+                ("ms_gradient", ctypes.c_double), ("slot_bytes", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+PARAM_NAMES = ("angle1", "mf0", "mfs", "r")
+
+
+class Adjoint:
+    """Discrete adjoint of the time loop (wraps lsh_adjoint): the gradient of
+    w * sum_n sum_g (eta1_n[g] - target)^2 + <bar_final, X_N> with respect to
+    the initial h1..q2y and to (angle1, mf0, mfs, r)."""
+
+    def __init__(self, params, gauges=(), device: int = 0):
+        self.lib = load()
+        self.params = params.copy()
+        self.gauges = np.ascontiguousarray(np.asarray(gauges, dtype=np.int32).reshape(-1))
+        self._a = ctypes.c_void_p()
+        g = self.gauges.ctypes.data if self.gauges.size else None
+        _check(self.lib.lsh_adjoint_create(ctypes.byref(self.params), int(device), int(self.gauges.size), g,
+                                           ctypes.byref(self._a)), "lsh_adjoint_create")
+        self.nsteps = 0
+
+    def close(self):
+        if self._a:
+            self.lib.lsh_adjoint_destroy(self._a)
+            self._a = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_budget(self, nbytes):
+        _check(self.lib.lsh_adjoint_set_budget(self._a, float(nbytes)), "lsh_adjoint_set_budget")
+
+    def forward(self, state, nsteps, target=None):
+        """Run `nsteps` from `state` (dict or 7 arrays); returns (J, eta series [nsteps, n_gauges])."""
+        arrs = [np.ascontiguousarray(state[v] if isinstance(state, dict) else state[i], dtype=np.float64).reshape(-1)
+                for i, v in enumerate(VARS)]
+        ng = self.gauges.size
+        t = None
+        if target is not None:
+            t = np.ascontiguousarray(target, dtype=np.float64).reshape(nsteps, ng)
+        eta = np.zeros((nsteps, ng))
+        J = ctypes.c_double()
+        self._keep = (arrs, t)
+        _check(self.lib.lsh_adjoint_forward(self._a, _ptr_array([a.ctypes.data for a in arrs]), int(nsteps),
+                                            t.ctypes.data if t is not None else None, ctypes.byref(J),
+                                            eta.ctypes.data if ng else None), "lsh_adjoint_forward")
+        self.nsteps = nsteps
+        return J.value, eta
+
+    def gradient(self, misfit_weight=1.0, bar_final=None):
+        """Returns (grad: dict h1..q2y -> (ny, nx), grad_params: dict angle1, mf0, mfs, r)."""
+        p = self.params
+        out = {v: np.zeros((p.ny, p.nx)) for v in VARS[:6]}
+        bf = None
+        if bar_final is not None:
+            arrs = [None if bar_final[v] is None else np.ascontiguousarray(bar_final[v], dtype=np.float64).reshape(-1)
+                    for v in VARS[:6]]
+            bf = _ptr_array([0 if a is None else a.ctypes.data for a in arrs])
+            self._keep_bf = arrs
+        gp = np.zeros(4)
+        _check(self.lib.lsh_adjoint_gradient(self._a, float(misfit_weight), bf,
+                                             _ptr_array([out[v].ctypes.data for v in VARS[:6]]), gp.ctypes.data),
+               "lsh_adjoint_gradient")
+        return out, dict(zip(PARAM_NAMES, gp.tolist()))
+
+    def stats(self):
+        st = AdjointStats()
+        _check(self.lib.lsh_adjoint_get_stats(self._a, ctypes.byref(st)), "lsh_adjoint_get_stats")
+        return st.as_dict()
+
+
+def revolve_plan(nsteps, slots):
+    """(forward steps of the checkpoint schedule, optimal recomputation count),
+    or raises if the schedule does not reverse every step once, in order."""
+    fw, opt = ctypes.c_longlong(), ctypes.c_longlong()
+    _check(load().lsh_revolve_plan(int(nsteps), int(slots), ctypes.byref(fw), ctypes.byref(opt)), "lsh_revolve_plan")
+    return fw.value, opt.value
+
+
+__all__ = ["Solver", "Batch", "Tune", "Adjoint", "revolve_plan", "LshError", "load", "device_available", "SIGNATURES", "_abi"]
