@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--adj-n", type=int, default=1024, help="adjoint workload grid size")
     ap.add_argument("--adj-steps", type=int, default=4000, help="adjoint workload steps")
     ap.add_argument("--adj-budget-gb", type=float, default=None, help="checkpoint budget (default 180 GB or free)")
+    ap.add_argument("--adj-thin", type=float, default=0.1,
+                    help="thin-layer projection of the adjoint, metres (0: the exact adjoint)")
     ap.add_argument("--count", type=int, default=256, help="ensemble scenarios")
     return ap.parse_args()
 
@@ -474,6 +476,7 @@ def run_adjoint(args):
     with Adjoint(p, gauges, device=local) as A:
         if args.adj_budget_gb is not None:
             A.set_budget(args.adj_budget_gb * 1e9)
+        A.set_thin_layer(args.adj_thin)
         with ClockSampler(local) as clk:
             t0 = time.perf_counter()
             J, _ = A.forward(sc.state, nsteps, target)
@@ -487,6 +490,7 @@ def run_adjoint(args):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"fjord{args.adj_n}x{args.adj_n}_order2_spherical_adjoint", "steps": nsteps,
                        "gauges": int(gauges.size), "twin_perturbation": [float(x) for x in f],
+                       "thin_layer_m": args.adj_thin,
                        "gradient": ["h2 field", "angle1", "mf0", "mfs", "r"]},
             "forward_s": t_fwd, "adjoint_forward_s": t1 - t0, "adjoint_gradient_s": t2 - t1, "misfit": J,
             "grad_params": gp, "grad_h2_l2": float(np.linalg.norm(g["h2"])), "stats": st,

@@ -245,6 +245,13 @@ typedef struct lsh_adjoint_stats {
 int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const int* gauge_cells,
                        lsh_adjoint** out);
 int lsh_adjoint_destroy(lsh_adjoint* a);
+/* thin-layer projection (default 0: the exact discrete adjoint): after every
+ * step, the adjoint of a layer thinner than h_adj (h, qx, qy of that layer)
+ * is set to 0, i.e. the gradient of the linearisation in which such layers
+ * are passive.  Over long runs with wet/dry fronts the exact adjoint grows
+ * without bound through the 1/h and sqrt(h) derivatives of thin layers; a
+ * few millimetres to centimetres keeps it finite. */
+int lsh_adjoint_set_thin_layer(lsh_adjoint* a, double h_adj);
 /* device bytes the checkpoint slots may take */
 int lsh_adjoint_set_budget(lsh_adjoint* a, double bytes);
 /* run nsteps from host_state (7 arrays); target: nsteps x n_gauges (NULL: no
@@ -257,6 +264,12 @@ int lsh_adjoint_forward(lsh_adjoint* a, const double* const host_state[LSH_NVARS
 int lsh_adjoint_gradient(lsh_adjoint* a, double misfit_weight, const double* const bar_final[6],
                          double* grad_state[6], double grad_params[4]);
 int lsh_adjoint_get_stats(lsh_adjoint* a, lsh_adjoint_stats* out);
+/* simulated time after each step of the recorded run (nsteps values): the
+ * time axis of the gauge series */
+int lsh_adjoint_get_times(lsh_adjoint* a, double* t_out);
+/* the recorded run's final state X_N (6 host arrays, entries may be NULL);
+ * valid after lsh_adjoint_forward, before lsh_adjoint_gradient */
+int lsh_adjoint_get_state(lsh_adjoint* a, double* const host_state[6]);
 /* the checkpoint schedule alone (no device work): the forward steps it takes
  * to reverse nsteps with `slots` slots (its first descent included; the
  * forward run's remaining steps to X_N not) and the optimum

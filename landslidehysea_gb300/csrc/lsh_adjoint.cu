@@ -130,14 +130,12 @@ __global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
         lsh::recon_adj_cell(a, (int)id);
 }
 
-struct P7 {
-    const double* p[7];
-};
-
-__global__ void __launch_bounds__(kAdjCellBlock) k_adj_tape(P7 W, int nx, int ny, unsigned* tape) {
-    const long long N = (long long)nx * ny;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
-        tape[id] = lsh::recon_tape_cell(W.p, nx, ny, (int)id);
+// The recomputation's reconstruction: slopes (bit-identical to k_recon's)
+// and the branch tape the reconstruction adjoint replays.
+__global__ void __launch_bounds__(kCellBlock) k_recon_tape(KArgs a, unsigned* tape) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.c.nx * a.c.ny) return;
+    tape[id] = lsh::recon_cell_tape(a, id);
 }
 
 // Max and arg-max (lowest cell on ties) of acc_w / area (0 below EPSILON).
@@ -197,6 +195,18 @@ __global__ void k_adj_gauges(double* hb1, double* hb2, const int* gauges, int ng
     hb2[id] += s;
 }
 
+// Thin-layer projection: the adjoint of a layer thinner than h_adj (in the
+// state the adjoint belongs to) is zeroed; the tangent-linear model zeroes
+// the same tangents, so the pair stays transposes of each other.
+__global__ void __launch_bounds__(kCellBlock) k_adj_project(double* b0, double* b1, double* b2,
+                                                            double* b3, double* b4, double* b5, const double* h1,
+                                                            const double* h2, long long N, double h_adj) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        if (h1[i] < h_adj) { b0[i] = 0.0; b1[i] = 0.0; b2[i] = 0.0; }
+        if (h2[i] < h_adj) { b3[i] = 0.0; b4[i] = 0.0; b5[i] = 0.0; }
+    }
+}
+
 __global__ void k_adj_init(AdjArgs a, const RateSel* rs, double* part) {
     double v[kRed] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (threadIdx.x == 0 && rs->cell >= 0) {
@@ -210,14 +220,18 @@ __global__ void k_adj_init(AdjArgs a, const RateSel* rs, double* part) {
 }
 
 // Sum the step's partials in a fixed order: red[0] = the dt adjoint of the
-// step's input dt; red[1..8] += the constant adjoints.
-__global__ void k_adj_reduce(const double* part, int nparts, double* red) {
-    const int k = threadIdx.x;
-    if (k >= kRed) return;
+// step's input dt; red[1..8] += the constant adjoints.  Warp k sums
+// component k (lane-strided, then a shuffle tree): deterministic.
+__global__ void __launch_bounds__(32 * kRed) k_adj_reduce(const double* part, int nparts, double* red) {
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double s = 0.0;
-    for (int i = 0; i < nparts; ++i) s += part[(size_t)i * kRed + k];
-    if (k == 0) red[0] = s;
-    else red[k] += s;
+    for (int i = lane; i < nparts; i += 32) s += part[(size_t)i * kRed + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        if (k == 0) red[0] = s;
+        else red[k] += s;
+    }
 }
 
 __global__ void k_set_dt(lsh::TimeRec* tm, const double* dt) {
@@ -295,6 +309,8 @@ struct lsh_adjoint {
     double* d_tgt = nullptr;               // nsteps * ng
     bool have_target = false;
     double misfit_weight = 1.0;
+    double h_adj = 0.0;       // thin-layer projection threshold (0: the exact adjoint)
+    double* hN[2] = {};       // h1, h2 of the recorded run's final state
     std::vector<double> h_dts;
     bool have_forward = false;
     bool spine_stored = false;  // slots 1.. hold the first descent (until a reverse sweep reuses them)
@@ -428,6 +444,18 @@ void zero6(double* const* v, size_t N, cudaStream_t s) {
     for (int k = 0; k < 6; ++k) cudaMemsetAsync(v[k], 0, N * sizeof(double), s);
 }
 
+// The misfit's adjoint at X_m (m >= 1: the gauges after step m - 1) added to
+// A->Xb, then the thin-layer projection with the depths h1, h2 of X_m.
+void misfit_and_project(lsh_adjoint* A, int m, const double* h1, const double* h2, cudaStream_t s) {
+    if (m >= 1 && A->have_target && A->ng > 0 && A->misfit_weight != 0.0)
+        k_adj_gauges<<<(A->ng + 127) / 128, 128, 0, s>>>(A->Xb[0], A->Xb[3], A->d_gauges, A->ng,
+                                                         A->d_eta + (size_t)(m - 1) * A->ng,
+                                                         A->d_tgt + (size_t)(m - 1) * A->ng, A->misfit_weight);
+    if (A->h_adj > 0.0)
+        k_adj_project<<<A->grid, kCellBlock, 0, s>>>(A->Xb[0], A->Xb[1], A->Xb[2], A->Xb[3], A->Xb[4], A->Xb[5],
+                                                     h1, h2, (long long)A->N, A->h_adj);
+}
+
 struct Ops : lsh::RevolveOps {
     lsh_adjoint* A;
     int status = 0;
@@ -463,11 +491,6 @@ int Ops::reverse_step(int n) {
     const size_t N = A->N;
     const unsigned nb = cell_blocks(A);
     const int G = A->grid;
-    // misfit term of X_{n+1}
-    if (A->have_target && A->ng > 0)
-        k_adj_gauges<<<(A->ng + 127) / 128, 128, 0, s>>>(A->Xb[0], A->Xb[3], A->d_gauges, A->ng,
-                                                         A->d_eta + (size_t)n * A->ng, A->d_tgt + (size_t)n * A->ng,
-                                                         A->misfit_weight);
     // recompute step n's intermediates
     k_set_dt<<<1, 1, 0, s>>>(A->tm, A->d_dts + n);
     double* const* X = A->X;
@@ -480,14 +503,11 @@ int Ops::reverse_step(int n) {
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
         Y7[6] = A->X[6];
         const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
-        k_recon<<<nb, kCellBlock, 0, s>>>(a1);
-        k_adj_tape<<<G, kAdjCellBlock, 0, s>>>(P7{{X[0], X[1], X[2], X[3], X[4], X[5], X[6]}}, A->p.nx, A->p.ny, A->tape1);
+        k_recon_tape<<<nb, kCellBlock, 0, s>>>(a1, A->tape1);
         fwd_passes<2>(A, a1, A->snap1, A->acc1, s);
         k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
         const KArgs a2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
-        k_recon<<<nb, kCellBlock, 0, s>>>(a2);
-        k_adj_tape<<<G, kAdjCellBlock, 0, s>>>(P7{{Y7[0], Y7[1], Y7[2], Y7[3], Y7[4], Y7[5], Y7[6]}}, A->p.nx, A->p.ny,
-                                               A->tape2);
+        k_recon_tape<<<nb, kCellBlock, 0, s>>>(a2, A->tape2);
         fwd_passes<2>(A, a2, A->snap2, A->acc2, s);
     }
     // the stage-1 rate's arg-max and the adjoint of the rate
@@ -510,8 +530,9 @@ int Ops::reverse_step(int n) {
         AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
         rev_stage<2, 1>(A, a1, A->snap1, A->rsel, 5, s);
     }
-    k_adj_reduce<<<1, 32, 0, s>>>(A->part, (A->order == 1 ? 5 : 10) * G, A->red);
+    k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part, (A->order == 1 ? 5 : 10) * G, A->red);
     for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
+    if (n >= 1) misfit_and_project(A, n, A->X[0], A->X[3], s);
     A->stats.reversed_steps += 1;
     A_CUDA(cudaGetLastError());
     return 0;
@@ -549,13 +570,20 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     cudaDeviceGetAttribute(&A->sms, cudaDevAttrMultiProcessorCount, A->device);
     A->grid = 2 * A->sms;
     { cudaError_t e = cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking); if (e != cudaSuccess) return bail(afail(e, "cudaStreamCreate")); }
-    // working arrays: X 7, Y 6, s1/s2 28, acc 14, snaps 12, Xb/Xbn/Yb 18, sxb/syb/accb 21, eta dummy 1
-    const int narr = 7 + 6 + 28 + 14 + 12 + 18 + 21 + 1;
+    // working arrays: X 7, Y 6, s1/s2 28, acc 14, snaps 12, Xb/Xbn/Yb 18, sxb/syb/accb 21, eta dummy 1, hN 2
+    const int narr = 7 + 6 + 28 + 14 + 12 + 18 + 21 + 1 + 2;
     const size_t geo_n = 7 * size_t(params->ny + 1);
     const size_t bytes = (size_t(narr) * A->npad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) +
                          2 * A->npad * sizeof(unsigned);
     { cudaError_t e = cudaMalloc(&A->slab, bytes); if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint work arrays")); }
-    cudaMemsetAsync(A->slab, 0, bytes, A->stream);
+    {
+        // zero the work arrays and wait: the geometry and gauge copies below go
+        // through the legacy default stream, which does not order against
+        // this non-blocking stream
+        cudaError_t e = cudaMemsetAsync(A->slab, 0, bytes, A->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(A->stream);
+        if (e != cudaSuccess) return bail(afail(e, "zeroing the adjoint work arrays"));
+    }
     double* cur = static_cast<double*>(A->slab);
     auto take = [&](double*& p) { p = cur; cur += A->npad; };
     for (int k = 0; k < 7; ++k) take(A->X[k]);
@@ -566,6 +594,8 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     for (int k = 0; k < 6; ++k) { take(A->Xb[k]); take(A->Xbn[k]); take(A->Yb[k]); }
     for (int k = 0; k < 7; ++k) { take(A->sxb[k]); take(A->syb[k]); take(A->accb[k]); }
     take(A->eta_dummy);
+    take(A->hN[0]);
+    take(A->hN[1]);
     A->geo_buf = cur;
     cur += (geo_n + 31) & ~size_t(31);
     A->tape1 = reinterpret_cast<unsigned*>(cur);
@@ -612,6 +642,12 @@ int lsh_adjoint_destroy(lsh_adjoint* A) {
     if (A->stream) cudaStreamDestroy(A->stream);
     (void)cudaGetLastError();
     delete A;
+    return LSH_OK;
+}
+
+int lsh_adjoint_set_thin_layer(lsh_adjoint* A, double h_adj) {
+    if (!A || !(h_adj >= 0.0)) return LSH_ERR_INVALID;
+    A->h_adj = h_adj;
     return LSH_OK;
 }
 
@@ -674,6 +710,8 @@ int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS
         k_cell_dt<<<cell_blocks(A), kCellBlock, 0, s>>>(a);
         k_init_finish<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
         k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts);
+        A_CUDA(cudaGetLastError());
+        A_CUDA(cudaStreamSynchronize(s));
     }
     Ops ops(A);
     A->stats = lsh_adjoint_stats{};
@@ -697,6 +735,7 @@ int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS
     while (nsteps - a > 1 && free > 0) {
         const int m = a + (int)lsh::revolve_split(nsteps - a, free + 1);
         run(a, m);
+        A_CUDA(cudaGetLastError());
         ++slot;
         if (int st = ops.store(slot)) return st;
         A->spine.push_back(m);
@@ -704,6 +743,8 @@ int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS
         --free;
     }
     run(a, nsteps);
+    A_CUDA(cudaMemcpyAsync(A->hN[0], A->X[0], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    A_CUDA(cudaMemcpyAsync(A->hN[1], A->X[3], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     A_CUDA(cudaGetLastError());
     A->h_dts.resize(nsteps + 1);
     A_CUDA(cudaMemcpyAsync(A->h_dts.data(), A->d_dts, sizeof(double) * (nsteps + 1), cudaMemcpyDeviceToHost, s));
@@ -735,6 +776,7 @@ int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* con
         else A_CUDA(cudaMemsetAsync(A->Xb[k], 0, N * sizeof(double), s));
     }
     A_CUDA(cudaMemsetAsync(A->red, 0, sizeof(double) * kRed, s));
+    misfit_and_project(A, A->nsteps, A->hN[0], A->hN[1], s);
     Ops ops(A);
     ops.cur = A->cur_step;
     A->stats.recompute_steps = 0;
@@ -761,7 +803,8 @@ int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* con
         AdjArgs aa = adj_args(A, A->X, nullptr, nullptr, nullptr, A->Xb, nullptr, nullptr, nullptr, A->h_dts[0]);
         double* part = A->part + (size_t)10 * A->grid * kRed;
         k_adj_init<<<1, 32, 0, s>>>(aa, A->rsel, part);
-        k_adj_reduce<<<1, 32, 0, s>>>(part, 1, A->red);
+        k_adj_reduce<<<1, 32 * kRed, 0, s>>>(part, 1, A->red);
+        misfit_and_project(A, 0, A->X[0], A->X[3], s);
     }
     A_CUDA(cudaGetLastError());
     for (int k = 0; k < 6; ++k)
@@ -776,6 +819,25 @@ int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* con
     if (grad_params) for (int k = 0; k < 4; ++k) grad_params[k] = gp[k];
     A->cur_step = ops.cur;
     A->stats.ms_gradient = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return LSH_OK;
+}
+
+int lsh_adjoint_get_times(lsh_adjoint* A, double* t_out) {
+    if (!A || !t_out || !A->have_forward) return LSH_ERR_INVALID;
+    double t = 0.0;
+    for (int n = 0; n < A->nsteps; ++n) {
+        t += A->h_dts[n];
+        t_out[n] = t;
+    }
+    return LSH_OK;
+}
+
+int lsh_adjoint_get_state(lsh_adjoint* A, double* const host_state[6]) {
+    if (!A || !host_state || A->cur_step != A->nsteps) return LSH_ERR_INVALID;
+    for (int k = 0; k < 6; ++k)
+        if (host_state[k])
+            A_CUDA(cudaMemcpyAsync(host_state[k], A->X[k], A->N * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
+    A_CUDA(cudaStreamSynchronize(A->stream));
     return LSH_OK;
 }
 

@@ -1097,6 +1097,14 @@ LSH_HD void edge_adj_body(const AdjArgs& a, int x, int y, double& dtb, ConstBar&
         else { id0 = y * nx + x - 1; id1 = id0 + 1; side0 = 1; }
     }
     e.interior = (id1 >= 0);
+    // the adjoint is linear in the output adjoints: none, nothing to do
+    {
+        bool zero = true;
+        for (int k = 0; k < 7; ++k) zero = zero && is_zero(a.accb[k][id0]);
+        if (e.interior)
+            for (int k = 0; k < 7; ++k) zero = zero && is_zero(a.accb[k][id1]);
+        if (zero) return;
+    }
     const int side1 = (DIR == 0) ? 2 : 0;
     // the forward's face construction (same helpers, host or device)
     KArgs f;
@@ -1248,7 +1256,7 @@ LSH_HD void volume_adj_body(const AdjArgs& a, int id, double& dtb, ConstBar& cb)
 // Branch tape of one cell's reconstruction (recon_cell): for variable k and
 // direction d (0 x, 1 y) bits 2 (7 d + k) .. +1 hold the minmod choice (0
 // zero, 1 the backward difference, 2 the forward one); bit 28: slopes zeroed
-// (negative reconstructed depth, a boundary line, or the dry shortcut).
+// (a reconstructed depth below kReconThin of the cell's, or the dry shortcut).
 LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) {
     const int j = id / nx, i = id - j * nx;
     {
@@ -1283,9 +1291,37 @@ LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) 
     const double h1 = W[0][id], h2 = W[3][id];
     const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
     const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
-    const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
-                     (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
+    const double g1 = kReconThin * h1, g2 = kReconThin * h2;
+    const bool bad = (h1 + dh1x < g1) || (h1 - dh1x < g1) || (h2 + dh2x < g2) || (h2 - dh2x < g2) ||
+                     (h1 + dh1y < g1) || (h1 - dh1y < g1) || (h2 + dh2y < g2) || (h2 - dh2y < g2);
     if (bad) return 1u << 28;
+    return t;
+}
+
+// The reconstruction of recon_cell (lsh_passes.cuh) writing its slopes and
+// returning the branch tape of recon_tape_cell in one pass: the same
+// operations, so the slopes are bit-identical to recon_cell's.
+LSH_HD unsigned recon_cell_tape(const KArgs& a, int id) {
+    const unsigned t = recon_tape_cell(a.W, a.c.nx, a.c.ny, id);
+    const int nx = a.c.nx, ny = a.c.ny;
+    const int j = id / nx, i = id - j * nx;
+    if (t & (1u << 28)) {
+        for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
+        return t;
+    }
+    auto rv = [&](int q, int k) -> double {
+        if (k == 0) return (a.W[0][q] + a.W[3][q]) - a.W[6][q];
+        if (k == 3) return a.W[3][q] - a.W[6][q];
+        return a.W[k][q];
+    };
+    for (int k = 0; k < 7; ++k) {
+        const double pc = rv(id, k);
+        const unsigned cx = (t >> (2 * k)) & 3u, cy = (t >> (2 * (7 + k))) & 3u;
+        // choice 1: the backward difference pc - back; 2: the forward one fwd - pc
+        a.sxw[k][id] = (cx == 0u) ? 0.0 : 0.5 * ((cx == 1u) ? pc - rv(id - 1, k) : rv(id + 1, k) - pc);
+        a.syw[k][id] = (cy == 0u) ? 0.0 : 0.5 * ((cy == 1u) ? pc - rv(id - nx, k) : rv(id + nx, k) - pc);
+    }
+    (void)ny; (void)i; (void)j;
     return t;
 }
 

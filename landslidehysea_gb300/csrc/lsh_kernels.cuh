@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
 }
 
 // Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
-// with a first-order fallback where a reconstructed depth would be negative.
+// with a first-order fallback where a reconstructed depth would fall below
+// kReconThin of the cell depth.
 __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
     if (a.tm->done) return;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;

@@ -15,6 +15,7 @@ namespace lsh {
 constexpr unsigned long long kRateInitBits = 0ULL;  // +0.0
 constexpr int kEdgeBlock = 128;
 constexpr int kCellBlock = 256;
+constexpr double kReconThin = 0.5;  // second order: least face depth / cell depth
 
 // Sticky error bit: an atomic OR on the device, a plain OR in host code.
 LSH_HD void err_or(int* word, int bit) {
@@ -237,8 +238,12 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
     const double h1 = a.W[0][id], h2 = a.W[3][id];
     const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
     const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
-    const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
-                     (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
+    // first order where a reconstructed depth would fall below kReconThin of
+    // the cell's: a thin face with a finite discharge has an unbounded
+    // velocity, whose wave speed would collapse dt
+    const double g1 = kReconThin * h1, g2 = kReconThin * h2;
+    const bool bad = (h1 + dh1x < g1) || (h1 - dh1x < g1) || (h2 + dh2x < g2) || (h2 - dh2x < g2) ||
+                     (h1 + dh1y < g1) || (h1 - dh1y < g1) || (h2 + dh2y < g2) || (h2 - dh2y < g2);
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
         a.sxw[k][id] = bad ? 0.0 : sx[k];

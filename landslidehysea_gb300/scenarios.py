@@ -112,7 +112,10 @@ def fjord(n=2048, seed=0, dcell_deg=0.0002, lat_c=60.0, lon_c=10.0, r=0.48, angl
     the north edge, centreline x_c(y) = A sin(2 pi y / lam + phi) with seeded
     A, lam, phi, walls sloping at wall_deg up to land at +land metres.  The
     slide is a seeded elliptic cap of `volume` m^3 on one wall at half the
-    axis depth; 16 gauges sit on the channel axis."""
+    axis depth (footprint 1 - 1.2 km by 0.5 - 0.7 km, shrunk to 1/20 of a
+    small domain; thickness at most 0.9 of the local depth, so the slide
+    starts submerged; meta["volume"] is what it holds); 16 gauges sit on the
+    channel axis."""
     rng = np.random.default_rng(seed)
     nx = ny = n
     d2r = math.pi / 180.0
@@ -139,16 +142,21 @@ def fjord(n=2048, seed=0, dcell_deg=0.0002, lat_c=60.0, lon_c=10.0, r=0.48, angl
     side = 1.0 if rng.uniform() < 0.5 else -1.0
     sw = half + 0.5 * daxis[js] / slope
     xs, ys = xc[js] + side * sw, ym[js]
-    a_len = rng.uniform(500.0, 700.0) * (n / 2048.0 if n < 2048 else 1.0)
-    b_wid = rng.uniform(250.0, 350.0) * (n / 2048.0 if n < 2048 else 1.0)
-    a_len = max(a_len, 3.0 * EARTH_RADIUS * dcell_deg * d2r)
-    b_wid = max(b_wid, 3.0 * EARTH_RADIUS * math.cos(lat_c * d2r) * dcell_deg * d2r)
+    a_len = rng.uniform(500.0, 700.0)
+    b_wid = rng.uniform(250.0, 350.0)
+    # a footprint within 1/20 of a small domain, but at least 3 cells
+    a_len = max(min(a_len, (ym[-1] - ym[0]) / 20.0), 3.0 * EARTH_RADIUS * dcell_deg * d2r)
+    b_wid = max(min(b_wid, (xm[-1] - xm[0]) / 20.0), 3.0 * EARTH_RADIUS * math.cos(lat_c * d2r) * dcell_deg * d2r)
     shape = np.maximum(0.0, 1.0 - ((xm[None, :] - xs) / b_wid) ** 2 - ((ym[:, None] - ys) / a_len) ** 2)
     # exact spherical cell areas
     lat_e = lat0 + np.arange(ny + 1) * dcell_deg
     area_row = EARTH_RADIUS ** 2 * (dcell_deg * d2r) * (np.sin(lat_e[1:] * d2r) - np.sin(lat_e[:-1] * d2r))
     vol_unit = float((shape * area_row[:, None]).sum())
     thick = volume / vol_unit if vol_unit > 0 else 0.0
+    # a submerged slide: at most 0.9 of the water depth where it is centred
+    # (half the axis depth); a thinner cap carries less than `volume`
+    thick = min(thick, 0.9 * 0.5 * daxis[js])
+    volume = thick * vol_unit
     h2 = thick * shape
     h1 = np.maximum(depth - h2, 0.0)
     h2 = np.where(depth > -land, h2, 0.0)

@@ -66,9 +66,12 @@ SIGNATURES = {
     "lsh_adjoint_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(P)]),
     "lsh_adjoint_destroy": (ctypes.c_int, [P]),
     "lsh_adjoint_set_budget": (ctypes.c_int, [P, ctypes.c_double]),
+    "lsh_adjoint_set_thin_layer": (ctypes.c_int, [P, ctypes.c_double]),
     "lsh_adjoint_forward": (ctypes.c_int, [P, P, ctypes.c_int, P, DP, P]),
     "lsh_adjoint_gradient": (ctypes.c_int, [P, ctypes.c_double, P, P, P]),
     "lsh_adjoint_get_stats": (ctypes.c_int, [P, P]),
+    "lsh_adjoint_get_times": (ctypes.c_int, [P, DP]),
+    "lsh_adjoint_get_state": (ctypes.c_int, [P, P]),
     "lsh_revolve_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -345,6 +348,10 @@ class Adjoint:
     def __exit__(self, *exc):
         self.close()
 
+    def set_thin_layer(self, h_adj):
+        """Thin-layer projection threshold (0: the exact adjoint)."""
+        _check(self.lib.lsh_adjoint_set_thin_layer(self._a, float(h_adj)), "lsh_adjoint_set_thin_layer")
+
     def set_budget(self, nbytes):
         _check(self.lib.lsh_adjoint_set_budget(self._a, float(nbytes)), "lsh_adjoint_set_budget")
 
@@ -380,6 +387,20 @@ class Adjoint:
                                              _ptr_array([out[v].ctypes.data for v in VARS[:6]]), gp.ctypes.data),
                "lsh_adjoint_gradient")
         return out, dict(zip(PARAM_NAMES, gp.tolist()))
+
+    def times(self):
+        """Simulated time after each step of the recorded run."""
+        t = np.zeros(self.nsteps)
+        _check(self.lib.lsh_adjoint_get_times(self._a, t.ctypes.data_as(DP)), "lsh_adjoint_get_times")
+        return t
+
+    def final_state(self):
+        """X_N of the recorded run (after forward, before gradient)."""
+        p = self.params
+        out = {v: np.zeros((p.ny, p.nx)) for v in VARS[:6]}
+        _check(self.lib.lsh_adjoint_get_state(self._a, _ptr_array([out[v].ctypes.data for v in VARS[:6]])),
+               "lsh_adjoint_get_state")
+        return out
 
     def stats(self):
         st = AdjointStats()

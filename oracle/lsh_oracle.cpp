@@ -54,6 +54,7 @@ constexpr double kEps = 1.1920928955078125e-07;  // FLT_EPSILON, Constantes.hxx:
 constexpr double kSqrt2 = 1.41421356237309504880;
 constexpr double kBig = 1e30;                       // "no limit" dt, Volumen_kernel.cu:226,256
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kReconThin = 0.5;               // second order: least face depth / cell depth
 
 using std::fabs;
 using std::sqrt;
@@ -686,7 +687,8 @@ struct Solver {
     }
 
     // minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H), halved, with a
-    // first-order fallback for any cell whose reconstructed depths go negative.
+    // first-order fallback for any cell where a reconstructed depth would fall
+    // below kReconThin times the cell's.
     void reconstruct(const T* const* W) {
         const int NX = nx, NY = ny;
 #pragma omp parallel for schedule(static)
@@ -710,8 +712,12 @@ struct Solver {
                 const T h1 = W[0][id], h2 = W[3][id];
                 const T dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
                 const T dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
-                const bool bad = (h1 + dh1x < 0.0) || (h1 - dh1x < 0.0) || (h2 + dh2x < 0.0) || (h2 - dh2x < 0.0) ||
-                                 (h1 + dh1y < 0.0) || (h1 - dh1y < 0.0) || (h2 + dh2y < 0.0) || (h2 - dh2y < 0.0);
+                // first order where a reconstructed depth would fall below half
+                // the cell's (a thin face with a finite discharge has an unbounded
+                // velocity, and its wave speed collapses dt)
+                const T g1 = kReconThin * h1, g2 = kReconThin * h2;
+                const bool bad = (h1 + dh1x < g1) || (h1 - dh1x < g1) || (h2 + dh2x < g2) || (h2 - dh2x < g2) ||
+                                 (h1 + dh1y < g1) || (h1 - dh1y < g1) || (h2 + dh2y < g2) || (h2 - dh2y < g2);
                 for (int k = 0; k < 7; ++k) {
                     slope_x[k][id] = bad ? T(0.0) : sx[k];
                     slope_y[k][id] = bad ? T(0.0) : sy[k];
@@ -877,11 +883,23 @@ struct Solver {
 // state-dependent CFL step, differentiated through the argmax cell).  The
 // time loop is orc_run's.  eta (nsteps * ng, may be NULL) gets the gauge
 // series; a NULL target means J = 0.
+// Thin-layer projection of the tangent (h_adj > 0): a layer thinner than
+// h_adj is passive in the linearisation, its (h, qx, qy) tangents set to 0.
+// Values are untouched, so the forward is unchanged.
+inline void thin_layer_projection(double* const*, size_t, double) {}
+inline void thin_layer_projection(Dual* const* W, size_t N, double h_adj) {
+    if (!(h_adj > 0.0)) return;
+    for (size_t i = 0; i < N; ++i)
+        for (int l = 0; l < 2; ++l)
+            if (W[3 * l][i].v < h_adj) { W[3 * l][i].d = 0.0; W[3 * l + 1][i].d = 0.0; W[3 * l + 2][i].d = 0.0; }
+}
+
 template <class T>
 int run_misfit(const lsh_params& p, const ConstsT<T>& c, T* const* W, long long nsteps, bool initial, T& dt,
-               int ng, const int* gauges, const double* target, T& J, double* eta) {
+               int ng, const int* gauges, const double* target, T& J, double* eta, double h_adj = 0.0) {
     Solver<T> S(p, c);
     const size_t N = S.N;
+    thin_layer_projection(W, N, h_adj);
     std::vector<T> tmp[6], tmp2[6];
     T* Wn[7];
     T* W2[7];
@@ -905,6 +923,7 @@ int run_misfit(const lsh_params& p, const ConstsT<T>& c, T* const* W, long long 
                 for (size_t id = 0; id < N; ++id) W[k][id] = 0.5 * (W[k][id] + W2[k][id]);
         }
         dt = dtn;
+        thin_layer_projection(W, N, h_adj);
         for (int gi = 0; gi < ng; ++gi) {
             const size_t id = size_t(gauges[gi]);
             const T e = (W[0][id] + W[3][id]) - W[6][id];
@@ -1008,10 +1027,11 @@ int orc_misfit_run(const lsh_params* p, double* const* W, long long nsteps, int 
 // Tangent-linear model of orc_misfit_run: dW[6] (tangents of h1..q2y, in and
 // out), dpar[4] the tangents of (angle1, mf0, mfs, r), *ddt_io the tangent of
 // dt (in and out; ignored on entry when initial != 0).  Values of W, dt and
-// J are bit-identical to orc_misfit_run's; *dJ is the directional derivative.
+// J are bit-identical to orc_misfit_run's; *dJ is the directional derivative
+// (h_adj > 0: of the thin-layer-projected linearisation, run_misfit).
 int orc_tl_run(const lsh_params* p, double* const* W, double* const* dW, const double* dpar, long long nsteps,
                int initial, double* dt_io, double* ddt_io, int ng, const int* gauges, const double* target,
-               double* J, double* dJ, double* eta) {
+               double* J, double* dJ, double* eta, double h_adj) {
     if (int s = check_params(p)) return s;
     using orc::Dual;
     const size_t N = size_t(p->nx) * p->ny;
@@ -1028,7 +1048,7 @@ int orc_tl_run(const lsh_params* p, double* const* W, double* const* dW, const d
         orc::make_consts_t<Dual>(*p, Dual(p->r, dpar[3]), Dual(p->mf0, dpar[1]), Dual(p->mfs, dpar[2]), tan1);
     Dual dt(*dt_io, initial ? 0.0 : *ddt_io);
     Dual Jd;
-    const int s = orc::run_misfit<Dual>(*p, c, Wd, nsteps, initial != 0, dt, ng, gauges, target, Jd, eta);
+    const int s = orc::run_misfit<Dual>(*p, c, Wd, nsteps, initial != 0, dt, ng, gauges, target, Jd, eta, h_adj);
     for (int k = 0; k < 6; ++k)
         for (size_t i = 0; i < N; ++i) {
             W[k][i] = st[k][i].v;

@@ -51,7 +51,8 @@ def lib():
         _lib.orc_fpmath.argtypes = [ctypes.c_int, P, P, ctypes.c_longlong]
         D = ctypes.POINTER(ctypes.c_double)
         _lib.orc_misfit_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, D, ctypes.c_int, P, P, D, P]
-        _lib.orc_tl_run.argtypes = [P, P, P, P, ctypes.c_longlong, ctypes.c_int, D, D, ctypes.c_int, P, P, D, D, P]
+        _lib.orc_tl_run.argtypes = [P, P, P, P, ctypes.c_longlong, ctypes.c_int, D, D, ctypes.c_int, P, P, D, D, P,
+                                    ctypes.c_double]
     return _lib
 
 
@@ -168,10 +169,11 @@ def misfit_run(params, arrs, nsteps, dt=None, gauges=None, target=None):
     return J.value, d.value, eta
 
 
-def tl_run(params, arrs, darrs, dpar, nsteps, dt=None, ddt=0.0, gauges=None, target=None):
+def tl_run(params, arrs, darrs, dpar, nsteps, dt=None, ddt=0.0, gauges=None, target=None, h_adj=0.0):
     """Tangent-linear run (oracle on dual numbers).  darrs: 6 tangent arrays
     (h1..q2y, None = 0), advanced in place with `arrs`; dpar: tangents of
-    (angle1, mf0, mfs, r).  Returns (J, dJ, dt_next, ddt_next)."""
+    (angle1, mf0, mfs, r); h_adj > 0: tangents of layers thinner than h_adj
+    are zeroed after every step.  Returns (J, dJ, dt_next, ddt_next)."""
     g, t = _gauge_args(gauges, target, nsteps)
     N = arrs[0].size
     dd = [np.zeros(N) if a is None else a for a in darrs]
@@ -184,7 +186,8 @@ def tl_run(params, arrs, darrs, dpar, nsteps, dt=None, ddt=0.0, gauges=None, tar
     dJ = ctypes.c_double()
     st = lib().orc_tl_run(ctypes.byref(params), _ptrs(arrs), _ptrs(dd), dp.ctypes.data, int(nsteps), int(dt is None),
                           ctypes.byref(d), ctypes.byref(dd_t), len(g), g.ctypes.data if len(g) else None,
-                          t.ctypes.data if t is not None else None, ctypes.byref(J), ctypes.byref(dJ), None)
+                          t.ctypes.data if t is not None else None, ctypes.byref(J), ctypes.byref(dJ), None,
+                          float(h_adj))
     if st:
         raise RuntimeError(f"orc_tl_run: status {st}")
     for a, b in zip(darrs, dd):

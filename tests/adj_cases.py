@@ -95,7 +95,9 @@ def native_lib(name):
         lib.adjl_set_component.argtypes = [ctypes.c_int]
         lib.adjl_set_bor.argtypes = [ctypes.c_double]
     elif name == "adj_host":
-        lib.adjh_run.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P, D, P, P]
+        lib.adjh_run.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P, D, P, P, ctypes.c_double]
+        lib.adjh_recon_check.restype = ctypes.c_longlong
+        lib.adjh_recon_check.argtypes = [P, P]
     _libs[name] = lib
     return lib
 
@@ -104,7 +106,7 @@ def _ptrs(arrs):
     return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data if a is not None else None for a in arrs])
 
 
-def host_adjoint(p, arrs, nsteps, gauges, target, wj=1.0, wfin=None):
+def host_adjoint(p, arrs, nsteps, gauges, target, wj=1.0, wfin=None, h_adj=0.0):
     """Gradient of wj * J + <wfin, X_N> by the host emulation of the adjoint
     sweep (the product's per-edge / per-cell adjoint bodies in loops).
     Returns (J, grad[6], grad_params[4] = d/d(angle1, mf0, mfs, r))."""
@@ -116,7 +118,8 @@ def host_adjoint(p, arrs, nsteps, gauges, target, wj=1.0, wfin=None):
     g = np.ascontiguousarray(gauges, dtype=np.int32)
     t = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
     lib.adjh_run(ctypes.byref(p), _ptrs(arrs), int(nsteps), len(g), g.ctypes.data, t.ctypes.data if t is not None else None,
-                 float(wj), _ptrs(wfin) if wfin is not None else None, ctypes.byref(J), _ptrs(grad), gpar.ctypes.data)
+                 float(wj), _ptrs(wfin) if wfin is not None else None, ctypes.byref(J), _ptrs(grad), gpar.ctypes.data,
+                 float(h_adj))
     return J.value, grad, gpar
 
 

@@ -131,7 +131,7 @@ extern "C" {
 // state (unchanged).  Outputs: J (the misfit alone), grad (6 arrays: the
 // gradient with respect to the initial h1..q2y), gpar (angle1, mf0, mfs, r).
 int adjh_run(const lsh_params* p, const double* const* W0, int nsteps, int ng, const int* gauges, const double* target,
-             double wj, const double* const* wfin, double* J, double* const* grad, double* gpar) {
+             double wj, const double* const* wfin, double* J, double* const* grad, double* gpar, double h_adj) {
     Host h(*p);
     const size_t N = h.N;
     std::vector<Vec> X(size_t(nsteps + 1) * 7);
@@ -194,19 +194,24 @@ int adjh_run(const lsh_params* p, const double* const* W0, int nsteps, int ng, c
     for (int k = 0; k < 6; ++k) { Xb[k].assign(N, 0.0); if (wfin && wfin[k]) Xb[k].assign(wfin[k], wfin[k] + N); }
     ConstBar cb;
     cb_zero(cb);
-    double dtb_next = 0.0;  // adjoint of dt_{n+1}
-    for (int n = nsteps - 1; n >= 0; --n) {
-        // misfit term at X_{n+1}
-        if (target && wj != 0.0) {
-            const double* Xn1[7];
-            for (int k = 0; k < 7; ++k) Xn1[k] = Xs(n + 1, k).data();
+    // the misfit's adjoint at X_m (m >= 1), then the thin-layer projection of X_m
+    auto misfit_and_project = [&](int m) {
+        if (target && wj != 0.0 && m >= 1) {
             for (int g = 0; g < ng; ++g) {
                 const int id = gauges[g];
-                const double d = eta[size_t(n) * ng + g] - target[size_t(n) * ng + g];
+                const double d = eta[size_t(m - 1) * ng + g] - target[size_t(m - 1) * ng + g];
                 Xb[0][id] += wj * 2.0 * d;
                 Xb[3][id] += wj * 2.0 * d;
             }
         }
+        if (h_adj > 0.0)
+            for (size_t i = 0; i < N; ++i)
+                for (int l = 0; l < 2; ++l)
+                    if (Xs(m, 3 * l)[i] < h_adj) Xb[3 * l][i] = Xb[3 * l + 1][i] = Xb[3 * l + 2][i] = 0.0;
+    };
+    misfit_and_project(nsteps);
+    double dtb_next = 0.0;  // adjoint of dt_{n+1}
+    for (int n = nsteps - 1; n >= 0; --n) {
         const double dt = dts[n];
         double dtb = 0.0;
         // d dt_{n+1} / d R = -dt_{n+1} / R at the stage-1 argmax cell
@@ -238,6 +243,7 @@ int adjh_run(const lsh_params* p, const double* const* W0, int nsteps, int ng, c
         }
         for (int k = 0; k < 6; ++k) Xb[k].swap(Xbn[k]);
         dtb_next = dtb;
+        if (n >= 1) misfit_and_project(n);
     }
     // dt_0 from the initial pass
     if (S0.argmax >= 0 && dtb_next != 0.0) {
@@ -252,9 +258,40 @@ int adjh_run(const lsh_params* p, const double* const* W0, int nsteps, int ng, c
         for (int k = 0; k < 6; ++k) a.Wbar[k] = Xb[k].data();
         init_wave_adj_cell(a, cell, rb * h.G.inv_area[j], cb);
     }
+    misfit_and_project(0);
     for (int k = 0; k < 6; ++k) std::memcpy(grad[k], Xb[k].data(), N * sizeof(double));
     param_grads(p->angle1, p->mf0, p->mfs, p->r, p->gravity, p->eps_h, p->L, p->H, cb, gpar);
     return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Slopes of recon_cell (the forward) against recon_cell_tape (the adjoint's
+// recomputation): the number of cells where any slope differs in any bit.
+long long adjh_recon_check(const lsh_params* p, const double* const* W) {
+    Host h(*p);
+    const size_t N = h.N;
+    Vec a[14], b[14];
+    for (int k = 0; k < 14; ++k) { a[k].assign(N, -1.0); b[k].assign(N, -2.0); }
+    KArgs ka, kb;
+    std::memset(&ka, 0, sizeof(ka));
+    std::memset(&kb, 0, sizeof(kb));
+    ka.c = kb.c = h.c;
+    for (int k = 0; k < 7; ++k) {
+        ka.W[k] = kb.W[k] = W[k];
+        ka.sxw[k] = a[k].data(); ka.syw[k] = a[7 + k].data();
+        kb.sxw[k] = b[k].data(); kb.syw[k] = b[7 + k].data();
+    }
+    long long bad = 0;
+    for (size_t id = 0; id < N; ++id) {
+        recon_cell(ka, int(id));
+        (void)recon_cell_tape(kb, int(id));
+        for (int k = 0; k < 14; ++k)
+            if (lshm::bits_of(a[k][id]) != lshm::bits_of(b[k][id])) { ++bad; break; }
+    }
+    return bad;
 }
 
 }  // extern "C"

@@ -117,15 +117,15 @@ def test_local_initial_wave_adjoint_vs_fd():
 
 
 # ---------------------------------------------------------------- the whole sweep vs the tangent-linear
-def _dot_check(p, arrs, gauges, n, dirs_list, tol):
+def _dot_check(p, arrs, gauges, n, dirs_list, tol, h_adj=0.0):
     _, _, eta = pyoracle.misfit_run(p, copy_arrs(arrs), n, gauges=gauges)
     tgt = eta + 0.01 * np.random.default_rng(5).standard_normal(eta.shape)
-    J, grad, gpar = host_adjoint(p, copy_arrs(arrs), n, gauges, tgt)
+    J, grad, gpar = host_adjoint(p, copy_arrs(arrs), n, gauges, tgt, h_adj=h_adj)
     Jo, _, _ = pyoracle.misfit_run(p, copy_arrs(arrs), n, gauges=gauges, target=tgt)
     assert J == Jo
     for dirs, dpar in dirs_list:
         dd = [None if x is None else x.copy() for x in dirs]
-        _, dJ, _, _ = pyoracle.tl_run(p, copy_arrs(arrs), dd, dpar, n, gauges=gauges, target=tgt)
+        _, dJ, _, _ = pyoracle.tl_run(p, copy_arrs(arrs), dd, dpar, n, gauges=gauges, target=tgt, h_adj=h_adj)
         ad = sum(float(np.dot(grad[k], dirs[k])) for k in range(6) if dirs[k] is not None) + float(np.dot(gpar, dpar))
         assert abs(ad - dJ) <= tol * max(abs(dJ), 1e-300), (dpar, dJ, ad)
 
@@ -144,3 +144,27 @@ def test_host_adjoint_equals_tangent_linear_scenarios(kind, order):
     dl = [(wet_direction(arrs, w, 7), [0, 0, 0, 0]) for w in ((3,), (0,), (1, 2), (4, 5))]
     dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
     _dot_check(p, arrs, gauges, 5, dl, 1e-11)
+
+
+@pytest.mark.parametrize("kind", ["shelf", "fjord", "smooth"])
+def test_fused_reconstruction_slopes_are_the_forwards(kind):
+    """The adjoint recomputation's reconstruction (slopes + branch tape in one
+    pass) writes the forward's slopes bit for bit."""
+    from adj_cases import _ptrs
+    if kind == "smooth":
+        p, arrs, _ = smooth_case(order=2)
+    else:
+        p, arrs, _ = scenario_case(kind, 2)
+    lib = native_lib("adj_host")
+    import ctypes
+    assert lib.adjh_recon_check(ctypes.byref(p), _ptrs(arrs)) == 0
+
+
+@pytest.mark.parametrize("kind,order,h_adj", [("shelf", 2, 0.5), ("fjord", 2, 0.05), ("fjord", 2, 5.0)])
+def test_thin_layer_projection_adjoint_is_the_tangent_linears_transpose(kind, order, h_adj):
+    """With the thin-layer projection on, the adjoint is still exactly the
+    transpose of the (equally projected) tangent-linear model."""
+    p, arrs, gauges = scenario_case(kind, order)
+    dl = [(wet_direction(arrs, w, 8), [0, 0, 0, 0]) for w in ((3,), (0,), (1, 2), (4, 5))]
+    dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
+    _dot_check(p, arrs, gauges, 6, dl, 1e-11, h_adj=h_adj)

@@ -21,11 +21,13 @@ def _state(p, arrs):
     return {v: arrs[i].reshape(p.ny, p.nx) for i, v in enumerate(VARS)}
 
 
-def _gpu_grad(p, arrs, gauges, n, tgt, budget=None, weight=1.0, bar_final=None):
+def _gpu_grad(p, arrs, gauges, n, tgt, budget=None, weight=1.0, bar_final=None, h_adj=0.0):
     from landslidehysea_gb300.solver import Adjoint
     with Adjoint(p, gauges) as A:
         if budget is not None:
             A.set_budget(budget)
+        if h_adj:
+            A.set_thin_layer(h_adj)
         J, eta = A.forward(_state(p, arrs), n, tgt)
         g, gp = A.gradient(weight, bar_final)
         st = A.stats()
@@ -193,3 +195,18 @@ def test_gradient_vs_central_finite_differences(gpu_lib):
         am[3][cell] -= h
         fd = (J_of(p, ap) - J_of(p, am)) / (2 * h)
         assert abs(fd - grad[3][cell]) <= 1e-6 * scale, (cell, fd, grad[3][cell])
+
+
+@pytest.mark.parametrize("kind,h_adj", [("fjord", 0.05), ("shelf", 0.5)])
+def test_gpu_thin_layer_projection(gpu_lib, kind, h_adj):
+    p, arrs, gauges = scenario_case(kind, 2)
+    n = 6
+    tgt = _target(p, arrs, gauges, n)
+    _, _, grad, gpar, _ = _gpu_grad(p, arrs, gauges, n, tgt, budget=3 * 6 * 8 * (arrs[0].size + 32) + 1.0,
+                                    h_adj=h_adj)
+    for which, dpar in (((3,), [0, 0, 0, 0]), ((0, 1, 2), [0, 0, 0, 0]), ((), [1, 0, 0, 0]), ((), [0, 0, 0, 1])):
+        d = wet_direction(arrs, which, 4) if which else [None] * 6
+        dd = [None if x is None else x.copy() for x in d]
+        _, dJ, _, _ = pyoracle.tl_run(p, copy_arrs(arrs), dd, dpar, n, gauges=gauges, target=tgt, h_adj=h_adj)
+        ad = sum(float(np.dot(grad[k], d[k])) for k in range(6) if d[k] is not None) + float(np.dot(gpar, dpar))
+        assert abs(ad - dJ) <= 1e-10 * max(abs(dJ), 1e-300), (which, dpar, dJ, ad)
