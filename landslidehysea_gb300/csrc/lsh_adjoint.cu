@@ -47,6 +47,16 @@ namespace {
 
 constexpr int kAdjEdgeBlock = 128;
 constexpr int kAdjCellBlock = 128;
+// Blocks per SM the edge and volume adjoint kernels are compiled for (their
+// register budget), and whether they run as SM-sized persistent grids or
+// with one edge / cell per thread (the hardware then balances the wet
+// region's blocks across SMs).
+#ifndef LSH_ADJ_MINBLOCKS
+#define LSH_ADJ_MINBLOCKS 4
+#endif
+#ifndef LSH_ADJ_PERSISTENT
+#define LSH_ADJ_PERSISTENT 0
+#endif
 constexpr int kRed = 9;        // dt adjoint + the 8 constant adjoints
 constexpr int kPartSlots = 11;  // partial-sum launches per reversed step (2 stages x 5, + initial dt)
 
@@ -85,7 +95,7 @@ struct RateSel {
 };
 
 template <int DIR, bool FIRST, int ORDER>
-__global__ void __launch_bounds__(kAdjEdgeBlock) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
+__global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_MINBLOCKS) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const int nx = a.c.nx, ny = a.c.ny;
@@ -110,7 +120,7 @@ __global__ void __launch_bounds__(kAdjEdgeBlock) k_adj_edges(AdjArgs a, const Ra
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kAdjCellBlock) k_adj_volume(AdjArgs a, const RateSel* rs, double* part) {
+__global__ void __launch_bounds__(kAdjCellBlock, LSH_ADJ_MINBLOCKS) k_adj_volume(AdjArgs a, const RateSel* rs, double* part) {
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const long long N = (long long)a.c.nx * a.c.ny;
@@ -294,7 +304,8 @@ struct lsh_adjoint {
     unsigned long long* rmax = nullptr;  // scratch for the arg-max
     long long* argmax = nullptr;
     RateSel* rsel = nullptr;
-    double* part = nullptr;    // kPartSlots x grid x kRed
+    double* part = nullptr;    // part_rows x kRed partial sums
+    long long part_rows = 0;
     double* red = nullptr;     // kRed
     // checkpoints
     double* slots = nullptr;
@@ -419,25 +430,43 @@ AdjArgs adj_args(const lsh_adjoint* A, const double* const* W, const double* con
     return a;
 }
 
+// Blocks of an adjoint launch over `items` edges or cells.
+int adj_blocks(const lsh_adjoint* A, long long items, int block) {
+    if (LSH_ADJ_PERSISTENT) return A->grid;
+    return (int)std::max(1LL, (items + block - 1) / block);
+}
+
 // Reverse of one stage: volume (MODE), passes last-first, reconstruction.
+// Each launch writes one partial-sum row per block at A->part + *nparts;
+// *nparts advances by the blocks launched.
 template <int ORDER, int MODE>
-void rev_stage(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, int part_slot, cudaStream_t s) {
-    const int G = A->grid;
-    double* part = A->part + (size_t)part_slot * G * kRed;
-    k_adj_volume<MODE><<<G, kAdjCellBlock, 0, s>>>(a, rs, part);
-    part += (size_t)G * kRed;
+void rev_stage(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, long long* nparts, cudaStream_t s) {
+    const int nx = A->p.nx, ny = A->p.ny;
+    const long long N = (long long)A->N;
+    auto edges = [&](int dir, int par) -> long long {
+        const int nl = (dir == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
+        return (long long)nl * ((dir == 0) ? nx : ny);
+    };
+    int g = adj_blocks(A, N, kAdjCellBlock);
+    k_adj_volume<MODE><<<g, kAdjCellBlock, 0, s>>>(a, rs, A->part + *nparts * kRed);
+    *nparts += g;
     a.snap[0] = snaps[2][0]; a.snap[1] = snaps[2][1];
-    k_adj_edges<1, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 1, part);
-    part += (size_t)G * kRed;
+    g = adj_blocks(A, edges(1, 1), kAdjEdgeBlock);
+    k_adj_edges<1, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    *nparts += g;
     a.snap[0] = snaps[1][0]; a.snap[1] = snaps[1][1];
-    k_adj_edges<1, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 0, part);
-    part += (size_t)G * kRed;
+    g = adj_blocks(A, edges(1, 0), kAdjEdgeBlock);
+    k_adj_edges<1, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    *nparts += g;
     a.snap[0] = snaps[0][0]; a.snap[1] = snaps[0][1];
-    k_adj_edges<0, false, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 1, part);
-    part += (size_t)G * kRed;
+    g = adj_blocks(A, edges(0, 1), kAdjEdgeBlock);
+    k_adj_edges<0, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    *nparts += g;
     a.snap[0] = a.snap[1] = nullptr;
-    k_adj_edges<0, true, ORDER><<<G, kAdjEdgeBlock, 0, s>>>(a, rs, 0, part);
-    if (ORDER == 2) k_adj_recon<<<G, kAdjCellBlock, 0, s>>>(a);
+    g = adj_blocks(A, edges(0, 0), kAdjEdgeBlock);
+    k_adj_edges<0, true, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    *nparts += g;
+    if (ORDER == 2) k_adj_recon<<<adj_blocks(A, N, kAdjCellBlock), kAdjCellBlock, 0, s>>>(a);
 }
 
 void zero6(double* const* v, size_t N, cudaStream_t s) {
@@ -517,20 +546,21 @@ int Ops::reverse_step(int n) {
     k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
     k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts + n + 1, A->rsel);
     zero6(A->Xbn, N, s);
+    long long nparts = 0;
     if (A->order == 1) {
         AdjArgs a = adj_args(A, X, nullptr, nullptr, A->acc1, A->Xbn, A->Xb, nullptr, nullptr, dt);
-        rev_stage<1, 0>(A, a, A->snap1, A->rsel, 0, s);
+        rev_stage<1, 0>(A, a, A->snap1, A->rsel, &nparts, s);
     } else {
         double* Y7[7];
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
         Y7[6] = A->X[6];
         zero6(A->Yb, N, s);
         AdjArgs a2 = adj_args(A, Y7, A->s2x, A->s2y, A->acc2, A->Yb, A->Xb, A->Xbn, A->tape2, dt);
-        rev_stage<2, 2>(A, a2, A->snap2, nullptr, 0, s);
+        rev_stage<2, 2>(A, a2, A->snap2, nullptr, &nparts, s);
         AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
-        rev_stage<2, 1>(A, a1, A->snap1, A->rsel, 5, s);
+        rev_stage<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s);
     }
-    k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part, (A->order == 1 ? 5 : 10) * G, A->red);
+    k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part, (int)nparts, A->red);
     for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
     if (n >= 1) misfit_and_project(A, n, A->X[0], A->X[3], s);
     A->stats.reversed_steps += 1;
@@ -615,7 +645,11 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
         if (e == cudaSuccess) e = cudaMalloc(&A->rmax, sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc(&A->argmax, sizeof(long long));
         if (e == cudaSuccess) e = cudaMalloc(&A->rsel, sizeof(RateSel));
-        if (e == cudaSuccess) e = cudaMalloc(&A->part, sizeof(double) * kRed * kPartSlots * A->grid);
+        // partial-sum rows of one reversed step: 2 volume + 8 edge launches (+1 for dt_0)
+        const long long ecap = (N / 2 + params->nx + params->ny + kAdjEdgeBlock) / kAdjEdgeBlock + 1;
+        const long long vcap = (N + kAdjCellBlock - 1) / kAdjCellBlock;
+        A->part_rows = std::max<long long>((long long)kPartSlots * A->grid, 2 * vcap + 8 * ecap + 1);
+        if (e == cudaSuccess) e = cudaMalloc(&A->part, sizeof(double) * kRed * A->part_rows);
         if (e == cudaSuccess) e = cudaMalloc(&A->red, sizeof(double) * kRed);
         if (e == cudaSuccess && n_gauges > 0) e = cudaMalloc(&A->d_gauges, sizeof(int) * n_gauges);
         if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint scalars"));
@@ -801,7 +835,7 @@ int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* con
         k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
         k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts, A->rsel);
         AdjArgs aa = adj_args(A, A->X, nullptr, nullptr, nullptr, A->Xb, nullptr, nullptr, nullptr, A->h_dts[0]);
-        double* part = A->part + (size_t)10 * A->grid * kRed;
+        double* part = A->part;
         k_adj_init<<<1, 32, 0, s>>>(aa, A->rsel, part);
         k_adj_reduce<<<1, 32 * kRed, 0, s>>>(part, 1, A->red);
         misfit_and_project(A, 0, A->X[0], A->X[3], s);
