@@ -244,6 +244,21 @@ __global__ void __launch_bounds__(32 * kRed) k_adj_reduce(const double* part, in
     }
 }
 
+// First level of the partial sums: block b adds rows [b chunk, (b+1) chunk)
+// into row b of out (warp k: component k, lane-strided then a shuffle tree),
+// a fixed order, so the total stays bit-reproducible.
+__global__ void __launch_bounds__(32 * kRed) k_adj_reduce_rows(const double* part, long long nparts, long long chunk,
+                                                               double* out) {
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long r0 = (long long)blockIdx.x * chunk;
+    const long long r1 = (r0 + chunk < nparts) ? r0 + chunk : nparts;
+    double s = 0.0;
+    for (long long i = r0 + lane; i < r1; i += 32) s += part[(size_t)i * kRed + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[(size_t)blockIdx.x * kRed + k] = s;
+}
+
 __global__ void k_set_dt(lsh::TimeRec* tm, const double* dt) {
     tm->dt = *dt;
     tm->rmax_bits = kRateInitBits;
@@ -306,6 +321,7 @@ struct lsh_adjoint {
     RateSel* rsel = nullptr;
     double* part = nullptr;    // part_rows x kRed partial sums
     long long part_rows = 0;
+    double* part2 = nullptr;   // 128 x kRed first-level sums
     double* red = nullptr;     // kRed
     // checkpoints
     double* slots = nullptr;
@@ -560,7 +576,12 @@ int Ops::reverse_step(int n) {
         AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
         rev_stage<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s);
     }
-    k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part, (int)nparts, A->red);
+    {
+        constexpr int kRows = 128;
+        const long long chunk = (nparts + kRows - 1) / kRows;
+        k_adj_reduce_rows<<<kRows, 32 * kRed, 0, s>>>(A->part, nparts, chunk, A->part2);
+        k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part2, kRows, A->red);
+    }
     for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
     if (n >= 1) misfit_and_project(A, n, A->X[0], A->X[3], s);
     A->stats.reversed_steps += 1;
@@ -650,6 +671,7 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
         const long long vcap = (N + kAdjCellBlock - 1) / kAdjCellBlock;
         A->part_rows = std::max<long long>((long long)kPartSlots * A->grid, 2 * vcap + 8 * ecap + 1);
         if (e == cudaSuccess) e = cudaMalloc(&A->part, sizeof(double) * kRed * A->part_rows);
+        if (e == cudaSuccess) e = cudaMalloc(&A->part2, sizeof(double) * kRed * 128);
         if (e == cudaSuccess) e = cudaMalloc(&A->red, sizeof(double) * kRed);
         if (e == cudaSuccess && n_gauges > 0) e = cudaMalloc(&A->d_gauges, sizeof(int) * n_gauges);
         if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint scalars"));
@@ -670,7 +692,7 @@ int lsh_adjoint_destroy(lsh_adjoint* A) {
     if (!A) return LSH_OK;
     if (A->stream) cudaStreamSynchronize(A->stream);
     cudaFree(A->slab);
-    cudaFree(A->tm); cudaFree(A->rmax); cudaFree(A->argmax); cudaFree(A->rsel); cudaFree(A->part); cudaFree(A->red);
+    cudaFree(A->tm); cudaFree(A->rmax); cudaFree(A->argmax); cudaFree(A->rsel); cudaFree(A->part); cudaFree(A->part2); cudaFree(A->red);
     cudaFree(A->d_gauges); cudaFree(A->d_eta); cudaFree(A->d_tgt); cudaFree(A->d_dts);
     cudaFree(A->slots);
     if (A->stream) cudaStreamDestroy(A->stream);
