@@ -36,6 +36,29 @@ sys.path.insert(0, ROOT)
 METRIC = "FP64 cell-updates/s at 2048^2"
 UNIT = "cell-updates/s"
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# FP64 operations per cell-update of the 2048^2 fjord step as the reference
+# scheme performs them (no dry or single-layer shortcuts), counted by running
+# the FP64 oracle on an operation-counting scalar (oracle/count.h); an FMA
+# counts 2, a division, square root, exp or cube root 1.  Comparisons (172
+# per cell-update) are not counted.  tests/test_oracle_opcount.py recomputes it.
+FJORD2048_FLOPS_PER_CELL_STEP = 802.5
+
+
+# DRAM bytes (read + write) per launch of each step kernel on the 2048^2
+# fjord, from one ncu capture (profiles/fjord2048_order2_dram_traffic.md):
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
+#       --clock-control none -k regex:"k_volume|k_edges|k_recon" -s 26 -c 13 \
+#       python bench.py --steps 2 --warmup 1 --no-cpu-baseline --no-e2e
+FJORD2048_DRAM_BYTES_PER_LAUNCH = {
+    "recon": 501.1e6, "edge_h0": 262.6e6, "edge_h1": 394.9e6, "edge_v0": 262.2e6, "edge_v1": 261.5e6,
+    "volume1": 625.9e6, "volume2": 827.7e6,
+}
+
+
+def flops_per_cell_step(ops):
+    """FP64 flops from an operation count by kind (FMA = 2)."""
+    return (ops["add"] + ops["mul"] + 2 * ops["fma"] + ops["div"] + ops["sqrt"] + ops["exp"] + ops["cbrt"]
+            + ops["pow"])
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -65,6 +88,27 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(x, dist, device):
+    """The largest of every rank's x (timings: the job ends with its slowest rank)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Units per second of the whole job: every rank's units over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
+def shard(count, rank, world):
+    """Scenario ids of one rank when an ensemble is split over `world` GPUs:
+    round-robin, so sizes drawn at random balance across ranks."""
+    return list(range(rank, count, world))
 
 
 def init_dist(world, local, backend):
@@ -266,11 +310,8 @@ def run_ours(args):
     launches = s.launch_count() - launches0
     s.synchronize()
     t_sim, dt_next, nsteps = s.time()
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * cells * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = whole_job_rate(world, cells * args.steps, ms * 1e-3)
 
     # per-kernel event timing of a few extra steps (dominant kernel for the roofline)
     prof = [s.profile_step() for _ in range(3)]
@@ -292,8 +333,17 @@ def run_ours(args):
     kernel_of = {"recon": "k_recon", "edge_h0": "k_edges_h<first>", "edge_h1": "k_edges_h", "edge_v0": "k_edges_v",
                  "edge_v1": "k_edges_v", "volume": "k_volume<0>", "volume1": "k_volume<1>", "volume2": "k_volume<2>",
                  "clock": "k_advance"}
+    fp64 = None
+    if fp64_peak and args.n == 2048:
+        ach = FJORD2048_FLOPS_PER_CELL_STEP * value / world / 1e9
+        fp64 = {"bound": "fp64", "achieved": round(ach, 1), "peak": round(fp64_peak, 1), "unit": "GFLOP/s",
+                "frac": round(ach / fp64_peak, 4), "flops_per_cell_step": FJORD2048_FLOPS_PER_CELL_STEP,
+                "what": "the reference scheme's FP64 operations per cell-update (oracle count, FMA = 2) x "
+                        "cell-updates/s, over the measured FP64 FMA peak (lsh_probe_fp64_peak)"}
+    traffic = FJORD2048_DRAM_BYTES_PER_LAUNCH.get(dom_name) if args.n == 2048 else None
     roofline = {"bound": "hbm", "kernel": f"{kernel_of[dom_name]} ({dom_name})", "achieved": round(achieved, 2),
-                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": None,
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": traffic,
+                "algorithmic_bytes": dom_bytes,
                 "peak_kind": f"{peak_kind} hbm_gbs", "step_kernel_ms": {k: round(statistics.mean(v), 4)
                                                                         for k, v in names_ms.items()},
                 "fp64_peak_gflops_measured": round(fp64_peak, 1) if fp64_peak else None,
@@ -315,7 +365,8 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": config_dict(sc, args.n, {"sim_time_s": t_sim, "dt_s": dt_next}),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "fp64_roofline": fp64, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches,
                 "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if dist:
@@ -351,13 +402,10 @@ def measure_e2e(sc, local, args, torch, np, VARS, Solver, dist):
     out = s.get_state()
     el = time.perf_counter() - t0
     s.close()
-    if dist:
-        tt = torch.tensor([el], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        el = float(tt.item())
+    el = max_over_ranks(el, dist, "cuda")
     world = dist.get_world_size() if dist else 1
     state_bytes = 7 * cells * 8
-    return {"value": world * cells * steps / el, "unit": UNIT, "h2d_bytes_per_step": state_bytes / steps,
+    return {"value": whole_job_rate(world, cells * steps, el), "unit": UNIT, "h2d_bytes_per_step": state_bytes / steps,
             "d2h_bytes_per_step": 64 + state_bytes / steps, "seconds": el,
             "what": "lsh_set_state(pinned host) + K x (lsh_step(1) + lsh_get_time) + lsh_get_state"}
 
@@ -368,18 +416,29 @@ def run_ensemble(args):
     slide volume), advanced together by the persistent work-queue kernels of
     lsh_batch (autotuned), against the same scenarios stepped one after the
     other with single-grid contexts (each its own CUDA graph).  Both arms run
-    the same K steps per scenario from the same state."""
+    the same K steps per scenario from the same state.  With N GPUs the
+    scenarios are split round-robin (no collective on the data path), the
+    job's time is the slowest rank's and the work is fixed: strong scaling."""
     import torch
     rank, world, local = dist_env()
-    if rank != 0:
-        return 0
+    dist = init_dist(world, local, "nccl")
     torch.cuda.set_device(local)
     from landslidehysea_gb300 import build as B
-    B.build()
+    if rank == 0 or world == 1:
+        B.build()
+    if dist:
+        dist.barrier()
     from landslidehysea_gb300 import scenarios
     from landslidehysea_gb300.solver import Batch, Solver
-    scs = scenarios.ensemble(args.count)
-    cells = sum(sc.nx * sc.ny for sc in scs)
+    ids = shard(args.count, rank, world)
+    scs = scenarios.ensemble(args.count, ids=ids)
+    all_cells = sum(s_.nx * s_.ny for s_ in scenarios.ensemble(args.count)) if world > 1 else \
+        sum(s_.nx * s_.ny for s_ in scs)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
     b = Batch([sc.params for sc in scs], device=local)
     for k, sc in enumerate(scs):
         b.set_state(k, sc.state)
@@ -390,13 +449,16 @@ def run_ensemble(args):
     launches0 = b.launch_count()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        barrier()
         t0 = time.perf_counter()
         b.step(args.steps)
         b.synchronize()
         el = time.perf_counter() - t0
+        barrier()
     launches = b.launch_count() - launches0
     b.close()
-    value = cells * args.steps / el
+    el = max_over_ranks(el, dist, "cuda")
+    value = all_cells * args.steps / el
 
     # serial: the same scenarios, one context at a time, K steps each after
     # the same number of earlier steps; CUDA events on the solver's stream
@@ -415,21 +477,27 @@ def run_ensemble(args):
             e1.record(stream)
             e1.synchronize()
             serial_ms += e0.elapsed_time(e1)
-    serial = cells * args.steps / (serial_ms * 1e-3)
+    serial_ms = max_over_ranks(serial_ms, dist, "cuda")
+    serial = all_cells * args.steps / (serial_ms * 1e-3)
     sizes = {}
     for sc in scs:
         sizes[sc.nx] = sizes.get(sc.nx, 0) + 1
-    line = {"metric": "FP64 cell-updates/s, batched ensemble", "value": value, "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"ensemble{args.count}_shelf_order2", "scenarios": args.count,
-                       "grids": {str(k): v for k, v in sorted(sizes.items())}, "cells": cells, "order": 2,
-                       "l2": f"inputs larger than L2 (~{cells * 36 * 8 / 1e9:.0f} GB resident)"},
-            "serial": {"value": serial, "ms_per_step": serial_ms / args.steps,
-                       "what": "each scenario alone through lsh_create/lsh_step (16-step CUDA graphs)"},
-            "batched_vs_serial": value / serial, "tune": tune, "gpu_launches": launches,
-            "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        line = {"metric": "FP64 cell-updates/s, batched ensemble", "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+                "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"ensemble{args.count}_shelf_order2", "scenarios": args.count,
+                           "grids_rank0": {str(k): v for k, v in sorted(sizes.items())}, "cells": all_cells,
+                           "order": 2, "split": "round-robin over ranks" if world > 1 else None,
+                           "l2": f"inputs larger than L2 (~{all_cells * 36 * 8 / 1e9 / world:.0f} GB per GPU)"},
+                "serial": {"value": serial, "ms_per_step": serial_ms / args.steps,
+                           "what": "each scenario alone through lsh_create/lsh_step (16-step CUDA graphs)"},
+                "batched_vs_serial": value / serial, "tune": tune, "gpu_launches": launches,
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 

@@ -179,16 +179,21 @@ def fjord(n=2048, seed=0, dcell_deg=0.0002, lat_c=60.0, lon_c=10.0, r=0.48, angl
 ENSEMBLE_SIZES = (128, 256, 512, 768)
 
 
-def ensemble(count=256, seed0=0, sizes=ENSEMBLE_SIZES, order=2, cfl=0.5):
+def ensemble_member(k, seed0=0, sizes=ENSEMBLE_SIZES, order=2, cfl=0.5):
+    """Scenario k of :func:`ensemble`, on its own (ensembles split over GPUs
+    build only their share)."""
+    rng = np.random.default_rng(1_000_003 + seed0 + k)
+    n = int(sizes[int(rng.integers(0, len(sizes)))])
+    ang = float(rng.uniform(8.0, 20.0))
+    rr = float(rng.uniform(0.45, 0.6))
+    vol = float(math.exp(rng.uniform(math.log(1e6), math.log(1e8))))
+    return shelf(n=n, seed=seed0 + k, r=rr, angle_deg=ang, cap_volume=vol, order=order, cfl=cfl)
+
+
+def ensemble(count=256, seed0=0, sizes=ENSEMBLE_SIZES, order=2, cfl=0.5, ids=None):
     """`count` shelf scenarios, scenario k seeded with seed0 + k: size drawn
     uniformly from `sizes`, Coulomb angle ~ U[8, 20] deg, r ~ U[0.45, 0.6],
-    slide volume ~ log-U[1e6, 1e8] m^3 (cap radius scaled to match)."""
-    out = []
-    for k in range(count):
-        rng = np.random.default_rng(1_000_003 + seed0 + k)
-        n = int(sizes[int(rng.integers(0, len(sizes)))])
-        ang = float(rng.uniform(8.0, 20.0))
-        rr = float(rng.uniform(0.45, 0.6))
-        vol = float(math.exp(rng.uniform(math.log(1e6), math.log(1e8))))
-        out.append(shelf(n=n, seed=seed0 + k, r=rr, angle_deg=ang, cap_volume=vol, order=order, cfl=cfl))
-    return out
+    slide volume ~ log-U[1e6, 1e8] m^3 (cap radius scaled to match).  `ids`:
+    only those members."""
+    ks = range(count) if ids is None else ids
+    return [ensemble_member(k, seed0, sizes, order, cfl) for k in ks]

@@ -38,6 +38,7 @@
 #include "../include/lsh.h"
 #include "../landslidehysea_gb300/csrc/lsh_fpmath.h"
 #include "dual.h"
+#include "count.h"
 
 #include <algorithm>
 #include <cmath>
@@ -185,6 +186,19 @@ inline Dual vfac(const Dual& h, const Dual& eps_h) {
 }
 inline Dual pow43(const Dual& h) { return h * cbrt_pos(h); }
 inline int sgn(const Dual& x) { return sgn(x.v); }
+
+// ... and on Cnt (operation counting)
+long long g_cnt[kCntThreads][16];
+inline Cnt tmin(const Cnt& a, const Cnt& b) { return (b < a) ? b : a; }
+inline Cnt tmax(const Cnt& a, const Cnt& b) { return (b > a) ? b : a; }
+inline Cnt max0(const Cnt& a) { return (a > 0.0) ? a : Cnt(0.0); }
+inline Cnt vfac(const Cnt& h, const Cnt& eps_h) {
+    if (h > eps_h) return 1.0 / h;
+    const Cnt h2 = h * h, m2 = eps_h * eps_h;
+    return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
+}
+inline Cnt pow43(const Cnt& h) { return h * cbrt_pos(h); }
+inline int sgn(const Cnt& x) { bump(kCmp); return sgn(x.v); }
 inline double pow_pos(double x, double e) { return lshm::pow_pos(x, e); }
 
 template <class T>
@@ -280,6 +294,7 @@ struct EdgeOut { T m[6], p[6]; T wave; };
 // edges with a single-layer specialisation): no sensitivity to h2 or q2.
 // Values are untouched, so the double oracle is unchanged.
 inline void single_layer_branch(Face<double>&, Face<double>&) {}
+inline void single_layer_branch(Face<Cnt>&, Face<Cnt>&) {}
 inline void single_layer_branch(Face<Dual>& A, Face<Dual>& B) {
     if (A.h2 == 0.0 && B.h2 == 0.0 && A.qn2 == 0.0 && B.qn2 == 0.0) {
         A.h2.d = B.h2.d = A.qn2.d = B.qn2.d = A.qt2.d = B.qt2.d = 0.0;
@@ -887,6 +902,7 @@ struct Solver {
 // h_adj is passive in the linearisation, its (h, qx, qy) tangents set to 0.
 // Values are untouched, so the forward is unchanged.
 inline void thin_layer_projection(double* const*, size_t, double) {}
+inline void thin_layer_projection(Cnt* const*, size_t, double) {}
 inline void thin_layer_projection(Dual* const* W, size_t N, double h_adj) {
     if (!(h_adj > 0.0)) return;
     for (size_t i = 0; i < N; ++i)
@@ -1058,6 +1074,34 @@ int orc_tl_run(const lsh_params* p, double* const* W, double* const* dW, const d
     *ddt_io = dt.d;
     *J = Jd.v;
     *dJ = Jd.d;
+    return s;
+}
+
+// FP64 operations of `nsteps` steps from W as the oracle performs them (the
+// reference scheme's arithmetic; the CUDA kernels skip some of it on dry and
+// single-layer work), by kind: counts[0..9] = add/sub, mul, fma, div, sqrt,
+// exp, cbrt, pow, compare, abs.  The initial-dt pass is included once.
+int orc_count_ops(const lsh_params* p, const double* const* W, long long nsteps, long long* counts) {
+    if (int s = check_params(p)) return s;
+    using orc::Cnt;
+    const size_t N = size_t(p->nx) * p->ny;
+    std::vector<Cnt> st[7];
+    Cnt* Wc[7];
+    for (int k = 0; k < 7; ++k) {
+        st[k].resize(N);
+        for (size_t i = 0; i < N; ++i) st[k][i] = Cnt(W[k][i]);
+        Wc[k] = st[k].data();
+    }
+    std::memset(orc::g_cnt, 0, sizeof(orc::g_cnt));
+    const orc::ConstsT<Cnt> c = orc::make_consts_t<Cnt>(*p, Cnt(p->r), Cnt(p->mf0), Cnt(p->mfs), Cnt(std::tan(p->angle1)));
+    std::memset(orc::g_cnt, 0, sizeof(orc::g_cnt));
+    Cnt dt, J;
+    const int s = orc::run_misfit<Cnt>(*p, c, Wc, nsteps, true, dt, 0, nullptr, nullptr, J, nullptr);
+    for (int k = 0; k < orc::kNumCnt; ++k) {
+        long long t = 0;
+        for (int th = 0; th < orc::kCntThreads; ++th) t += orc::g_cnt[th][k];
+        counts[k] = t;
+    }
     return s;
 }
 

@@ -23,7 +23,7 @@ _ref = None
 
 def build(force=False):
     """Compile the oracle (a second or two)."""
-    srcs = [os.path.join(HERE, "lsh_oracle.cpp"), os.path.join(HERE, "dual.h"),
+    srcs = [os.path.join(HERE, "lsh_oracle.cpp"), os.path.join(HERE, "dual.h"), os.path.join(HERE, "count.h"),
             os.path.join(HERE, "..", "landslidehysea_gb300", "csrc", "lsh_fpmath.h")]
     if force or not os.path.exists(ORACLE_SO) or \
             os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(f) for f in srcs):
@@ -51,6 +51,7 @@ def lib():
         _lib.orc_fpmath.argtypes = [ctypes.c_int, P, P, ctypes.c_longlong]
         D = ctypes.POINTER(ctypes.c_double)
         _lib.orc_misfit_run.argtypes = [P, P, ctypes.c_longlong, ctypes.c_int, D, ctypes.c_int, P, P, D, P]
+        _lib.orc_count_ops.argtypes = [P, P, ctypes.c_longlong, P]
         _lib.orc_tl_run.argtypes = [P, P, P, P, ctypes.c_longlong, ctypes.c_int, D, D, ctypes.c_int, P, P, D, D, P,
                                     ctypes.c_double]
     return _lib
@@ -194,3 +195,26 @@ def tl_run(params, arrs, darrs, dpar, nsteps, dt=None, ddt=0.0, gauges=None, tar
         if a is not None and a is not b:
             a[...] = b
     return J.value, dJ.value, d.value, dd_t.value
+
+
+OP_KINDS = ("add", "mul", "fma", "div", "sqrt", "exp", "cbrt", "pow", "cmp", "abs")
+
+
+def count_ops(params, arrs, nsteps):
+    """FP64 operations of the initial-dt pass and `nsteps` steps from `arrs`
+    as the oracle performs them, by kind (dict)."""
+    counts = np.zeros(16, dtype=np.int64)
+    held = [np.ascontiguousarray(a, dtype=np.float64).copy() for a in arrs]  # alive across the call
+    st = lib().orc_count_ops(ctypes.byref(params), _ptrs(held), int(nsteps), counts.ctypes.data)
+    if st:
+        raise RuntimeError(f"orc_count_ops: status {st}")
+    return dict(zip(OP_KINDS, counts[:len(OP_KINDS)].tolist()))
+
+
+def ops_per_cell_step(params, arrs, steps=(1, 3)):
+    """FP64 operations per cell-update of the step (the initial-dt pass
+    removed by differencing two run lengths)."""
+    a, b = steps
+    ca, cb = count_ops(params, arrs, a), count_ops(params, arrs, b)
+    n = params.nx * params.ny * (b - a)
+    return {k: (cb[k] - ca[k]) / n for k in OP_KINDS}
