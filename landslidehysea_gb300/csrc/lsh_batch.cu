@@ -281,7 +281,6 @@ extern "C" {
 int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** out) {
     if (!out || !params || n < 1) return LSH_ERR_INVALID;
     *out = nullptr;
-    if (lsh_check_device() != 0) return LSH_ERR_NO_DEVICE;
     for (int s = 0; s < n; ++s) {
         if (const char* why = lsh::params_problem(params + s)) {
             lsh::set_last_error("scenario " + std::to_string(s) + ": " + why);
@@ -289,6 +288,7 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
         }
         if (params[s].order != params[0].order) { lsh::set_last_error("all scenarios of a batch must share the order"); return LSH_ERR_INVALID; }
     }
+    if (lsh_check_device() != 0) return LSH_ERR_NO_DEVICE;
     lsh_batch* b = new (std::nothrow) lsh_batch();
     if (!b) return LSH_ERR_HOST_OOM;
     b->n = n;
