@@ -370,14 +370,8 @@ KArgs fwd_args(const lsh_adjoint* A, const double* const* W, double* const* Wout
     return a;
 }
 
-dim3 grid_h(const lsh_adjoint* A, int par) {
-    const int nlines = (A->p.ny - par) / 2 + 1;
-    return dim3((A->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min(nlines, 65535));
-}
-dim3 grid_v(const lsh_adjoint* A, int par) {
-    const int nlines = (A->p.nx - par) / 2 + 1;
-    return dim3((nlines + kEdgeBlock - 1) / kEdgeBlock, std::min(A->p.ny, 65535));
-}
+dim3 grid_h(const lsh_adjoint* A, int par) { return edge_grid_h(A->p.nx, A->p.ny, par); }
+dim3 grid_v(const lsh_adjoint* A, int par) { return edge_grid_v(A->p.nx, A->p.ny, par); }
 unsigned cell_blocks(const lsh_adjoint* A) { return unsigned((A->N + kCellBlock - 1) / kCellBlock); }
 
 // The four colour passes of one stage; snaps (may be null) get acc[0], acc[3]
@@ -385,36 +379,36 @@ unsigned cell_blocks(const lsh_adjoint* A) { return unsigned((A->N + kCellBlock 
 template <int ORDER>
 void fwd_passes(const lsh_adjoint* A, const KArgs& a, double* snaps[3][2], double* const* acc, cudaStream_t s) {
     const size_t bytes = A->N * sizeof(double);
-    k_edges_h<true, ORDER><<<grid_h(A, 0), kEdgeBlock, 0, s>>>(a, 0);
+    k_edges_h<true, ORDER><<<grid_h(A, 0), edge_block_h(), 0, s>>>(a, 0);
     if (snaps) { cudaMemcpyAsync(snaps[0][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[0][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
-    k_edges_h<false, ORDER><<<grid_h(A, 1), kEdgeBlock, 0, s>>>(a, 1);
+    k_edges_h<false, ORDER><<<grid_h(A, 1), edge_block_h(), 0, s>>>(a, 1);
     if (snaps) { cudaMemcpyAsync(snaps[1][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[1][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
-    k_edges_v<ORDER><<<grid_v(A, 0), kEdgeBlock, 0, s>>>(a, 0);
+    k_edges_v<ORDER><<<grid_v(A, 0), edge_block_v(), 0, s>>>(a, 0);
     if (snaps) { cudaMemcpyAsync(snaps[2][0], acc[0], bytes, cudaMemcpyDeviceToDevice, s); cudaMemcpyAsync(snaps[2][1], acc[3], bytes, cudaMemcpyDeviceToDevice, s); }
-    k_edges_v<ORDER><<<grid_v(A, 1), kEdgeBlock, 0, s>>>(a, 1);
+    k_edges_v<ORDER><<<grid_v(A, 1), edge_block_v(), 0, s>>>(a, 1);
 }
 
 // One forward step X -> X (the product's step: the same kernels and order),
 // with the time record's dt; k_advance leaves the next dt in the record.
 void fwd_step(const lsh_adjoint* A, cudaStream_t s) {
-    const unsigned nb = cell_blocks(A);
+    const dim3 nbc = cell_grid(A->p.nx, A->p.ny);
     double* const* X = A->X;
     if (A->order == 1) {
         const KArgs a = fwd_args(A, X, X, nullptr, A->acc1, nullptr, nullptr);
         fwd_passes<1>(A, a, nullptr, A->acc1, s);
-        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+        k_volume<0><<<nbc, cell_block(), 0, s>>>(a);
     } else {
         double* Y7[7];
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
         Y7[6] = A->X[6];
         const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
-        k_recon<<<nb, kCellBlock, 0, s>>>(a1);
+        k_recon<<<nbc, cell_block(), 0, s>>>(a1);
         fwd_passes<2>(A, a1, nullptr, A->acc1, s);
-        k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+        k_volume<1><<<nbc, cell_block(), 0, s>>>(a1);
         const KArgs a2 = fwd_args(A, Y7, X, X, A->acc2, A->s2x, A->s2y);
-        k_recon<<<nb, kCellBlock, 0, s>>>(a2);
+        k_recon<<<nbc, cell_block(), 0, s>>>(a2);
         fwd_passes<2>(A, a2, nullptr, A->acc2, s);
-        k_volume<2><<<nb, kCellBlock, 0, s>>>(a2);
+        k_volume<2><<<nbc, cell_block(), 0, s>>>(a2);
     }
     k_advance<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
 }
@@ -535,6 +529,7 @@ int Ops::reverse_step(int n) {
     cudaStream_t s = A->stream;
     const size_t N = A->N;
     const unsigned nb = cell_blocks(A);
+    const dim3 nbc = cell_grid(A->p.nx, A->p.ny);
     const int G = A->grid;
     // recompute step n's intermediates
     k_set_dt<<<1, 1, 0, s>>>(A->tm, A->d_dts + n);
@@ -550,7 +545,7 @@ int Ops::reverse_step(int n) {
         const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
         k_recon_tape<<<nb, kCellBlock, 0, s>>>(a1, A->tape1);
         fwd_passes<2>(A, a1, A->snap1, A->acc1, s);
-        k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+        k_volume<1><<<nbc, cell_block(), 0, s>>>(a1);
         const KArgs a2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
         k_recon_tape<<<nb, kCellBlock, 0, s>>>(a2, A->tape2);
         fwd_passes<2>(A, a2, A->snap2, A->acc2, s);
@@ -763,7 +758,7 @@ int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS
         k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
         k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
         k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_cell_dt<<<cell_blocks(A), kCellBlock, 0, s>>>(a);
+        k_cell_dt<<<cell_grid(A->p.nx, A->p.ny), cell_block(), 0, s>>>(a);
         k_init_finish<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
         k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts);
         A_CUDA(cudaGetLastError());

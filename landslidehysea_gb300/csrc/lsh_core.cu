@@ -136,51 +136,43 @@ KArgs base_args(const lsh_ctx* ctx) {
     return a;
 }
 
-dim3 grid_h(const lsh_ctx* ctx, int par) {
-    const int nlines = (ctx->p.ny - par) / 2 + 1;
-    return dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min(nlines, 65535));
-}
+dim3 grid_h(const lsh_ctx* ctx, int par) { return edge_grid_h(ctx->p.nx, ctx->p.ny, par); }
+dim3 grid_v(const lsh_ctx* ctx, int par) { return edge_grid_v(ctx->p.nx, ctx->p.ny, par); }
 
-dim3 grid_v(const lsh_ctx* ctx, int par) {
-    const int nlines = (ctx->p.nx - par) / 2 + 1;
-    return dim3((nlines + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535));
-}
-
-unsigned cell_blocks(const lsh_ctx* ctx) { return unsigned((ctx->N + kCellBlock - 1) / kCellBlock); }
 
 template <int ORDER>
 void enqueue_passes(const lsh_ctx* ctx, const KArgs& a, cudaStream_t s) {
-    k_edges_h<true, ORDER><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0);
-    k_edges_h<false, ORDER><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1);
-    k_edges_v<ORDER><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0);
-    k_edges_v<ORDER><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1);
+    k_edges_h<true, ORDER><<<grid_h(ctx, 0), edge_block_h(), 0, s>>>(a, 0);
+    k_edges_h<false, ORDER><<<grid_h(ctx, 1), edge_block_h(), 0, s>>>(a, 1);
+    k_edges_v<ORDER><<<grid_v(ctx, 0), edge_block_v(), 0, s>>>(a, 0);
+    k_edges_v<ORDER><<<grid_v(ctx, 1), edge_block_v(), 0, s>>>(a, 1);
 }
 
 // Enqueue one time step; returns the number of kernels launched.
 int enqueue_step(const lsh_ctx* ctx, cudaStream_t s) {
-    const unsigned nb = cell_blocks(ctx);
+    const dim3 nbc = cell_grid(ctx->p.nx, ctx->p.ny);
     if (ctx->p.order == 1) {
         KArgs a = base_args(ctx);
         for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
         for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
         enqueue_passes<1>(ctx, a, s);
-        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+        k_volume<0><<<nbc, cell_block(), 0, s>>>(a);
         k_advance<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
         return 6;
     }
     KArgs a1 = base_args(ctx);
     for (int k = 0; k < 7; ++k) a1.W[k] = ctx->X[k];
     for (int k = 0; k < 6; ++k) a1.Wout[k] = ctx->Y[k];
-    k_recon<<<nb, kCellBlock, 0, s>>>(a1);
+    k_recon<<<nbc, cell_block(), 0, s>>>(a1);
     enqueue_passes<2>(ctx, a1, s);
-    k_volume<1><<<nb, kCellBlock, 0, s>>>(a1);
+    k_volume<1><<<nbc, cell_block(), 0, s>>>(a1);
     KArgs a2 = base_args(ctx);
     for (int k = 0; k < 6; ++k) a2.W[k] = ctx->Y[k];
     a2.W[6] = ctx->X[6];
     for (int k = 0; k < 6; ++k) { a2.Wout[k] = ctx->X[k]; a2.Xavg[k] = ctx->X[k]; }
-    k_recon<<<nb, kCellBlock, 0, s>>>(a2);
+    k_recon<<<nbc, cell_block(), 0, s>>>(a2);
     enqueue_passes<2>(ctx, a2, s);
-    k_volume<2><<<nb, kCellBlock, 0, s>>>(a2);
+    k_volume<2><<<nbc, cell_block(), 0, s>>>(a2);
     k_advance<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
     return 13;
 }
@@ -211,9 +203,9 @@ int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKin
     }
     KArgs a = base_args(ctx);
     for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
-    const unsigned nb = cell_blocks(ctx);
+    const dim3 nbc = cell_grid(ctx->p.nx, ctx->p.ny);
     cudaStream_t s = ctx->stream;
-    k_init_eta<<<nb, kCellBlock, 0, s>>>(a);
+    k_init_eta<<<nbc, cell_block(), 0, s>>>(a);
     TimeRec init{};
     init.rmax_bits = kRateInitBits;
     init.t_end = INFINITY;
@@ -223,7 +215,7 @@ int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKin
     k_init_wave<0, false><<<dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ctx->p.ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
     k_init_wave<1, false><<<dim3(((ctx->p.nx) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
     k_init_wave<1, false><<<dim3(((ctx->p.nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-    k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
+    k_cell_dt<<<nbc, cell_block(), 0, s>>>(a);
     k_init_finish<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
     ctx->launches += 7;
     LSH_CUDA(cudaGetLastError());
@@ -495,7 +487,7 @@ int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels) {
     const int nk = ctx->kernels_per_step;
     std::vector<cudaEvent_t> ev(nk + 1);
     for (auto& e : ev) LSH_CUDA(cudaEventCreate(&e));
-    const unsigned nb = cell_blocks(ctx);
+    const dim3 nbc = cell_grid(ctx->p.nx, ctx->p.ny);
     int i = 0;
     auto mark = [&]() { cudaEventRecord(ev[i++], s); };
     mark();
@@ -503,11 +495,11 @@ int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels) {
         KArgs a = base_args(ctx);
         for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
         for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
-        k_edges_h<true, 1><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
-        k_edges_h<false, 1><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
-        k_edges_v<1><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
-        k_edges_v<1><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
-        k_volume<0><<<nb, kCellBlock, 0, s>>>(a); mark();
+        k_edges_h<true, 1><<<grid_h(ctx, 0), edge_block_h(), 0, s>>>(a, 0); mark();
+        k_edges_h<false, 1><<<grid_h(ctx, 1), edge_block_h(), 0, s>>>(a, 1); mark();
+        k_edges_v<1><<<grid_v(ctx, 0), edge_block_v(), 0, s>>>(a, 0); mark();
+        k_edges_v<1><<<grid_v(ctx, 1), edge_block_v(), 0, s>>>(a, 1); mark();
+        k_volume<0><<<nbc, cell_block(), 0, s>>>(a); mark();
     } else {
         for (int stage = 0; stage < 2; ++stage) {
             KArgs a = base_args(ctx);
@@ -519,13 +511,13 @@ int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels) {
                 a.W[6] = ctx->X[6];
                 for (int k = 0; k < 6; ++k) { a.Wout[k] = ctx->X[k]; a.Xavg[k] = ctx->X[k]; }
             }
-            k_recon<<<nb, kCellBlock, 0, s>>>(a); mark();
-            k_edges_h<true, 2><<<grid_h(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
-            k_edges_h<false, 2><<<grid_h(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
-            k_edges_v<2><<<grid_v(ctx, 0), kEdgeBlock, 0, s>>>(a, 0); mark();
-            k_edges_v<2><<<grid_v(ctx, 1), kEdgeBlock, 0, s>>>(a, 1); mark();
-            if (stage == 0) k_volume<1><<<nb, kCellBlock, 0, s>>>(a);
-            else k_volume<2><<<nb, kCellBlock, 0, s>>>(a);
+            k_recon<<<nbc, cell_block(), 0, s>>>(a); mark();
+            k_edges_h<true, 2><<<grid_h(ctx, 0), edge_block_h(), 0, s>>>(a, 0); mark();
+            k_edges_h<false, 2><<<grid_h(ctx, 1), edge_block_h(), 0, s>>>(a, 1); mark();
+            k_edges_v<2><<<grid_v(ctx, 0), edge_block_v(), 0, s>>>(a, 0); mark();
+            k_edges_v<2><<<grid_v(ctx, 1), edge_block_v(), 0, s>>>(a, 1); mark();
+            if (stage == 0) k_volume<1><<<nbc, cell_block(), 0, s>>>(a);
+            else k_volume<2><<<nbc, cell_block(), 0, s>>>(a);
             mark();
         }
     }
@@ -665,26 +657,24 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     a.tm = tm;
 
     const int nx = p->nx, ny = p->ny;
-    const unsigned nb = unsigned((size_t(nx) * ny + kCellBlock - 1) / kCellBlock);
+    const dim3 nbc = cell_grid(nx, ny);
     if (!(*dt_io > 0.0)) {
         // initial dt (ShallowWater.cu:236-257) into the time record
         k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
         k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
         k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
         k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_cell_dt<<<nb, kCellBlock, 0, s>>>(a);
+        k_cell_dt<<<nbc, cell_block(), 0, s>>>(a);
         k_noalloc_take_dt<<<1, 1, 0, s>>>(tm, 2.0 * p->cfl);
     }
-    const dim3 gh0((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535));
-    const dim3 gh1((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535));
-    const dim3 gv0((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535));
-    const dim3 gv1(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535));
+    const dim3 gh0 = edge_grid_h(nx, ny, 0), gh1 = edge_grid_h(nx, ny, 1);
+    const dim3 gv0 = edge_grid_v(nx, ny, 0), gv1 = edge_grid_v(nx, ny, 1);
     for (int i = 0; i < nsteps; ++i) {
-        k_edges_h<true, 1><<<gh0, kEdgeBlock, 0, s>>>(a, 0);
-        k_edges_h<false, 1><<<gh1, kEdgeBlock, 0, s>>>(a, 1);
-        k_edges_v<1><<<gv0, kEdgeBlock, 0, s>>>(a, 0);
-        k_edges_v<1><<<gv1, kEdgeBlock, 0, s>>>(a, 1);
-        k_volume<0><<<nb, kCellBlock, 0, s>>>(a);
+        k_edges_h<true, 1><<<gh0, edge_block_h(), 0, s>>>(a, 0);
+        k_edges_h<false, 1><<<gh1, edge_block_h(), 0, s>>>(a, 1);
+        k_edges_v<1><<<gv0, edge_block_v(), 0, s>>>(a, 0);
+        k_edges_v<1><<<gv1, edge_block_v(), 0, s>>>(a, 1);
+        k_volume<0><<<nbc, cell_block(), 0, s>>>(a);
         k_advance<<<1, 1, 0, s>>>(tm, 2.0 * p->cfl);
     }
     LSH_CUDA(cudaGetLastError());

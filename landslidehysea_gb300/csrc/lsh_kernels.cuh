@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/lsh.h"
 #include "lsh_passes.cuh"
 
@@ -18,28 +20,71 @@ using lsh::kCellBlock;
 using lsh::kEdgeBlock;
 using lsh::kRateInitBits;
 
-// Horizontal edges of parity `par`: x along threads, edge rows along blocks.
+// Thread-block shapes of the edge passes (x along threadIdx.x, lines along
+// threadIdx.y; kEdgeBlock threads): a warp spans LSH_EDGE_H_BX cells of an
+// edge row, or LSH_EDGE_V_BX edge columns (2 LSH_EDGE_V_BX cells) of a row,
+// and 32 / BX lines, so fewer warps straddle a wet/dry front than with
+// one-line warps, while each row segment stays one contiguous load.
+#ifndef LSH_EDGE_H_BX
+#define LSH_EDGE_H_BX 16
+#endif
+#ifndef LSH_EDGE_V_BX
+#define LSH_EDGE_V_BX 8
+#endif
+constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeBlock / LSH_EDGE_H_BX;
+constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeBlock / LSH_EDGE_V_BX;
+
+// Horizontal edges of parity `par`: x along threadIdx.x, edge rows par, par+2, ... along threadIdx.y / blocks.y.
 template <bool FIRST, int ORDER>
 __global__ void __launch_bounds__(kEdgeBlock) k_edges_h(KArgs a, int par) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = blockIdx.x * kEdgeHBX + threadIdx.x;
     if (x >= nx) return;
     const double dt = a.tm->dt;
     const int nlines = (ny - par) / 2 + 1;
-    for (int t = blockIdx.y; t < nlines; t += gridDim.y) lsh::do_edge<0, FIRST, ORDER>(a, x, par + 2 * t, dt);
+    for (int t = blockIdx.y * kEdgeHBY + threadIdx.y; t < nlines; t += gridDim.y * kEdgeHBY)
+        lsh::do_edge<0, FIRST, ORDER>(a, x, par + 2 * t, dt);
 }
 
-// Vertical edges of parity `par`: edge columns along threads, rows along blocks.
+// Vertical edges of parity `par`: edge columns par, par+2, ... along threadIdx.x, rows along threadIdx.y / blocks.y.
 template <int ORDER>
 __global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * kEdgeVBX + threadIdx.x;
     const int x = par + 2 * t;
     if (x > nx) return;
     const double dt = a.tm->dt;
-    for (int y = blockIdx.y; y < ny; y += gridDim.y) lsh::do_edge<1, false, ORDER>(a, x, y, dt);
+    for (int y = blockIdx.y * kEdgeVBY + threadIdx.y; y < ny; y += gridDim.y * kEdgeVBY)
+        lsh::do_edge<1, false, ORDER>(a, x, y, dt);
+}
+
+// Launch shapes of the two edge passes.
+inline dim3 edge_block_h() { return dim3(kEdgeHBX, kEdgeHBY); }
+inline dim3 edge_block_v() { return dim3(kEdgeVBX, kEdgeVBY); }
+inline dim3 edge_grid_h(int nx, int ny, int par) {
+    const int nlines = (ny - par) / 2 + 1;
+    return dim3((nx + kEdgeHBX - 1) / kEdgeHBX, std::min((nlines + kEdgeHBY - 1) / kEdgeHBY, 65535));
+}
+inline dim3 edge_grid_v(int nx, int ny, int par) {
+    const int nlines = (nx - par) / 2 + 1;
+    return dim3((nlines + kEdgeVBX - 1) / kEdgeVBX, std::min((ny + kEdgeVBY - 1) / kEdgeVBY, 65535));
+}
+
+// Cell kernels: blocks of kCellBlock threads shaped LSH_CELL_BX x
+// (kCellBlock / LSH_CELL_BX) over (x, y); LSH_CELL_BX = kCellBlock is one
+// row segment per block.
+#ifndef LSH_CELL_BX
+#define LSH_CELL_BX 16
+#endif
+constexpr int kCellBX = LSH_CELL_BX, kCellBY = kCellBlock / LSH_CELL_BX;
+inline dim3 cell_block() { return dim3(kCellBX, kCellBY); }
+inline dim3 cell_grid(int nx, int ny) { return dim3((nx + kCellBX - 1) / kCellBX, (ny + kCellBY - 1) / kCellBY); }
+// The cell of this thread, or -1 outside the grid.
+__device__ __forceinline__ int cell_of_thread(int nx, int ny) {
+    const int x = blockIdx.x * kCellBX + threadIdx.x, y = blockIdx.y * kCellBY + threadIdx.y;
+    return (x < nx && y < ny) ? y * nx + x : -1;
 }
 
 // Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
@@ -47,8 +92,8 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
 // kReconThin of the cell depth.
 __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
     if (a.tm->done) return;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.c.nx * a.c.ny) return;
+    const int id = cell_of_thread(a.c.nx, a.c.ny);
+    if (id < 0) return;
     lsh::recon_cell(a, id);
 }
 
@@ -57,10 +102,10 @@ __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
 template <int MODE>
 __global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
     if (a.tm->done) return;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = cell_of_thread(a.c.nx, a.c.ny);
     const double dt = a.tm->dt;
     unsigned long long bits = kRateInitBits;
-    if (id < a.c.nx * a.c.ny) bits = lsh::volume_cell<MODE>(a, id, dt);
+    if (id >= 0) bits = lsh::volume_cell<MODE>(a, id, dt);
     if (MODE != 2) lsh::block_max_bits<kCellBlock>(bits, &a.tm->rmax_bits);
 }
 
@@ -94,9 +139,9 @@ __global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
 
 // Per-cell rate of the initial wave pass (obtenerDeltaTVolumenesGPU) and its max.
 __global__ void __launch_bounds__(kCellBlock) k_cell_dt(KArgs a) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = cell_of_thread(a.c.nx, a.c.ny);
     unsigned long long bits = kRateInitBits;
-    if (id < a.c.nx * a.c.ny) bits = lsh::init_cell_rate(a, id);
+    if (id >= 0) bits = lsh::init_cell_rate(a, id);
     lsh::block_max_bits<kCellBlock>(bits, &a.tm->rmax_bits);
 }
 
@@ -111,8 +156,8 @@ __global__ void k_init_finish(TimeRec* tm, double two_cfl) {
 
 // eta1 max initial value h1 + h2 - H, time 0 (Problema.cxx:542-546)
 __global__ void __launch_bounds__(kCellBlock) k_init_eta(KArgs a) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.c.nx * a.c.ny) return;
+    const int id = cell_of_thread(a.c.nx, a.c.ny);
+    if (id < 0) return;
     a.eta_max[id] = a.W[0][id] + a.W[3][id] - a.W[6][id];
     a.eta_time[id] = 0.0;
 }

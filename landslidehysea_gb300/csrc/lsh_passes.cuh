@@ -262,11 +262,13 @@ __device__ __forceinline__ void block_max_bits(unsigned long long v, unsigned lo
         const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
         v = (w > v) ? w : v;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // linear thread index (blocks may be 2-D; warps are x-fastest)
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : kRateInitBits;
+        v = (lane < BLOCK / 32) ? red[lane] : kRateInitBits;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
