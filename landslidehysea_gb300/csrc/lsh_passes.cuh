@@ -372,7 +372,12 @@ LSH_HD void init_wave_edge(const KArgs& a, int x, int y) {
         B.qn1 = A.qn1 * bor;
         B.qn2 = A.qn2 * bor;
     }
-    const double wv = lsh::edge_initial_wave(A, B, len, a.c);
+    // both faces empty and still: every term of the bound is an exact zero and
+    // lmax = 0 + eps_h, so the wave is len * eps_h without the FP64 work
+    using lsh::is_zero;
+    const bool empty = is_zero(A.h1) && is_zero(A.h2) && is_zero(B.h1) && is_zero(B.h2) && is_zero(A.qn1) &&
+                       is_zero(A.qn2) && is_zero(B.qn1) && is_zero(B.qn2);
+    const double wv = empty ? len * (0.0 + a.c.eps_h) : lsh::edge_initial_wave(A, B, len, a.c);
     if (FIRST) {
         a.acc[6][id0] = 0.0 + wv;
         if (id1 >= 0) a.acc[6][id1] = 0.0 + wv;

@@ -94,6 +94,7 @@ def native_lib(name):
         lib.adjl_initial_wave.argtypes = [ctypes.c_uint64, ctypes.c_int, D, D]
         lib.adjl_set_component.argtypes = [ctypes.c_int]
         lib.adjl_set_bor.argtypes = [ctypes.c_double]
+        lib.adjl_initial_wave_empty.restype = ctypes.c_int
     elif name == "adj_host":
         lib.adjh_run.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P, D, P, P, ctypes.c_double]
         lib.adjh_recon_check.restype = ctypes.c_longlong

@@ -269,3 +269,30 @@ double adjl_initial_wave(uint64_t seed, int ndir, double* fd_out, double* adj_ou
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// The initial-dt pass's empty-edge shortcut (lsh_passes.cuh init_wave_edge):
+// for two faces with zero depths and normal discharges (either sign of zero)
+// the bound is exactly len * (0 + eps_h).  Returns the number of mismatches.
+int adjl_initial_wave_empty(void) {
+    Consts c{};
+    c.g = 9.81; c.r = 0.5; c.gp = c.g * 0.5; c.inv_gp = 1.0 / c.gp; c.sqrt_g = std::sqrt(c.g);
+    int bad = 0;
+    const double epss[3] = {1e-5, 5e-3, 1e-3}, lens[3] = {11.1, 22.2, 37.0};
+    for (double eps : epss)
+        for (double len : lens)
+            for (int sg = 0; sg < 4; ++sg) {
+                c.eps_h = eps;
+                c.inv_eps = 1.0 / eps;
+                Face A{}, B{};
+                if (sg & 1) { A.qn1 = -0.0; B.qn2 = -0.0; A.h1 = -0.0; }
+                if (sg & 2) { A.qt1 = 3.0; B.qt2 = -2.0; }  // tangential discharge does not enter the bound
+                A.H = 150.0; B.H = 120.0;
+                const double w = edge_initial_wave(A, B, len, c), s = len * (0.0 + eps);
+                if (lshm::bits_of(w) != lshm::bits_of(s)) ++bad;
+            }
+    return bad;
+}
+
+}  // extern "C"

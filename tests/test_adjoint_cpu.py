@@ -168,3 +168,9 @@ def test_thin_layer_projection_adjoint_is_the_tangent_linears_transpose(kind, or
     dl = [(wet_direction(arrs, w, 8), [0, 0, 0, 0]) for w in ((3,), (0,), (1, 2), (4, 5))]
     dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
     _dot_check(p, arrs, gauges, 6, dl, 1e-11, h_adj=h_adj)
+
+
+def test_initial_wave_empty_edge_shortcut_is_exact():
+    """The kernels skip the initial-dt bound's FP64 work on empty, still edge
+    pairs: the general formula gives exactly len * eps_h there."""
+    assert native_lib("adj_local").adjl_initial_wave_empty() == 0
