@@ -340,11 +340,14 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         const int k = 3 * layer;
         useA[layer] = (M[k] > 0.0);
         useB[layer] = e.interior && (P[k] > 0.0);
-        if (useA[layer]) { denA[layer] = fmad(factor, M[k], kEps); dta[layer] = (hp0[layer] * e.area0) / denA[layer]; }
-        if (useB[layer]) { denB[layer] = fmad(factor, P[k], kEps); dtbv[layer] = (hp1[layer] * e.area1) / denB[layer]; }
-        dtl[layer] = tmin(dta[layer], dtbv[layer]);
-        if (!(dt <= dtl[layer])) {
-            lim[layer] = true;
+        const double ha = hp0[layer] * e.area0, hb = hp1[layer] * e.area1;
+        if (useA[layer]) denA[layer] = fmad(factor, M[k], kEps);
+        if (useB[layer]) denB[layer] = fmad(factor, P[k], kEps);
+        lim[layer] = (useA[layer] && !(dt * denA[layer] <= ha)) || (useB[layer] && !(dt * denB[layer] <= hb));
+        if (lim[layer]) {
+            if (useA[layer]) dta[layer] = ha / denA[layer];
+            if (useB[layer]) dtbv[layer] = hb / denB[layer];
+            dtl[layer] = tmin(dta[layer], dtbv[layer]);
             alpha[layer] = dtl[layer] / (dt + kEps);
         }
     }

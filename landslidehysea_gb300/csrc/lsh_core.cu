@@ -88,6 +88,7 @@ struct lsh_ctx {
     double* sy[7] = {};
     double* eta_max = nullptr;
     double* eta_time = nullptr;
+    unsigned char* szero = nullptr;  // order 2: per-cell "stored slopes are zero" flags
     double* geo_buf = nullptr;
     Geo geo{};
     TimeRec* tm = nullptr;
@@ -132,6 +133,7 @@ KArgs base_args(const lsh_ctx* ctx) {
     }
     a.eta_max = ctx->eta_max;
     a.eta_time = ctx->eta_time;
+    a.szero = ctx->szero;
     a.tm = ctx->tm;
     return a;
 }
@@ -320,7 +322,8 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     const size_t n_pad = (ctx->N + 31) & ~size_t(31);  // 256-byte aligned arrays
     const int n_arrays = 7 + 6 + 7 + 2 + ((p->order == 2) ? 14 : 0);
     const size_t geo_n = size_t(7) * (p->ny + 1);
-    const size_t bytes = (size_t(n_arrays) * n_pad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) + 256;
+    const size_t bytes = (size_t(n_arrays) * n_pad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) + 256 +
+                         ((p->order == 2) ? n_pad : 0);  // + one byte per cell: slopes-are-zero flags
     {
         cudaError_t e = cudaMalloc(&ctx->slab, bytes);
         if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc"));
@@ -340,6 +343,13 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     ctx->geo_buf = cur;
     cur += (geo_n + 31) & ~size_t(31);
     ctx->tm = reinterpret_cast<TimeRec*>(cur);
+    if (p->order == 2) {
+        ctx->szero = reinterpret_cast<unsigned char*>(cur) + 256;
+        // no slope is known to be zero yet; wait before the legacy-stream copies below
+        cudaError_t e = cudaMemsetAsync(ctx->szero, 0, n_pad, ctx->own);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->own);
+        if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemset slope flags"));
+    }
 
     const size_t st = size_t(p->ny + 1);
     std::vector<double> g(geo_n, 0.0);

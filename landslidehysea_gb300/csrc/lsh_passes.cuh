@@ -40,6 +40,7 @@ struct KArgs {
     double* eta_max;
     double* eta_time;
     TimeRec* tm;
+    unsigned char* szero;  // per cell: 1 when the stored slopes are all zero (may be null)
 };
 
 // Depths of a face (first order: the cell's; second order: reconstructed).
@@ -223,8 +224,12 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
         if (dry && j > 0) dry = is_zero(a.W[0][id - nx]) && is_zero(a.W[3][id - nx]);
         if (dry && j < ny - 1) dry = is_zero(a.W[0][id + nx]) && is_zero(a.W[3][id + nx]);
         if (dry) {
+            // zero slopes; a cell whose stored slopes are already zero (and stays
+            // dry, the common case far from the flow) skips the 14 stores
+            if (a.szero && a.szero[id]) return;
 #pragma unroll
             for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
+            if (a.szero) a.szero[id] = 1;
             return;
         }
     }
@@ -249,6 +254,7 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
         a.sxw[k][id] = bad ? 0.0 : sx[k];
         a.syw[k][id] = bad ? 0.0 : sy[k];
     }
+    if (a.szero) a.szero[id] = 0;  // conservative: only the dry path marks zeros
 }
 
 #if defined(__CUDACC__)

@@ -331,11 +331,16 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
 #pragma unroll
     for (int layer = 0; layer < (L2 ? 2 : 1); ++layer) {
         const int k = 3 * layer;
-        double dta = kBig, dtb = kBig;
-        if (M[k] > 0.0) dta = ((layer ? hp01 : hp00) * e.area0) / fmad(factor, M[k], kEps);
-        if (e.interior && P[k] > 0.0) dtb = ((layer ? hp11 : hp10) * e.area1) / fmad(factor, P[k], kEps);
-        const double dtl = tmin(dta, dtb);
-        if (!(dt <= dtl)) {
+        // limited when dt exceeds the time a side takes to empty its layer,
+        // hp area / (beta M + eps): tested as dt (beta M + eps) > hp area (the
+        // denominator is positive), so the divisions run only on limited edges
+        const bool oa = (M[k] > 0.0), ob = e.interior && (P[k] > 0.0);
+        const double ha = (layer ? hp01 : hp00) * e.area0, hb = (layer ? hp11 : hp10) * e.area1;
+        const double da = oa ? fmad(factor, M[k], kEps) : 1.0, db = ob ? fmad(factor, P[k], kEps) : 1.0;
+        const bool lim = (oa && !(dt * da <= ha)) || (ob && !(dt * db <= hb));
+        if (lim) {
+            const double dta = oa ? ha / da : kBig, dtb = ob ? hb / db : kBig;
+            const double dtl = tmin(dta, dtb);
             const double alpha = dtl / (dt + kEps);
 #pragma unroll
             for (int q = 0; q < 3; ++q) { M[k + q] = alpha * M[k + q]; P[k + q] = alpha * P[k + q]; }

@@ -427,11 +427,17 @@ bool edge_flux(const EdgeIn<T>& e, T dt, const ConstsT<T>& c, EdgeOut<T>& o) {
     const T factor = 1.0 * c.beta;
     for (int layer = 0; layer < 2; ++layer) {
         const int k = 3 * layer;
-        T dta = kBig, dtb = kBig;
-        if (M[k] > 0.0) dta = ((layer ? hp01 : hp00) * e.area0) / fmad(factor, M[k], kEps);
-        if (e.interior && P[k] > 0.0) dtb = ((layer ? hp11 : hp10) * e.area1) / fmad(factor, P[k], kEps);
-        const T dtl = tmin(dta, dtb);
-        if (!(dt <= dtl)) {
+        // the reference limits when dt > min(hp area / (beta M + eps)) over the
+        // outflow sides; the denominators are positive, so the test is
+        // dt (beta M + eps) > hp area, and the quotients are formed only for a
+        // limited edge (the CUDA kernels evaluate the same sequence)
+        const bool oa = (M[k] > 0.0), ob = e.interior && (P[k] > 0.0);
+        const T ha = (layer ? hp01 : hp00) * e.area0, hb = (layer ? hp11 : hp10) * e.area1;
+        const T da = oa ? fmad(factor, M[k], kEps) : T(1.0), db = ob ? fmad(factor, P[k], kEps) : T(1.0);
+        const bool lim = (oa && !(dt * da <= ha)) || (ob && !(dt * db <= hb));
+        if (lim) {
+            const T dta = oa ? ha / da : T(kBig), dtb = ob ? hb / db : T(kBig);
+            const T dtl = tmin(dta, dtb);
             const T alpha = dtl / (dt + kEps);
             for (int q = k; q < k + 3; ++q) { M[q] = alpha * M[q]; P[q] = alpha * P[q]; }
         }
