@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--n", type=int, default=2048, help="grid size (n x n); the headline is 2048")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint"), default="fjord",
+    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint", "adjoint-batch"), default="fjord",
                     help="fjord: the 2048^2 headline; ensemble: the batched 256-scenario ensemble vs serial; "
                          "adjoint: gradient of the 16-gauge misfit on the 1024^2 fjord vs its forward")
     ap.add_argument("--adj-n", type=int, default=1024, help="adjoint workload grid size")
@@ -80,6 +80,9 @@ def parse():
     ap.add_argument("--adj-thin", type=float, default=0.1,
                     help="thin-layer projection of the adjoint, metres (0: the exact adjoint)")
     ap.add_argument("--count", type=int, default=256, help="ensemble scenarios")
+    ap.add_argument("--cal-count", type=int, default=64, help="batched-adjoint scenarios")
+    ap.add_argument("--cal-steps", type=int, default=300, help="batched-adjoint steps (the full calibration: 3000)")
+    ap.add_argument("--cal-serial", type=int, default=1, help="also run the members one by one (1) or not (0)")
     return ap.parse_args()
 
 
@@ -571,12 +574,86 @@ def run_adjoint(args):
     return 0
 
 
+def run_adjoint_batch(args):
+    """Batched adjoint calibration: `cal_count` fjord scenarios on grids drawn
+    from 256^2 .. 1024^2 (seed = scenario id), each with the 16-gauge misfit
+    against its twin run (Coulomb angle, Manning coefficients and density
+    ratio scaled by seeded +-5%), run forward and reversed together under one
+    checkpoint schedule with a joint budget (default 180 GB or free memory).
+    `value` is cell-steps of all scenarios over the wall time of
+    lsh_adjoint_batch_forward + lsh_adjoint_batch_gradient; `serial` runs the
+    same members one after another through lsh_adjoint_forward / _gradient
+    with the same slot count, and must give the same gradients bit for bit."""
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from landslidehysea_gb300 import build as B
+    B.build()
+    from landslidehysea_gb300 import scenarios
+    from landslidehysea_gb300.solver import AdjointBatch
+    nsteps = args.cal_steps
+    mem = [scenarios.calibration_member(k) for k in range(args.cal_count)]
+    scs = [m[0] for m in mem]
+    gauges = [scenarios.gauge_cells(sc) for sc in scs]
+    cells = [sc.params.nx * sc.params.ny for sc in scs]
+    # the twins' gauge series (one checkpoint slot each: a plain forward run)
+    with AdjointBatch([m[1] for m in mem], gauges, device=local) as T:
+        T.set_budget(sum(6 * 8 * ((c + 31) // 32 * 32) for c in cells) + 1.0)
+        _, targets = T.forward([sc.state for sc in scs], nsteps)
+    line = {"metric": "batched adjoint: gradient cell-steps/s (forward + reverse sweep)", "unit": "cell-steps/s",
+            "n_gpus": 1, "steps": nsteps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"calibration{args.cal_count}_fjord_order2_spherical_adjoint",
+                       "scenarios": args.cal_count, "steps": nsteps,
+                       "sizes": {str(n): sum(1 for sc in scs if sc.params.nx == n) for n in scenarios.CALIBRATION_SIZES},
+                       "cells": int(sum(cells)), "gauges_per_scenario": 16, "thin_layer_m": args.adj_thin,
+                       "gradient": ["h2 field", "angle1", "mf0", "mfs", "r"]}}
+    work = float(sum(cells)) * nsteps
+    with AdjointBatch([sc.params for sc in scs], gauges, device=local) as A:
+        if args.adj_budget_gb is not None:
+            A.set_budget(args.adj_budget_gb * 1e9)
+        A.set_thin_layer(args.adj_thin)
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            J, _ = A.forward([sc.state for sc in scs], nsteps, targets)
+            t1 = time.perf_counter()
+            _, gp = A.gradient(want_state=True)
+            t2 = time.perf_counter()
+        st = A.stats()
+        line.update({"value": work / (t2 - t0), "ms_per_step": 1e3 * (t2 - t0) / nsteps,
+                     "forward_s": t1 - t0, "gradient_s": t2 - t1, "gradient_over_forward": (t2 - t1) / (t1 - t0),
+                     "stats": st, "clocks": clk.summary(),
+                     "misfit_sum": float(np.sum(J)),
+                     "grad_params_first": gp[0]})
+        if args.cal_serial:
+            same = True
+            ts = time.perf_counter()
+            for i, sc in enumerate(scs):
+                m = A.member(i)
+                m.forward(sc.state, nsteps, targets[i])
+                _, g1 = m.gradient()
+                same = same and g1 == gp[i]
+            t_serial = time.perf_counter() - ts
+            line["serial"] = {"value": work / t_serial, "seconds": t_serial, "same_gradients": bool(same),
+                              "what": "the same members one after another (lsh_adjoint_forward + lsh_adjoint_gradient, "
+                                      "the batch's slot count)"}
+            line["batched_over_serial"] = t_serial / (t2 - t0)
+    line["gpu_launches"] = None
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "ours" and args.workload == "ensemble":
         return run_ensemble(args)
     if args.impl == "ours" and args.workload == "adjoint":
         return run_adjoint(args)
+    if args.impl == "ours" and args.workload == "adjoint-batch":
+        return run_adjoint_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

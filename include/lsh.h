@@ -270,6 +270,44 @@ int lsh_adjoint_get_times(lsh_adjoint* a, double* t_out);
 /* the recorded run's final state X_N (6 host arrays, entries may be NULL);
  * valid after lsh_adjoint_forward, before lsh_adjoint_gradient */
 int lsh_adjoint_get_state(lsh_adjoint* a, double* const host_state[6]);
+/* ------------------------------------------------------------------------
+ * Batched adjoint: n scenarios (uneven grids, each with its own parameters
+ * and gauges) run forward and reversed together, for one step count.  One
+ * checkpoint schedule drives every member with the same slot count, taken
+ * from a joint budget (default 180 GB, capped by free device memory) over
+ * the members' summed slot bytes; each member's kernels run on its own
+ * stream, so the members overlap on the GPU.  Each member's misfit and
+ * gradient are bit-identical to an lsh_adjoint of its own with that slot
+ * count.
+ * ------------------------------------------------------------------------ */
+typedef struct lsh_adjoint_batch lsh_adjoint_batch;
+
+/* params[n]; n_gauges[n] (NULL: none) and gauge_cells[n] (member i's cells) */
+int lsh_adjoint_batch_create(int n, const lsh_params* params, const int* n_gauges, const int* const* gauge_cells,
+                             int device, lsh_adjoint_batch** out);
+int lsh_adjoint_batch_destroy(lsh_adjoint_batch* b);
+int lsh_adjoint_batch_set_thin_layer(lsh_adjoint_batch* b, double h_adj);
+/* device bytes all members' checkpoint slots may take together */
+int lsh_adjoint_batch_set_budget(lsh_adjoint_batch* b, double bytes);
+/* host_states: n x LSH_NVARS arrays (member i's variable k at [i LSH_NVARS + k]);
+ * targets[n] (NULL, or entries NULL: no misfit), misfits[n] (may be NULL),
+ * gauge_series[n] (may be NULL, entries may be NULL): as lsh_adjoint_forward */
+int lsh_adjoint_batch_forward(lsh_adjoint_batch* b, const double* const* host_states, int nsteps,
+                              const double* const* targets, double* misfits, double* const* gauge_series);
+/* gradient of misfit_weights[i] * J_i (NULL: weights 1) for every member;
+ * grad_states: n x 6 host arrays (may be NULL, entries may be NULL);
+ * grad_params: n x 4 (may be NULL) */
+int lsh_adjoint_batch_gradient(lsh_adjoint_batch* b, const double* misfit_weights, double* const* grad_states,
+                               double* grad_params);
+/* slots per member, steps, schedule counts per member; ms_* are the batch's
+ * wall times; slot_bytes is the bytes of one slot of every member together */
+int lsh_adjoint_batch_get_stats(lsh_adjoint_batch* b, lsh_adjoint_stats* out);
+/* member i, owned by the batch (lsh_adjoint_destroy refuses it); after a
+ * batch forward run it may be run on its own with the batch's slot count;
+ * lsh_adjoint_batch_gradient then refuses the batch if the members' records
+ * no longer stand at the same point of the schedule */
+int lsh_adjoint_batch_member(lsh_adjoint_batch* b, int i, lsh_adjoint** out);
+
 /* the checkpoint schedule alone (no device work): the forward steps it takes
  * to reverse nsteps with `slots` slots (its first descent included; the
  * forward run's remaining steps to X_N not) and the optimum

@@ -339,6 +339,9 @@ struct lsh_adjoint {
     double h_adj = 0.0;       // thin-layer projection threshold (0: the exact adjoint)
     double* hN[2] = {};       // h1, h2 of the recorded run's final state
     std::vector<double> h_dts;
+    std::vector<double> h_eta;  // the gauge series, nsteps x ng
+    double h_red[kRed] = {};    // dt and constant adjoints after the sweep
+    bool in_batch = false;      // a member of an lsh_adjoint_batch (destroyed with it)
     bool have_forward = false;
     bool spine_stored = false;  // slots 1.. hold the first descent (until a reverse sweep reuses them)
     int cur_step = -1;          // step of the state in X
@@ -584,7 +587,238 @@ int Ops::reverse_step(int n) {
     return 0;
 }
 
+// ------------------------------------------------------------------ phases
+//
+// lsh_adjoint_forward and lsh_adjoint_gradient run these for one adjoint;
+// lsh_adjoint_batch_* runs them for every member in lockstep, so that each
+// member's stream holds a few steps of work at a time and the members'
+// kernels overlap.  All of it is asynchronous on A->stream except the copies
+// into pageable host memory, which wait for the stream to reach them.
+
+// The initial-dt wave pass over X (the same kernels as lsh_set_state).
+void init_wave_pass(const lsh_adjoint* A, const KArgs& a, cudaStream_t s) {
+    const int nx = A->p.nx, ny = A->p.ny;
+    k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+    k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+    k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
+    k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+}
+
+// The steps after which the forward sweep stores a checkpoint: the binomial
+// schedule's first descent over [0, nsteps) with `slots` slots, slot 0
+// holding X_0.
+std::vector<int> spine_steps(int nsteps, int slots) {
+    std::vector<int> v;
+    int a = 0, free = slots - 1;
+    while (nsteps - a > 1 && free > 0) {
+        const int m = a + (int)lsh::revolve_split(nsteps - a, free + 1);
+        v.push_back(m);
+        a = m;
+        --free;
+    }
+    return v;
+}
+
+double slot_bytes_of(const lsh_adjoint* A) { return 6.0 * A->npad * sizeof(double); }
+
+// The per-step records for nsteps and `want` checkpoint slots.  On
+// LSH_ERR_GPU_OOM no slots are held.
+int fwd_alloc(lsh_adjoint* A, int nsteps, int want) {
+    if (nsteps != A->nsteps) {
+        cudaFree(A->d_dts); cudaFree(A->d_eta); cudaFree(A->d_tgt);
+        A->d_dts = nullptr; A->d_eta = nullptr; A->d_tgt = nullptr;
+        A->nsteps = 0;
+        A_CUDA(cudaMalloc(&A->d_dts, sizeof(double) * (nsteps + 1)));
+        if (A->ng > 0) {
+            A_CUDA(cudaMalloc(&A->d_eta, sizeof(double) * (size_t)nsteps * A->ng));
+            A_CUDA(cudaMalloc(&A->d_tgt, sizeof(double) * (size_t)nsteps * A->ng));
+        }
+        A->nsteps = nsteps;
+    }
+    if (want != A->n_slots) {
+        cudaFree(A->slots);
+        A->slots = nullptr;
+        A->n_slots = 0;
+        A_CUDA(cudaMalloc(&A->slots, (size_t)want * (size_t)slot_bytes_of(A)));
+        A->n_slots = want;
+    }
+    return 0;
+}
+
+// Uploads X_0 and the target, runs the initial-dt pass, stores X_0 in slot 0.
+int fwd_begin(lsh_adjoint* A, const double* const host_state[LSH_NVARS], const double* target) {
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    A->have_forward = false;
+    A->spine_stored = false;
+    A->cur_step = -1;
+    A->have_target = (target != nullptr) && A->ng > 0;
+    if (A->have_target)
+        A_CUDA(cudaMemcpyAsync(A->d_tgt, target, sizeof(double) * (size_t)A->nsteps * A->ng, cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < 7; ++k)
+        A_CUDA(cudaMemcpyAsync(A->X[k], host_state[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
+    lsh::TimeRec init{};
+    init.t_end = INFINITY;
+    A_CUDA(cudaMemcpyAsync(A->tm, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+    init_wave_pass(A, a, s);
+    k_cell_dt<<<cell_grid(A->p.nx, A->p.ny), cell_block(), 0, s>>>(a);
+    k_init_finish<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
+    k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts);
+    A_CUDA(cudaGetLastError());
+    A->stats = lsh_adjoint_stats{};
+    A->stats.slots = A->n_slots;
+    A->stats.nsteps = A->nsteps;
+    A->stats.slot_bytes = slot_bytes_of(A);
+    A->spine.clear();
+    Ops ops(A);
+    return ops.store(0);
+}
+
+// Step n -> n + 1 with its dt and gauge records.
+int fwd_record_step(lsh_adjoint* A, int n) {
+    cudaStream_t s = A->stream;
+    fwd_step(A, s);
+    k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts + n + 1);
+    if (A->ng > 0)
+        k_gauge_eta<<<(A->ng + 127) / 128, 128, 0, s>>>(A->X[0], A->X[3], A->X[6], A->d_gauges, A->ng,
+                                                       A->d_eta + (size_t)n * A->ng);
+    A->stats.forward_steps += 1;
+    A_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// After step N: the final depths (the projection at N reads them), then the
+// dt and gauge records into host memory.
+int fwd_end(lsh_adjoint* A) {
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    A_CUDA(cudaMemcpyAsync(A->hN[0], A->X[0], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    A_CUDA(cudaMemcpyAsync(A->hN[1], A->X[3], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    A->h_dts.resize(A->nsteps + 1);
+    A->h_eta.resize((size_t)A->nsteps * A->ng);
+    A_CUDA(cudaMemcpyAsync(A->h_dts.data(), A->d_dts, sizeof(double) * (A->nsteps + 1), cudaMemcpyDeviceToHost, s));
+    if (A->ng > 0)
+        A_CUDA(cudaMemcpyAsync(A->h_eta.data(), A->d_eta, sizeof(double) * A->h_eta.size(), cudaMemcpyDeviceToHost, s));
+    return 0;
+}
+
+// Waits for the forward run; the misfit and the gauge series.
+int fwd_host(lsh_adjoint* A, const double* target, double* misfit, double* gauge_series) {
+    A_CUDA(cudaStreamSynchronize(A->stream));
+    double J = 0.0;
+    if (A->have_target)
+        for (size_t i = 0; i < A->h_eta.size(); ++i) { const double d = A->h_eta[i] - target[i]; J = lshm::fmad(d, d, J); }
+    if (misfit) *misfit = J;
+    if (gauge_series && A->ng > 0) std::memcpy(gauge_series, A->h_eta.data(), sizeof(double) * A->h_eta.size());
+    A->have_forward = true;
+    A->spine_stored = true;
+    A->cur_step = A->nsteps;
+    return 0;
+}
+
+// The adjoint at X_N: the final state's cotangent (bar_final: 6 host arrays,
+// entries may be null), the misfit at N, the projection.
+int grad_begin(lsh_adjoint* A, double misfit_weight, const double* const bar_final[6]) {
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    A->misfit_weight = misfit_weight;
+    for (int k = 0; k < 6; ++k) {
+        if (bar_final && bar_final[k]) A_CUDA(cudaMemcpyAsync(A->Xb[k], bar_final[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
+        else A_CUDA(cudaMemsetAsync(A->Xb[k], 0, N * sizeof(double), s));
+    }
+    A_CUDA(cudaMemsetAsync(A->red, 0, sizeof(double) * kRed, s));
+    misfit_and_project(A, A->nsteps, A->hN[0], A->hN[1], s);
+    A->stats.recompute_steps = 0;
+    A->stats.reversed_steps = 0;
+    A->spine_stored = false;  // the sweep reuses the slots
+    A->cur_step = -1;
+    A_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// After the sweep (`cur`: the step of the state in X): the adjoint of dt_0
+// through the initial-dt pass of X_0, the misfit-free projection at X_0.
+int grad_tail(lsh_adjoint* A, int cur) {
+    cudaStream_t s = A->stream;
+    const size_t N = A->N;
+    if (cur != 0) {
+        Ops ops(A);
+        if (int st = ops.restore(0, 0)) return st;
+    }
+    A->cur_step = 0;
+    const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+    init_wave_pass(A, a, s);
+    const int G = A->grid;
+    cudaMemsetAsync(A->rmax, 0, sizeof(unsigned long long), s);
+    k_init_cell<<<1, 1, 0, s>>>(A->argmax);
+    k_adj_rate_max<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax);
+    k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
+    k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts, A->rsel);
+    AdjArgs aa = adj_args(A, A->X, nullptr, nullptr, nullptr, A->Xb, nullptr, nullptr, nullptr, A->h_dts[0]);
+    k_adj_init<<<1, 32, 0, s>>>(aa, A->rsel, A->part);
+    k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part, 1, A->red);
+    misfit_and_project(A, 0, A->X[0], A->X[3], s);
+    A_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// The state gradient (6 host arrays, entries may be null) and the reduced
+// dt and constant adjoints into host memory; returns after the copies.
+int grad_copy(lsh_adjoint* A, double* const grad_state[6]) {
+    cudaStream_t s = A->stream;
+    for (int k = 0; k < 6; ++k)
+        if (grad_state && grad_state[k])
+            A_CUDA(cudaMemcpyAsync(grad_state[k], A->Xb[k], A->N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    A_CUDA(cudaMemcpyAsync(A->h_red, A->red, sizeof(A->h_red), cudaMemcpyDeviceToHost, s));
+    A_CUDA(cudaStreamSynchronize(s));
+    return 0;
+}
+
+// d/d(angle1, mf0, mfs, r) from the constant adjoints.
+void grad_params_of(const lsh_adjoint* A, double gp[4]) {
+    const double* red = A->h_red;
+    ConstBar cb{red[1], red[2], red[3], red[4], red[5], red[6], red[7], red[8]};
+    lsh::param_grads(A->p.angle1, A->p.mf0, A->p.mfs, A->p.r, A->p.gravity, A->p.eps_h, A->p.L, A->p.H, cb, gp);
+}
+
+// The schedule's operations applied to every member in turn: one schedule,
+// one slot count, every member's state at the same step.
+struct BatchOps : lsh::RevolveOps {
+    std::vector<Ops> ops;
+    int advance(int from, int to) override {
+        for (int n = from; n < to; ++n)
+            for (auto& o : ops)
+                if (int st = o.advance(n, n + 1)) return st;
+        return 0;
+    }
+    int store(int k) override {
+        for (auto& o : ops)
+            if (int st = o.store(k)) return st;
+        return 0;
+    }
+    int restore(int k, int step) override {
+        for (auto& o : ops)
+            if (int st = o.restore(k, step)) return st;
+        return 0;
+    }
+    int reverse_step(int n) override {
+        for (auto& o : ops)
+            if (int st = o.reverse_step(n)) return st;
+        return 0;
+    }
+};
+
 }  // namespace
+
+struct lsh_adjoint_batch {
+    std::vector<lsh_adjoint*> m;
+    double budget = -1.0;  // < 0: 180 GB, capped by free memory at the forward run
+    int nsteps = 0;
+    int n_slots = 0;
+    bool have_forward = false;
+    lsh_adjoint_stats stats{};
+};
 
 // ------------------------------------------------------------------ C ABI
 
@@ -683,8 +917,7 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     return LSH_OK;
 }
 
-int lsh_adjoint_destroy(lsh_adjoint* A) {
-    if (!A) return LSH_OK;
+static void destroy_adjoint(lsh_adjoint* A) {
     if (A->stream) cudaStreamSynchronize(A->stream);
     cudaFree(A->slab);
     cudaFree(A->tm); cudaFree(A->rmax); cudaFree(A->argmax); cudaFree(A->rsel); cudaFree(A->part); cudaFree(A->part2); cudaFree(A->red);
@@ -693,6 +926,15 @@ int lsh_adjoint_destroy(lsh_adjoint* A) {
     if (A->stream) cudaStreamDestroy(A->stream);
     (void)cudaGetLastError();
     delete A;
+}
+
+int lsh_adjoint_destroy(lsh_adjoint* A) {
+    if (!A) return LSH_OK;
+    if (A->in_batch) {
+        lsh::set_last_error("lsh_adjoint_destroy: a batch member is destroyed with its batch");
+        return LSH_ERR_INVALID;
+    }
+    destroy_adjoint(A);
     return LSH_OK;
 }
 
@@ -713,104 +955,29 @@ int lsh_adjoint_forward(lsh_adjoint* A, const double* const host_state[LSH_NVARS
     if (!A || !host_state || nsteps < 1) return LSH_ERR_INVALID;
     for (int k = 0; k < LSH_NVARS; ++k) if (!host_state[k]) return LSH_ERR_INVALID;
     const auto t0 = std::chrono::steady_clock::now();
-    cudaStream_t s = A->stream;
-    const size_t N = A->N;
-    // (re)allocate the per-step records and the checkpoint slots
-    if (nsteps != A->nsteps) {
-        cudaFree(A->d_dts); cudaFree(A->d_eta); cudaFree(A->d_tgt);
-        A->d_dts = nullptr; A->d_eta = nullptr; A->d_tgt = nullptr;
-        A_CUDA(cudaMalloc(&A->d_dts, sizeof(double) * (nsteps + 1)));
-        if (A->ng > 0) {
-            A_CUDA(cudaMalloc(&A->d_eta, sizeof(double) * (size_t)nsteps * A->ng));
-            A_CUDA(cudaMalloc(&A->d_tgt, sizeof(double) * (size_t)nsteps * A->ng));
-        }
-        A->nsteps = nsteps;
-    }
-    const double slot_bytes = 6.0 * A->npad * sizeof(double);
-    int want = (int)std::min<double>((double)nsteps, std::floor(A->budget / slot_bytes));
+    int want = (int)std::min<double>((double)nsteps, std::floor(A->budget / slot_bytes_of(A)));
     if (want < 1) { lsh::set_last_error("lsh_adjoint: the checkpoint budget holds no state"); return LSH_ERR_INVALID; }
-    if (want != A->n_slots) {
-        cudaFree(A->slots);
-        A->slots = nullptr;
-        A->n_slots = 0;
-        cudaError_t e = cudaMalloc(&A->slots, (size_t)want * (size_t)slot_bytes);
-        while (e == cudaErrorMemoryAllocation && want > 1) {
-            (void)cudaGetLastError();
-            want = want / 2;
-            e = cudaMalloc(&A->slots, (size_t)want * (size_t)slot_bytes);
-        }
-        if (e != cudaSuccess) return afail(e, "cudaMalloc checkpoint slots");
-        A->n_slots = want;
+    int st = fwd_alloc(A, nsteps, want);
+    while (st == LSH_ERR_GPU_OOM && want > 1) {
+        want /= 2;
+        st = fwd_alloc(A, nsteps, want);
     }
-    A->have_target = (target != nullptr) && A->ng > 0;
-    if (A->have_target)
-        A_CUDA(cudaMemcpyAsync(A->d_tgt, target, sizeof(double) * (size_t)nsteps * A->ng, cudaMemcpyHostToDevice, s));
-    for (int k = 0; k < 7; ++k)
-        A_CUDA(cudaMemcpyAsync(A->X[k], host_state[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
-    // initial dt (the same kernels as lsh_set_state)
-    {
-        lsh::TimeRec init{};
-        init.t_end = INFINITY;
-        A_CUDA(cudaMemcpyAsync(A->tm, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-        const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
-        const int nx = A->p.nx, ny = A->p.ny;
-        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_cell_dt<<<cell_grid(A->p.nx, A->p.ny), cell_block(), 0, s>>>(a);
-        k_init_finish<<<1, 1, 0, s>>>(A->tm, 2.0 * A->c.cfl);
-        k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts);
-        A_CUDA(cudaGetLastError());
-        A_CUDA(cudaStreamSynchronize(s));
-    }
-    Ops ops(A);
-    A->stats = lsh_adjoint_stats{};
-    A->stats.slots = A->n_slots;
-    A->stats.nsteps = nsteps;
-    A->stats.slot_bytes = slot_bytes;
-    if (int st = ops.store(0)) return st;
-    A->spine.clear();
+    if (st) return st;
+    if ((st = fwd_begin(A, host_state, target))) return st;
     // the schedule's first descent, with the gauge series and dt records
-    int a = 0, free = A->n_slots - 1, slot = 0;
-    auto run = [&](int from, int to) {
-        for (int n = from; n < to; ++n) {
-            fwd_step(A, s);
-            k_record<<<1, 1, 0, s>>>(A->tm, A->d_dts + n + 1);
-            if (A->ng > 0)
-                k_gauge_eta<<<(A->ng + 127) / 128, 128, 0, s>>>(A->X[0], A->X[3], A->X[6], A->d_gauges, A->ng,
-                                                               A->d_eta + (size_t)n * A->ng);
-        }
-        A->stats.forward_steps += to - from;
-    };
-    while (nsteps - a > 1 && free > 0) {
-        const int m = a + (int)lsh::revolve_split(nsteps - a, free + 1);
-        run(a, m);
-        A_CUDA(cudaGetLastError());
-        ++slot;
-        if (int st = ops.store(slot)) return st;
+    Ops ops(A);
+    int a = 0, slot = 0;
+    for (const int m : spine_steps(nsteps, A->n_slots)) {
+        for (int n = a; n < m; ++n)
+            if ((st = fwd_record_step(A, n))) return st;
+        if ((st = ops.store(++slot))) return st;
         A->spine.push_back(m);
         a = m;
-        --free;
     }
-    run(a, nsteps);
-    A_CUDA(cudaMemcpyAsync(A->hN[0], A->X[0], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    A_CUDA(cudaMemcpyAsync(A->hN[1], A->X[3], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    A_CUDA(cudaGetLastError());
-    A->h_dts.resize(nsteps + 1);
-    A_CUDA(cudaMemcpyAsync(A->h_dts.data(), A->d_dts, sizeof(double) * (nsteps + 1), cudaMemcpyDeviceToHost, s));
-    std::vector<double> eta((size_t)nsteps * A->ng);
-    if (A->ng > 0)
-        A_CUDA(cudaMemcpyAsync(eta.data(), A->d_eta, sizeof(double) * eta.size(), cudaMemcpyDeviceToHost, s));
-    A_CUDA(cudaStreamSynchronize(s));
-    double J = 0.0;
-    if (A->have_target)
-        for (size_t i = 0; i < eta.size(); ++i) { const double d = eta[i] - target[i]; J = lshm::fmad(d, d, J); }
-    if (misfit) *misfit = J;
-    if (gauge_series && A->ng > 0) std::memcpy(gauge_series, eta.data(), sizeof(double) * eta.size());
-    A->have_forward = true;
-    A->spine_stored = true;
-    A->cur_step = nsteps;
+    for (int n = a; n < nsteps; ++n)
+        if ((st = fwd_record_step(A, n))) return st;
+    if ((st = fwd_end(A))) return st;
+    if ((st = fwd_host(A, target, misfit, gauge_series))) return st;
     A->stats.ms_forward = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return LSH_OK;
 }
@@ -819,56 +986,16 @@ int lsh_adjoint_gradient(lsh_adjoint* A, double misfit_weight, const double* con
                          double grad_params[4]) {
     if (!A || !A->have_forward) return LSH_ERR_INVALID;
     const auto t0 = std::chrono::steady_clock::now();
-    cudaStream_t s = A->stream;
-    const size_t N = A->N;
-    A->misfit_weight = misfit_weight;
-    for (int k = 0; k < 6; ++k) {
-        if (bar_final && bar_final[k]) A_CUDA(cudaMemcpyAsync(A->Xb[k], bar_final[k], N * sizeof(double), cudaMemcpyHostToDevice, s));
-        else A_CUDA(cudaMemsetAsync(A->Xb[k], 0, N * sizeof(double), s));
-    }
-    A_CUDA(cudaMemsetAsync(A->red, 0, sizeof(double) * kRed, s));
-    misfit_and_project(A, A->nsteps, A->hN[0], A->hN[1], s);
+    const bool pre = A->spine_stored;
     Ops ops(A);
     ops.cur = A->cur_step;
-    A->stats.recompute_steps = 0;
-    A->stats.reversed_steps = 0;
-    const bool pre = A->spine_stored;
-    A->spine_stored = false;  // the sweep below reuses the slots
-    A->cur_step = -1;
+    if (int st = grad_begin(A, misfit_weight, bar_final)) return st;
     if (int st = lsh::revolve_reverse(ops, 0, A->nsteps, 0, A->n_slots - 1, pre)) return st;
-    // dt_0 from the initial pass of X_0
-    {
-        if (ops.cur != 0) { if (int st = ops.restore(0, 0)) return st; ops.cur = 0; }
-        const KArgs a = fwd_args(A, A->X, nullptr, nullptr, A->acc1, nullptr, nullptr);
-        const int nx = A->p.nx, ny = A->p.ny;
-        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        const int G = A->grid;
-        cudaMemsetAsync(A->rmax, 0, sizeof(unsigned long long), s);
-        k_init_cell<<<1, 1, 0, s>>>(A->argmax);
-        k_adj_rate_max<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax);
-        k_adj_argmax<<<G, kCellBlock, 0, s>>>(A->acc1[6], A->geo, A->p.nx, (long long)N, A->rmax, A->argmax);
-        k_adj_ratebar<<<1, 1, 0, s>>>(A->rmax, A->argmax, A->red, A->d_dts, A->rsel);
-        AdjArgs aa = adj_args(A, A->X, nullptr, nullptr, nullptr, A->Xb, nullptr, nullptr, nullptr, A->h_dts[0]);
-        double* part = A->part;
-        k_adj_init<<<1, 32, 0, s>>>(aa, A->rsel, part);
-        k_adj_reduce<<<1, 32 * kRed, 0, s>>>(part, 1, A->red);
-        misfit_and_project(A, 0, A->X[0], A->X[3], s);
-    }
-    A_CUDA(cudaGetLastError());
-    for (int k = 0; k < 6; ++k)
-        if (grad_state && grad_state[k])
-            A_CUDA(cudaMemcpyAsync(grad_state[k], A->Xb[k], N * sizeof(double), cudaMemcpyDeviceToHost, s));
-    double red[kRed];
-    A_CUDA(cudaMemcpyAsync(red, A->red, sizeof(red), cudaMemcpyDeviceToHost, s));
-    A_CUDA(cudaStreamSynchronize(s));
-    ConstBar cb{red[1], red[2], red[3], red[4], red[5], red[6], red[7], red[8]};
+    if (int st = grad_tail(A, ops.cur)) return st;
+    if (int st = grad_copy(A, grad_state)) return st;
     double gp[4];
-    lsh::param_grads(A->p.angle1, A->p.mf0, A->p.mfs, A->p.r, A->p.gravity, A->p.eps_h, A->p.L, A->p.H, cb, gp);
+    grad_params_of(A, gp);
     if (grad_params) for (int k = 0; k < 4; ++k) grad_params[k] = gp[k];
-    A->cur_step = ops.cur;
     A->stats.ms_gradient = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return LSH_OK;
 }
@@ -941,6 +1068,178 @@ int lsh_revolve_plan(int nsteps, int slots, long long* forward_steps, long long*
     if (c.bad || c.next != -1) return LSH_ERR_INVALID;
     if (forward_steps) *forward_steps = descent + c.fw;
     if (optimal) *optimal = lsh::revolve_cost(nsteps, slots);
+    return LSH_OK;
+}
+
+// ------------------------------------------------------------------ batch
+
+int lsh_adjoint_batch_create(int n, const lsh_params* params, const int* n_gauges, const int* const* gauge_cells,
+                             int device, lsh_adjoint_batch** out) {
+    if (!out || n < 1 || !params) return LSH_ERR_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        const int ng = n_gauges ? n_gauges[i] : 0;
+        if (ng < 0 || (ng > 0 && (!gauge_cells || !gauge_cells[i]))) {
+            lsh::set_last_error("lsh_adjoint_batch_create: member " + std::to_string(i) + ": gauges");
+            return LSH_ERR_INVALID;
+        }
+        if (const char* why = lsh::params_problem(&params[i])) {
+            lsh::set_last_error("lsh_adjoint_batch_create: member " + std::to_string(i) + ": " + why);
+            return LSH_ERR_INVALID;
+        }
+    }
+    lsh_adjoint_batch* B = new (std::nothrow) lsh_adjoint_batch();
+    if (!B) return LSH_ERR_HOST_OOM;
+    for (int i = 0; i < n; ++i) {
+        lsh_adjoint* A = nullptr;
+        const int ng = n_gauges ? n_gauges[i] : 0;
+        const int st = lsh_adjoint_create(&params[i], device, ng, ng > 0 ? gauge_cells[i] : nullptr, &A);
+        if (st != LSH_OK) {
+            lsh_adjoint_batch_destroy(B);
+            return st;
+        }
+        A->in_batch = true;
+        A->budget = 0.0;  // until the batch's forward run sets the slot count
+        B->m.push_back(A);
+    }
+    *out = B;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_destroy(lsh_adjoint_batch* B) {
+    if (!B) return LSH_OK;
+    for (lsh_adjoint* A : B->m) destroy_adjoint(A);
+    delete B;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_set_thin_layer(lsh_adjoint_batch* B, double h_adj) {
+    if (!B || !(h_adj >= 0.0)) return LSH_ERR_INVALID;
+    for (lsh_adjoint* A : B->m) A->h_adj = h_adj;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_set_budget(lsh_adjoint_batch* B, double bytes) {
+    if (!B || !(bytes >= 0.0)) return LSH_ERR_INVALID;
+    B->budget = bytes;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_forward(lsh_adjoint_batch* B, const double* const* host_states, int nsteps,
+                              const double* const* targets, double* misfits, double* const* gauge_series) {
+    if (!B || !host_states || nsteps < 1) return LSH_ERR_INVALID;
+    const int n = (int)B->m.size();
+    for (int i = 0; i < n * LSH_NVARS; ++i) if (!host_states[i]) return LSH_ERR_INVALID;
+    const auto t0 = std::chrono::steady_clock::now();
+    B->have_forward = false;
+    // one slot count for all: with a common step count, equal counts
+    // minimise the members' summed recomputation under a joint budget
+    double per_slot = 0.0;
+    for (lsh_adjoint* A : B->m) per_slot += slot_bytes_of(A);
+    double budget = B->budget;
+    if (budget < 0.0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = std::min(180e9, std::max(0.0, (double)fr - 4e9));
+    }
+    int want = (int)std::min<double>((double)nsteps, std::floor(budget / per_slot));
+    if (want < 1) { lsh::set_last_error("lsh_adjoint_batch: the checkpoint budget holds no batch state"); return LSH_ERR_INVALID; }
+    for (;;) {
+        int st = 0;
+        for (lsh_adjoint* A : B->m)
+            if ((st = fwd_alloc(A, nsteps, want))) break;
+        if (st == 0) break;
+        if (st != LSH_ERR_GPU_OOM || want == 1) return st;
+        for (lsh_adjoint* A : B->m) { cudaFree(A->slots); A->slots = nullptr; A->n_slots = 0; }
+        want /= 2;
+    }
+    B->nsteps = nsteps;
+    B->n_slots = want;
+    // a member run on its own keeps the batch's slot count
+    for (lsh_adjoint* A : B->m) A->budget = want * slot_bytes_of(A);
+    for (int i = 0; i < n; ++i)
+        if (int st = fwd_begin(B->m[i], host_states + (size_t)i * LSH_NVARS, targets ? targets[i] : nullptr)) return st;
+    BatchOps ops;
+    for (lsh_adjoint* A : B->m) ops.ops.emplace_back(A);
+    int a = 0, slot = 0;
+    auto run = [&](int to) -> int {
+        for (int s = a; s < to; ++s)
+            for (lsh_adjoint* A : B->m)
+                if (int st = fwd_record_step(A, s)) return st;
+        return 0;
+    };
+    const std::vector<int> spine = spine_steps(nsteps, want);
+    for (const int m : spine) {
+        if (int st = run(m)) return st;
+        if (int st = ops.store(++slot)) return st;
+        a = m;
+    }
+    if (int st = run(nsteps)) return st;
+    for (lsh_adjoint* A : B->m) if (int st = fwd_end(A)) return st;
+    for (int i = 0; i < n; ++i) {
+        lsh_adjoint* A = B->m[i];
+        A->spine = spine;
+        if (int st = fwd_host(A, targets ? targets[i] : nullptr, misfits ? misfits + i : nullptr,
+                              gauge_series ? gauge_series[i] : nullptr))
+            return st;
+    }
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    B->stats = lsh_adjoint_stats{};
+    B->stats.slots = want;
+    B->stats.nsteps = nsteps;
+    B->stats.forward_steps = B->m[0]->stats.forward_steps;
+    B->stats.ms_forward = ms;
+    B->stats.slot_bytes = per_slot;
+    for (lsh_adjoint* A : B->m) A->stats.ms_forward = ms;
+    B->have_forward = true;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_gradient(lsh_adjoint_batch* B, const double* misfit_weights, double* const* grad_states,
+                               double* grad_params) {
+    if (!B || !B->have_forward) return LSH_ERR_INVALID;
+    const int n = (int)B->m.size();
+    // the members must still hold the batch's run: same steps, slots and step
+    const lsh_adjoint* A0 = B->m[0];
+    for (lsh_adjoint* A : B->m)
+        if (!A->have_forward || A->nsteps != B->nsteps || A->n_slots != B->n_slots || A->cur_step != A0->cur_step ||
+            A->spine_stored != A0->spine_stored) {
+            lsh::set_last_error("lsh_adjoint_batch_gradient: a member was run on its own since the batch's forward run");
+            return LSH_ERR_INVALID;
+        }
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool pre = A0->spine_stored;
+    BatchOps ops;
+    for (lsh_adjoint* A : B->m) ops.ops.emplace_back(A);
+    ops.cur = A0->cur_step;
+    for (int i = 0; i < n; ++i)
+        if (int st = grad_begin(B->m[i], misfit_weights ? misfit_weights[i] : 1.0, nullptr)) return st;
+    if (int st = lsh::revolve_reverse(ops, 0, B->nsteps, 0, B->n_slots - 1, pre)) return st;
+    for (lsh_adjoint* A : B->m) if (int st = grad_tail(A, ops.cur)) return st;
+    for (int i = 0; i < n; ++i) {
+        lsh_adjoint* A = B->m[i];
+        if (int st = grad_copy(A, grad_states ? grad_states + (size_t)i * 6 : nullptr)) return st;
+        double gp[4];
+        grad_params_of(A, gp);
+        if (grad_params) for (int k = 0; k < 4; ++k) grad_params[(size_t)i * 4 + k] = gp[k];
+    }
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    B->stats.recompute_steps = B->m[0]->stats.recompute_steps;
+    B->stats.reversed_steps = B->m[0]->stats.reversed_steps;
+    B->stats.ms_gradient = ms;
+    for (lsh_adjoint* A : B->m) A->stats.ms_gradient = ms;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_get_stats(lsh_adjoint_batch* B, lsh_adjoint_stats* out) {
+    if (!B || !out) return LSH_ERR_INVALID;
+    *out = B->stats;
+    return LSH_OK;
+}
+
+int lsh_adjoint_batch_member(lsh_adjoint_batch* B, int i, lsh_adjoint** out) {
+    if (!B || !out || i < 0 || i >= (int)B->m.size()) return LSH_ERR_INVALID;
+    *out = B->m[i];
     return LSH_OK;
 }
 

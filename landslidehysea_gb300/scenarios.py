@@ -197,3 +197,30 @@ def ensemble(count=256, seed0=0, sizes=ENSEMBLE_SIZES, order=2, cfl=0.5, ids=Non
     only those members."""
     ks = range(count) if ids is None else ids
     return [ensemble_member(k, seed0, sizes, order, cfl) for k in ks]
+
+
+CALIBRATION_SIZES = (256, 512, 768, 1024)
+
+
+def calibration_member(k, seed0=0, sizes=CALIBRATION_SIZES, order=2):
+    """Scenario k of a batched calibration: the fjord generator with seed
+    seed0 + k on a grid drawn uniformly from `sizes`, plus its twin's
+    parameters (Coulomb angle, Manning coefficients and density ratio
+    scaled by seeded +-5%), whose gauge series is the calibration target.
+    Returns (scenario, twin parameters)."""
+    import copy
+    rng = np.random.default_rng(2_000_003 + seed0 + k)
+    n = int(sizes[int(rng.integers(0, len(sizes)))])
+    sc = fjord(n=n, seed=seed0 + k, order=order)
+    f = 1.0 + 0.05 * rng.choice([-1.0, 1.0], 4)
+    twin = copy.copy(sc.params)
+    p = sc.params
+    twin.angle1, twin.mf0, twin.mfs, twin.r = p.angle1 * f[0], p.mf0 * f[1], p.mfs * f[2], p.r * f[3]
+    return sc, twin
+
+
+def gauge_cells(sc):
+    """Flat cell indices of a scenario's gauges that lie on the grid."""
+    p = sc.params
+    return np.array([int(j) * p.nx + int(i) for i, j in sc.gauges if i >= 0 and j >= 0], dtype=np.int32)
+

@@ -72,6 +72,14 @@ SIGNATURES = {
     "lsh_adjoint_get_stats": (ctypes.c_int, [P, P]),
     "lsh_adjoint_get_times": (ctypes.c_int, [P, DP]),
     "lsh_adjoint_get_state": (ctypes.c_int, [P, P]),
+    "lsh_adjoint_batch_create": (ctypes.c_int, [ctypes.c_int, P, P, P, ctypes.c_int, ctypes.POINTER(P)]),
+    "lsh_adjoint_batch_destroy": (ctypes.c_int, [P]),
+    "lsh_adjoint_batch_set_thin_layer": (ctypes.c_int, [P, ctypes.c_double]),
+    "lsh_adjoint_batch_set_budget": (ctypes.c_int, [P, ctypes.c_double]),
+    "lsh_adjoint_batch_forward": (ctypes.c_int, [P, P, ctypes.c_int, P, DP, P]),
+    "lsh_adjoint_batch_gradient": (ctypes.c_int, [P, P, P, P]),
+    "lsh_adjoint_batch_get_stats": (ctypes.c_int, [P, P]),
+    "lsh_adjoint_batch_member": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(P)]),
     "lsh_revolve_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -103,6 +111,12 @@ def _check(status, what):
 
 def _ptr_array(ptrs):
     return (ctypes.c_void_p * LSH_NVARS)(*ptrs)
+
+
+def _ptrs(ptrs):
+    """A C array of pointers of any length (0 entries are NULL)."""
+    ptrs = list(ptrs)
+    return (ctypes.c_void_p * max(1, len(ptrs)))(*[p or None for p in ptrs])
 
 
 def device_available():
@@ -321,20 +335,27 @@ class Adjoint:
     w * sum_n sum_g (eta1_n[g] - target)^2 + <bar_final, X_N> with respect to
     the initial h1..q2y and to (angle1, mf0, mfs, r)."""
 
-    def __init__(self, params, gauges=(), device: int = 0):
+    def __init__(self, params, gauges=(), device: int = 0, _member=None):
         self.lib = load()
         self.params = params.copy()
         self.gauges = np.ascontiguousarray(np.asarray(gauges, dtype=np.int32).reshape(-1))
         self._a = ctypes.c_void_p()
+        self._owner = None
+        self.nsteps = 0
+        if _member is not None:
+            # a member of an AdjointBatch: owned (and destroyed) by it
+            self._owner, handle = _member
+            self._a = ctypes.c_void_p(handle)
+            return
         g = self.gauges.ctypes.data if self.gauges.size else None
         _check(self.lib.lsh_adjoint_create(ctypes.byref(self.params), int(device), int(self.gauges.size), g,
                                            ctypes.byref(self._a)), "lsh_adjoint_create")
-        self.nsteps = 0
 
     def close(self):
-        if self._a:
+        if self._a and self._owner is None:
             self.lib.lsh_adjoint_destroy(self._a)
-            self._a = ctypes.c_void_p()
+        self._a = ctypes.c_void_p()
+        self._owner = None
 
     def __del__(self):
         try:
@@ -408,6 +429,112 @@ class Adjoint:
         return st.as_dict()
 
 
+class AdjointBatch:
+    """Batched adjoint (wraps lsh_adjoint_batch): scenarios on uneven grids run
+    forward and reversed together under one checkpoint schedule and a joint
+    memory budget; each member's results equal its own Adjoint's."""
+
+    def __init__(self, params_list, gauges_list=None, device: int = 0):
+        self.lib = load()
+        n = len(params_list)
+        self.params = [p.copy() for p in params_list]
+        gl = gauges_list if gauges_list is not None else [()] * n
+        if len(gl) != n:
+            raise ValueError("one gauge list per scenario")
+        self.gauges = [np.ascontiguousarray(np.asarray(g, dtype=np.int32).reshape(-1)) for g in gl]
+        arr = (LshParams * n)(*self.params)
+        ng = np.array([g.size for g in self.gauges], dtype=np.int32)
+        gp = _ptrs([g.ctypes.data if g.size else 0 for g in self.gauges])
+        self._b = ctypes.c_void_p()
+        _check(self.lib.lsh_adjoint_batch_create(n, ctypes.cast(arr, P), ng.ctypes.data, gp, int(device),
+                                                 ctypes.byref(self._b)), "lsh_adjoint_batch_create")
+        self.n = n
+        self.nsteps = 0
+        self._members = {}
+
+    def close(self):
+        if self._b:
+            for m in self._members.values():
+                m._a = ctypes.c_void_p()
+                m._owner = None
+            self._members = {}
+            self.lib.lsh_adjoint_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_thin_layer(self, h_adj):
+        _check(self.lib.lsh_adjoint_batch_set_thin_layer(self._b, float(h_adj)), "lsh_adjoint_batch_set_thin_layer")
+
+    def set_budget(self, nbytes):
+        """Device bytes all members' checkpoint slots may take together."""
+        _check(self.lib.lsh_adjoint_batch_set_budget(self._b, float(nbytes)), "lsh_adjoint_batch_set_budget")
+
+    def forward(self, states, nsteps, targets=None):
+        """Run `nsteps` from each member's state; returns (misfits [n], list of eta series [nsteps, n_gauges_i])."""
+        if len(states) != self.n:
+            raise ValueError("one state per scenario")
+        arrs = []
+        for st in states:
+            arrs += [np.ascontiguousarray(st[v] if isinstance(st, dict) else st[i], dtype=np.float64).reshape(-1)
+                     for i, v in enumerate(VARS)]
+        tg = None
+        tl = None
+        if targets is not None:
+            tl = [None if t is None else np.ascontiguousarray(t, dtype=np.float64).reshape(nsteps, g.size)
+                  for t, g in zip(targets, self.gauges)]
+            tg = _ptrs([0 if t is None else t.ctypes.data for t in tl])
+        series = [np.zeros((nsteps, g.size)) for g in self.gauges]
+        misfits = np.zeros(self.n)
+        self._keep = (arrs, tl, series)
+        _check(self.lib.lsh_adjoint_batch_forward(self._b, _ptrs([a.ctypes.data for a in arrs]), int(nsteps), tg,
+                                                  misfits.ctypes.data_as(DP),
+                                                  _ptrs([s.ctypes.data if s.size else 0 for s in series])),
+               "lsh_adjoint_batch_forward")
+        self.nsteps = nsteps
+        return misfits, series
+
+    def gradient(self, misfit_weights=None, want_state=True):
+        """Returns (list of dicts h1..q2y -> (ny, nx) or None, list of dicts angle1, mf0, mfs, r)."""
+        w = None
+        if misfit_weights is not None:
+            w = np.ascontiguousarray(misfit_weights, dtype=np.float64).reshape(self.n)
+        outs = None
+        gs = None
+        if want_state:
+            outs = [{v: np.zeros((p.ny, p.nx)) for v in VARS[:6]} for p in self.params]
+            gs = _ptrs([o[v].ctypes.data for o in outs for v in VARS[:6]])
+        gp = np.zeros((self.n, 4))
+        _check(self.lib.lsh_adjoint_batch_gradient(self._b, w.ctypes.data if w is not None else None, gs,
+                                                   gp.ctypes.data), "lsh_adjoint_batch_gradient")
+        return (outs if outs is not None else [None] * self.n), [dict(zip(PARAM_NAMES, r.tolist())) for r in gp]
+
+    def stats(self):
+        st = AdjointStats()
+        _check(self.lib.lsh_adjoint_batch_get_stats(self._b, ctypes.byref(st)), "lsh_adjoint_batch_get_stats")
+        return st.as_dict()
+
+    def member(self, i):
+        """Member i as an Adjoint owned by this batch (run on its own with the batch's slot count)."""
+        if i not in self._members:
+            h = ctypes.c_void_p()
+            _check(self.lib.lsh_adjoint_batch_member(self._b, int(i), ctypes.byref(h)), "lsh_adjoint_batch_member")
+            m = Adjoint(self.params[i], self.gauges[i], _member=(self, h.value))
+            m.nsteps = self.nsteps
+            self._members[i] = m
+        return self._members[i]
+
+
 def revolve_plan(nsteps, slots):
     """(forward steps of the checkpoint schedule, optimal recomputation count),
     or raises if the schedule does not reverse every step once, in order."""
@@ -416,4 +543,4 @@ def revolve_plan(nsteps, slots):
     return fw.value, opt.value
 
 
-__all__ = ["Solver", "Batch", "Tune", "Adjoint", "revolve_plan", "LshError", "load", "device_available", "SIGNATURES", "_abi"]
+__all__ = ["Solver", "Batch", "Tune", "Adjoint", "AdjointBatch", "revolve_plan", "LshError", "load", "device_available", "SIGNATURES", "_abi"]

@@ -65,6 +65,24 @@ def test_batch_and_adjoint_reject_bad_input(lib):
     assert lib.lsh_adjoint_create(ctypes.byref(good), 0, 1, None, ctypes.byref(a)) == LSH_ERR_INVALID
 
 
+def test_adjoint_batch_rejects_bad_input(lib):
+    good = default_params(8, 6, dx=10.0, dy=10.0)
+    bad = _bad_params()["r1"]
+    b = ctypes.c_void_p()
+    arr = (type(good) * 2)(good, bad)
+    assert lib.lsh_adjoint_batch_create(2, arr, None, None, 0, ctypes.byref(b)) == LSH_ERR_INVALID
+    assert b"member 1" in lib.lsh_last_error()
+    assert not b
+    arr = (type(good) * 2)(good, good)
+    ng = (ctypes.c_int * 2)(0, 1)
+    assert lib.lsh_adjoint_batch_create(2, arr, ng, None, 0, ctypes.byref(b)) == LSH_ERR_INVALID
+    assert lib.lsh_adjoint_batch_create(0, arr, None, None, 0, ctypes.byref(b)) == LSH_ERR_INVALID
+    assert lib.lsh_adjoint_batch_forward(None, None, 3, None, None, None) == LSH_ERR_INVALID
+    assert lib.lsh_adjoint_batch_gradient(None, None, None, None) == LSH_ERR_INVALID
+    assert lib.lsh_adjoint_batch_set_budget(None, 1.0) == LSH_ERR_INVALID
+    assert lib.lsh_adjoint_batch_destroy(None) == 0
+
+
 def test_no_alloc_entry_rejects_oversize_and_second_order(lib):
     t, dt = ctypes.c_double(0.0), ctypes.c_double(0.1)
     fake = (ctypes.c_void_p * 7)(*([1] * 7))  # never dereferenced: rejected before any device work
