@@ -67,12 +67,67 @@ LSH_HD double rint_even(double x) {
 #endif
 }
 
+// The two 32-bit halves of x.  On the device through a PTX move, which the
+// compiler cannot see through: an integer test on the bits that is
+// equivalent to a floating-point compare (x == 0, !isfinite(x)) would
+// otherwise be folded back into an FP64 compare.
+LSH_HD void halves(double x, uint32_t& lo, uint32_t& hi) {
+#if defined(__CUDA_ARCH__)
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+#else
+    const uint64_t u = bits_of(x);
+    lo = (uint32_t)u;
+    hi = (uint32_t)(u >> 32);
+#endif
+}
+
 // 2^k for -1022 <= k <= 1023
 LSH_HD double pow2i(int k) { return from_bits((uint64_t)(k + 1023) << 52); }
 
+// ---- comparisons on the integer pipe
+//
+// The GPU's FP64 unit takes one warp instruction per 16 cycles per SM, and a
+// double compare occupies it like an add.  These forms compare bit patterns
+// on the integer ALUs instead.  For operands that are not NaN each returns
+// exactly what the IEEE comparison returns (-0 == +0), so they are exact
+// restatements of the compares they replace.
+
+constexpr uint64_t kMag = 0x7fffffffffffffffULL;
+
+// x > 0
+LSH_HD bool gt0(double x) { return (int64_t)bits_of(x) > 0; }
+// x < 0
+LSH_HD bool lt0(double x) {
+    const uint64_t u = bits_of(x);
+    return (int64_t)u < 0 && (u << 1) != 0;
+}
+// x < c and x > c for a constant c > 0: doubles >= -0 order like their
+// patterns, and every negative pattern (-0 included) is below c's
+LSH_HD bool lt_pos(double x, double c) { return (int64_t)bits_of(x) < (int64_t)bits_of(c); }
+LSH_HD bool gt_pos(double x, double c) { return (int64_t)bits_of(x) > (int64_t)bits_of(c); }
+// |x| by clearing the sign bit (integer pipe): the bits fabs gives.  A
+// fabs whose result feeds an integer-pipe compare would otherwise be
+// materialised by an FP64 instruction.
+LSH_HD double abs_bits(double x) { return from_bits(bits_of(x) & kMag); }
+// |a| < |b|
+LSH_HD bool abs_lt(double a, double b) { return (bits_of(a) & kMag) < (bits_of(b) & kMag); }
+// a key ordered like the doubles, -0 and +0 both 0: the magnitude, negated
+// for a negative value
+LSH_HD int64_t okey(double x) {
+    const int64_t k = (int64_t)bits_of(x);
+    return (k < 0) ? -(k & (int64_t)kMag) : k;
+}
+// a < b, any non-NaN a and b
+LSH_HD bool lt(double a, double b) { return okey(a) < okey(b); }
+
+constexpr int64_t kInfBits = 0x7ff0000000000000LL;  // +inf; positive NaNs lie above
+
 LSH_HD double exp_neg(double x) {
-    if (x < 0x1p-54) return (x == x) ? 1.0 : x;  // NaN stays NaN
-    if (x > 746.0) return 0.0;
+    // the range tests on the integer pipe: x < 2^-54 (negative x, -0 and
+    // negative NaNs included), then 746 < x <= +inf; NaN stays NaN
+    const int64_t k0 = (int64_t)bits_of(x);
+    if (k0 < (int64_t)bits_of(0x1p-54)) return (k0 & (int64_t)kMag) > kInfBits ? x : 1.0;
+    if (k0 > (int64_t)bits_of(746.0) && k0 <= kInfBits) return 0.0;
     const double inv_ln2 = 1.4426950408889634074;
     const double ln2_hi = 6.93147180369123816490e-01;  // 0x3fe62e42fee00000: low 32 bits zero
     const double ln2_lo = 1.90821492927058770002e-10;
@@ -100,16 +155,18 @@ LSH_HD double exp_neg(double x) {
 }
 
 LSH_HD double cbrt_pos(double x) {
-    if (!(x > 0.0)) return x;  // 0 -> 0, NaN -> NaN
-    if (x == INFINITY) return x;
+    // the range tests on the integer pipe: 0 < x < +inf goes on, anything
+    // else (0, +inf, NaN, negative) comes back as it is
+    const int64_t kx = (int64_t)bits_of(x);
+    if (!(kx > 0 && kx < kInfBits)) return x;
     int scale = 0;
-    if (x < 0x1p-1000) { x *= 0x1p300; scale = -100; }  // keep the exponent normal
+    if (kx < (int64_t)bits_of(0x1p-1000)) { x *= 0x1p300; scale = -100; }  // keep the exponent normal
     const uint64_t u = bits_of(x);
     const int e = (int)((u >> 52) & 0x7ff) - 1023;
     const double m = from_bits((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);  // [1, 2)
     int q = e / 3, rem = e - 3 * q;
     if (rem < 0) { rem += 3; q -= 1; }
-    const double a = m * (double)(1 << rem);  // [1, 8)
+    const double a = m * pow2i(rem);  // [1, 8)
     double z = fmad(fmad(0.0115, a, -0.1656), a, 1.1098);
     const double third = 1.0 / 3.0;
     for (int i = 0; i < 5; ++i) {

@@ -113,7 +113,7 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
     else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
     // dry edge (Arista_kernel.cu:397): nothing to add; the first pass still
     // writes the zeros that initialise the accumulators
-    if (!((0.5 * (e.A.h1 + e.B.h1) >= lsh::kEps) || (0.5 * (e.A.h2 + e.B.h2) >= lsh::kEps))) {
+    if (lshm::lt_pos(0.5 * (e.A.h1 + e.B.h1), lsh::kEps) && lshm::lt_pos(0.5 * (e.A.h2 + e.B.h2), lsh::kEps)) {
         if (FIRST) {
 #pragma unroll
             for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
@@ -196,10 +196,16 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
     }
 }
 
+// minmod: the operand of smaller magnitude when both are nonzero with one
+// sign (b on a tie), else 0 -- on the bit patterns (integer pipe); for
+// operands that are not NaN the same as the compares
+//   a > 0 && b > 0 ? (a < b ? a : b) : a < 0 && b < 0 ? (a > b ? a : b) : 0
 LSH_HD double minmod(double a, double b) {
-    if (a > 0.0 && b > 0.0) return (a < b) ? a : b;
-    if (a < 0.0 && b < 0.0) return (a > b) ? a : b;
-    return 0.0;
+    const uint64_t ua = lshm::bits_of(a), ub = lshm::bits_of(b);
+    const bool nonzero = ((ua << 1) != 0) && ((ub << 1) != 0);
+    const bool same = ((ua ^ ub) >> 63) == 0;
+    if (!(nonzero && same)) return 0.0;
+    return ((ua & lshm::kMag) < (ub & lshm::kMag)) ? a : b;
 }
 
 LSH_HD double recon_var(const KArgs& a, int id, int k) {
@@ -246,9 +252,12 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
     // first order where a reconstructed depth would fall below kReconThin of
     // the cell's: a thin face with a finite discharge has an unbounded
     // velocity, whose wave speed would collapse dt
+    // (the compares on the integer pipe)
     const double g1 = kReconThin * h1, g2 = kReconThin * h2;
-    const bool bad = (h1 + dh1x < g1) || (h1 - dh1x < g1) || (h2 + dh2x < g2) || (h2 - dh2x < g2) ||
-                     (h1 + dh1y < g1) || (h1 - dh1y < g1) || (h2 + dh2y < g2) || (h2 - dh2y < g2);
+    using lshm::okey;
+    const int64_t k1 = okey(g1), k2 = okey(g2);
+    const bool bad = okey(h1 + dh1x) < k1 || okey(h1 - dh1x) < k1 || okey(h2 + dh2x) < k2 || okey(h2 - dh2x) < k2 ||
+                     okey(h1 + dh1y) < k1 || okey(h1 - dh1y) < k1 || okey(h2 + dh2y) < k2 || okey(h2 - dh2y) < k2;
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
         a.sxw[k][id] = bad ? 0.0 : sx[k];
@@ -301,7 +310,7 @@ LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
     if (MODE != 2 && a.c.track_eta) {
         // actualizarEta1MaximaGPU (Volumen_kernel.cu:182-213): state before the step
         const double v = wo[0] - a.W[6][id];
-        if (v > a.eta_max[id]) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
+        if (lshm::lt(a.eta_max[id], v)) { a.eta_max[id] = v; a.eta_time[id] = a.tm->t; }
     }
     // a dry, still cell with nothing flowing in maps to itself through the
     // whole update (dt contribution 1e30; its second-order pressure

@@ -74,43 +74,68 @@ struct TimeRec {
 
 struct V4 { double x, y, z, w; };
 
-LSH_HD double tmin(double a, double b) { return (b < a) ? b : a; }
-LSH_HD double tmax(double a, double b) { return (b > a) ? b : a; }
-LSH_HD double max0(double a) { return (a > 0.0) ? a : 0.0; }
+// Compares run on the integer pipe (lsh_fpmath.h: exact for non-NaN
+// operands): lt_pos / gt_pos against the positive thresholds EPSILON, eps_h,
+// vmax, lt / okey for operands of either sign.
+using lshm::abs_bits;
+using lshm::abs_lt;
+using lshm::gt0;
+using lshm::gt_pos;
+using lshm::lt;
+using lshm::lt0;
+using lshm::lt_pos;
+using lshm::okey;
+
+LSH_HD double tmin(double a, double b) { return lt(b, a) ? b : a; }
+LSH_HD double tmax(double a, double b) { return lt(a, b) ? b : a; }
+LSH_HD double max0(double a) { return gt0(a) ? a : 0.0; }
 LSH_HD double fmad(double a, double b, double c) { return lshm::fmad(a, b, c); }
 LSH_HD double exp_neg(double x) { return lshm::exp_neg(x); }
 
 // sqrt(2) h / sqrt(h^4 + max(h, eps_h)^4); exactly 1/h for h > eps_h
 LSH_HD double vfac(double h, double eps_h) {
-    if (h > eps_h) return 1.0 / h;
+    if (gt_pos(h, eps_h)) return 1.0 / h;
     const double h2 = h * h, m2 = eps_h * eps_h;
     return (kSqrt2 * h) / sqrt(fmad(h2, h2, m2 * m2));
 }
 
 LSH_HD double pow43(double h) { return h * lshm::cbrt_pos(h); }
 
-LSH_HD int sgn(double x) { return (fabs(x) < kEps) ? 0 : ((x > 0) ? 1 : -1); }
+LSH_HD int sgn(double x) { return abs_lt(x, kEps) ? 0 : (gt0(x) ? 1 : -1); }
 
 // x == +0 or -0, by bit pattern (integer pipe)
-LSH_HD bool is_zero(double x) { return (lshm::bits_of(x) << 1) == 0; }
+LSH_HD bool is_zero(double x) {
+    uint32_t lo, hi;
+    lshm::halves(x, lo, hi);
+    return ((hi << 1) | lo) == 0u;
+}
 
+// NaN or Inf, by the exponent bits (integer pipe)
 LSH_HD bool is_bad(double x) {
-    // NaN or Inf by bit pattern (integer pipe, no FP64 compare)
-    return (lshm::bits_of(x) & 0x7ff0000000000000ULL) == 0x7ff0000000000000ULL;
+    uint32_t lo, hi;
+    lshm::halves(x, lo, hi);
+    return (hi & 0x7ff00000u) == 0x7ff00000u;
 }
 
 // Compare-and-swap sequence of Arista_kernel.cu:193-234 (with its (2,1)
 // compare) or, with `full`, the same sequence made a true sort.
+// The compares run on ordered keys (okey), which travel with the values.
+LSH_HD void cswap(double& a, double& b, int64_t& ka, int64_t& kb) {
+    if (ka > kb) {
+        const double t = a; a = b; b = t;
+        const int64_t k = ka; ka = kb; kb = k;
+    }
+}
 LSH_HD void sort_eig(V4& D, int full) {
-    double t;
-    if (D.x > D.y) { t = D.y; D.y = D.x; D.x = t; }
-    if (D.x > D.z) { t = D.z; D.z = D.x; D.x = t; }
-    if (D.x > D.w) { t = D.w; D.w = D.x; D.x = t; }
-    if (D.y > D.z) { t = D.z; D.z = D.y; D.y = t; }
-    if (D.y > D.w) { t = D.w; D.w = D.y; D.y = t; }
-    if (full) { if (D.y > D.z) { t = D.z; D.z = D.y; D.y = t; } }
-    else if (D.z > D.y) { t = D.y; D.y = D.z; D.z = t; }
-    if (D.z > D.w) { t = D.w; D.w = D.z; D.z = t; }
+    int64_t kx = okey(D.x), ky = okey(D.y), kz = okey(D.z), kw = okey(D.w);
+    cswap(D.x, D.y, kx, ky);
+    cswap(D.x, D.z, kx, kz);
+    cswap(D.x, D.w, kx, kw);
+    cswap(D.y, D.z, ky, kz);
+    cswap(D.y, D.w, ky, kw);
+    if (full) cswap(D.y, D.z, ky, kz);
+    else cswap(D.z, D.y, kz, ky);
+    cswap(D.z, D.w, kz, kw);
 }
 
 // aproximarAutovalores1D (Arista_kernel.cu:152-237).  L2 == false: the
@@ -121,16 +146,16 @@ LSH_HD V4 eig(double h1, double h2, double u1, double u2, double q, const Consts
                                   double Fknown = -1.0, double sqrt_h = -1.0) {
     const double h = L2 ? h1 + h2 : h1;
     // single layer: vfac(h1 + 0) is vfac(h1), which the caller may already hold
-    const double F = (!L2 && Fknown >= 0.0) ? Fknown : vfac(h, c.eps_h);
+    const double F = (!L2 && !lt0(Fknown)) ? Fknown : vfac(h, c.eps_h);
     const double u = q * F;
     // sqrt_h >= 0: sqrt(h1) is known and h2 == 0, so sqrt(g h) = sqrt(g) sqrt(h1)
-    const double cg = (sqrt_h >= 0.0) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
+    const double cg = !lt0(sqrt_h) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     double uu = 0.0, ci = 0.0;
     if (L2) {
         uu = fmad(u1, h2, u2 * h1) * F;
         const double d = u1 - u2;
         const double aux = fmad(-((d * d) * F), c.inv_gp, 1.0);
-        ci = sqrt((((c.gp * h1) * h2) * F) * fabs(aux));
+        ci = sqrt((((c.gp * h1) * h2) * F) * abs_bits(aux));
     }
     V4 D{u - cg, uu - ci, uu + ci, u + cg};
     sort_eig(D, c.eig_sort);
@@ -150,8 +175,8 @@ LSH_HD double friction_mu(double h1, double u1, double h2, double u2, const Cons
     const double mustop = c.tan1 + (c.tan2 - c.tan1) / (1.0 + h2 / L2c);
     const double mustart = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2c);
     double muf;
-    if (fr > beta) muf = c.tan1 + (c.tan2 - c.tan1) / (1.0 + beta * h2 / (fr * L2c));
-    else if (fabs(fr) < kEps) muf = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2c);
+    if (gt_pos(fr, beta)) muf = c.tan1 + (c.tan2 - c.tan1) / (1.0 + beta * h2 / (fr * L2c));
+    else if (abs_lt(fr, kEps)) muf = c.tan3 + (c.tan4 - c.tan3) / (1.0 + h2 / L2c);
     else muf = fmad(lshm::pow_pos(fr / beta, chi), mustop - mustart, mustart);
     return (muf * c.L) / c.H;
 }
@@ -195,15 +220,15 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
 
     // tratamientoSecoMojado (Arista_kernel.cu:301-321)
     if (L2) {
-        if ((Ah2 < eps) && (H1 - Bh2 > H0)) Bq2 = 0.0;
-        if ((Bh2 < eps) && (H0 - Ah2 > H1)) Aq2 = 0.0;
-        if ((Ah1 < eps) && (H1 - Bh1 - Bh2 > H0 - Ah2)) Bq1 = 0.0;
-        if ((Bh1 < eps) && (H0 - Ah1 - Ah2 > H1 - Bh2)) Aq1 = 0.0;
-        if ((Ah2 + Ah1 < eps) && (H1 - Bh1 - Bh2 > H0)) { Bq1 = 0.0; Bq2 = 0.0; }
-        if ((Bh2 + Bh1 < eps) && (H0 - Ah1 - Ah2 > H1)) { Aq1 = 0.0; Aq2 = 0.0; }
+        if (lt_pos(Ah2, eps) && lt(H0, H1 - Bh2)) Bq2 = 0.0;
+        if (lt_pos(Bh2, eps) && lt(H1, H0 - Ah2)) Aq2 = 0.0;
+        if (lt_pos(Ah1, eps) && lt(H0 - Ah2, H1 - Bh1 - Bh2)) Bq1 = 0.0;
+        if (lt_pos(Bh1, eps) && lt(H1 - Bh2, H0 - Ah1 - Ah2)) Aq1 = 0.0;
+        if (lt_pos(Ah2 + Ah1, eps) && lt(H0, H1 - Bh1 - Bh2)) { Bq1 = 0.0; Bq2 = 0.0; }
+        if (lt_pos(Bh2 + Bh1, eps) && lt(H1, H0 - Ah1 - Ah2)) { Aq1 = 0.0; Aq2 = 0.0; }
     } else {
-        if ((Ah1 < eps) && (H1 - Bh1 > H0)) Bq1 = 0.0;
-        if ((Bh1 < eps) && (H0 - Ah1 > H1)) Aq1 = 0.0;
+        if (lt_pos(Ah1, eps) && lt(H0, H1 - Bh1)) Bq1 = 0.0;
+        if (lt_pos(Bh1, eps) && lt(H1, H0 - Ah1)) Aq1 = 0.0;
     }
 
     const double fA1 = vfac(Ah1, eps), fB1 = vfac(Bh1, eps);
@@ -216,7 +241,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         u2ij = fmad(sa2, fA2 * Aq2, sb2 * (fB2 * Bq2)) / (sa2 + sb2 + kEps);
     }
     // a face's celerity sqrt(g h) is sqrt(g) sqrt(h1) when its granular layer is empty
-    const bool oneA = !L2 || (Ah2 == 0.0), oneB = !L2 || (Bh2 == 0.0);
+    const bool oneA = !L2 || is_zero(Ah2), oneB = !L2 || is_zero(Bh2);
 
     const double Hm = tmin(H0, H1);
     const double deta1 = L2 ? max0(Bh1 + Bh2 - H1 + Hm) - max0(Ah1 + Ah2 - H0 + Hm)
@@ -230,7 +255,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     if (L2) {
         const double mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
         const double sc = ((fsc_of(h1ij, c) * mu) * c.g) * h2ij;
-        coul = fabs(h2ij * u2ij) < (c.peso * sc) * dt;
+        coul = lt(abs_bits(h2ij * u2ij), (c.peso * sc) * dt);
         if (coul) tp2.w = (gh2 * c.r) * deta1;
     }
 
@@ -239,38 +264,38 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     const V4 E1 = eig<L2>(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, L2 ? Bq1 + Bq2 : Bq1, c, fB1, oneB ? sb1 : -1.0);
     const double aut1 = tmin(D.x, tmin(E0.x, E1.x));
     const double aut3 = tmax(D.w, tmax(E0.w, E1.w));
-    double lmax = tmax(fabs(aut3), fabs(aut1));
-    const double umax = L2 ? tmax(fabs(u1ij), fabs(u2ij)) : fabs(u1ij);
-    if (umax > lmax) lmax = umax;
-    double aut2 = tmax(fabs(D.y), fabs(D.z));
+    double lmax = tmax(abs_bits(aut3), abs_bits(aut1));
+    const double umax = L2 ? tmax(abs_bits(u1ij), abs_bits(u2ij)) : abs_bits(u1ij);
+    if (lt(lmax, umax)) lmax = umax;
+    double aut2 = tmax(abs_bits(D.y), abs_bits(D.z));
     if (sgn(aut1 + aut3) < 0) aut2 = -aut2;
 
     double a0, a1, a2 = 0.0;
-    if ((fabs(aut1 - aut3) >= kEps) && (fabs(aut1 - aut2) >= kEps) && (fabs(aut2 - aut3) >= kEps)) {
-        if (L2 && (h1ij >= eps) && (h2ij >= eps)) {
+    if (!abs_lt(aut1 - aut3, kEps) && !abs_lt(aut1 - aut2, kEps) && !abs_lt(aut2 - aut3, kEps)) {
+        if (L2 && !lt_pos(h1ij, eps) && !lt_pos(h2ij, eps)) {
             const double d12 = aut1 - aut2, d13 = aut1 - aut3, d23 = aut2 - aut3;
             const double inv = 1.0 / ((d12 * d13) * d23);
-            const double a = (fabs(aut1) * d23) * inv;
-            const double b = -((fabs(aut2) * d13) * inv);
-            const double cc = (fabs(aut3) * d12) * inv;
+            const double a = (abs_bits(aut1) * d23) * inv;
+            const double b = -((abs_bits(aut2) * d13) * inv);
+            const double cc = (abs_bits(aut3) * d12) * inv;
             a0 = fmad(a * aut2, aut3, fmad(b * aut1, aut3, (cc * aut1) * aut2));
             a1 = -fmad(a, aut2 + aut3, fmad(b, aut1 + aut3, cc * (aut1 + aut2)));
             a2 = a + b + cc;
         } else {
             const double inv = 1.0 / (aut3 - aut1);
-            a0 = fmad(aut3, fabs(aut1), -(aut1 * fabs(aut3))) * inv;
-            a1 = (fabs(aut3) - fabs(aut1)) * inv;
+            a0 = fmad(aut3, abs_bits(aut1), -(aut1 * abs_bits(aut3))) * inv;
+            a1 = (abs_bits(aut3) - abs_bits(aut1)) * inv;
         }
     } else {
         a0 = lmax; a1 = 0.0;
     }
 
-    const double FAy = (Ah1 < kEps) ? 0.0 : (fA1 * Aq1) * Aq1, FBy = (Bh1 < kEps) ? 0.0 : (fB1 * Bq1) * Bq1;
+    const double FAy = lt_pos(Ah1, kEps) ? 0.0 : (fA1 * Aq1) * Aq1, FBy = lt_pos(Bh1, kEps) ? 0.0 : (fB1 * Bq1) * Bq1;
     const double dFx = Bq1 - Aq1, dFy = FBy - FAy;
     double dFz = 0.0, dFw = 0.0, FAw = 0.0, FBw = 0.0;
     if (L2) {
-        FAw = (Ah2 < kEps) ? 0.0 : (fA2 * Aq2) * Aq2;
-        FBw = (Bh2 < kEps) ? 0.0 : (fB2 * Bq2) * Bq2;
+        FAw = lt_pos(Ah2, kEps) ? 0.0 : (fA2 * Aq2) * Aq2;
+        FBw = lt_pos(Bh2, kEps) ? 0.0 : (fB2 * Bq2) * Bq2;
         dFz = Bq2 - Aq2;
         dFw = FBw - FAw;
     }
@@ -282,7 +307,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
 
     V4 I{deta1, Bq1 - Aq1, 0.0, Bq2 - Aq2};
     if (!coul) {
-        if ((Ah1 > eps) && (Bh1 > eps)) I.x = I.x - deta2;
+        if (gt_pos(Ah1, eps) && gt_pos(Bh1, eps)) I.x = I.x - deta2;
         I.z = deta2;
     }
 
@@ -297,7 +322,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     const double Fmx = half_x + (Aq1 - Qx), Fmy = half_y + (FAy - Qy);
     const double Fpx = half_x + (Qx - Bq1), Fpy = half_y + (Qy - FBy);
 
-    const double u1t = (fabs(Fmx) < kEps) ? 0.0 : ((Fmx > 0.0) ? fA1 * e.A.qt1 : fB1 * e.B.qt1);
+    const double u1t = abs_lt(Fmx, kEps) ? 0.0 : (gt0(Fmx) ? fA1 * e.A.qt1 : fB1 * e.B.qt1);
     const double s1 = Fmx * u1t;
     double M[6] = {Fmx, Fmy, s1, 0.0, 0.0, 0.0};
     double P[6] = {Fpx, Fpy, -s1, 0.0, 0.0, 0.0};
@@ -309,7 +334,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         const double half_z = 0.5 * (dFz + tp.z), half_w = 0.5 * (dFw + tp.w);
         const double Fmz = half_z + (Aq2 - Qz), Fmw = half_w + (FAw - Qw);
         const double Fpz = half_z + (Qz - Bq2), Fpw = half_w + (Qw - FBw);
-        const double u2t = (fabs(Fmz) < kEps) ? 0.0 : ((Fmz > 0.0) ? fA2 * e.A.qt2 : fB2 * e.B.qt2);
+        const double u2t = abs_lt(Fmz, kEps) ? 0.0 : (gt0(Fmz) ? fA2 * e.A.qt2 : fB2 * e.B.qt2);
         const double s2 = Fmz * u2t;
         M[3] = Fmz; M[4] = Fmw; M[5] = s2;
         P[3] = Fpz; P[4] = Fpw; P[5] = -s2;
@@ -334,10 +359,10 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         // limited when dt exceeds the time a side takes to empty its layer,
         // hp area / (beta M + eps): tested as dt (beta M + eps) > hp area (the
         // denominator is positive), so the divisions run only on limited edges
-        const bool oa = (M[k] > 0.0), ob = e.interior && (P[k] > 0.0);
+        const bool oa = gt0(M[k]), ob = e.interior && gt0(P[k]);
         const double ha = (layer ? hp01 : hp00) * e.area0, hb = (layer ? hp11 : hp10) * e.area1;
         const double da = oa ? fmad(factor, M[k], kEps) : 1.0, db = ob ? fmad(factor, P[k], kEps) : 1.0;
-        const bool lim = (oa && !(dt * da <= ha)) || (ob && !(dt * db <= hb));
+        const bool lim = (oa && lt(ha, dt * da)) || (ob && lt(hb, dt * db));
         if (lim) {
             const double dta = oa ? ha / da : kBig, dtb = ob ? hb / db : kBig;
             const double dtl = tmin(dta, dtb);
@@ -347,9 +372,9 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         }
     }
 
-    if (lmax < eps) lmax = lmax + eps;
+    if (lt_pos(lmax, eps)) lmax = lmax + eps;
     o.wave = e.len * lmax;
-    if (c.peso != 1.0) {
+    if (lshm::bits_of(c.peso) != lshm::bits_of(1.0)) {
         o.wave = o.wave * c.inv_peso;
 #pragma unroll
         for (int k = 0; k < 6; ++k) { M[k] = c.peso * M[k]; P[k] = c.peso * P[k]; }
@@ -371,9 +396,9 @@ LSH_HD double edge_initial_wave(const Face& A, const Face& B, double len, const 
     const double u2ij = fmad(sa, fA2 * A.qn2, sb * (fB2 * B.qn2)) / (sa + sb + kEps);
     const V4 D = eig<true>(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
     double lmax = tmax(D.x, D.w);
-    const double b = tmax(fabs(u1ij), fabs(u2ij));
-    if (b > lmax) lmax = b;
-    if (lmax < eps) lmax = lmax + eps;
+    const double b = tmax(abs_bits(u1ij), abs_bits(u2ij));
+    if (lt(lmax, b)) lmax = b;
+    if (lt_pos(lmax, eps)) lmax = lmax + eps;
     return len * lmax;
 }
 
@@ -381,8 +406,8 @@ LSH_HD double edge_initial_wave(const Face& A, const Face& B, double len, const 
 // the layer-2 damping (0 times a factor) is skipped.
 template <bool L2>
 LSH_HD void filtro(double w[6], double dt, const Consts& c) {
-    if (w[0] < 0.0) w[0] = 0.0;
-    if (w[3] < 0.0) w[3] = 0.0;
+    if (lt0(w[0])) w[0] = 0.0;
+    if (lt0(w[3])) w[3] = 0.0;
 #pragma unroll
     for (int layer = 0; layer < (L2 ? 2 : 1); ++layer) {
         const int k = 3 * layer;
@@ -391,7 +416,7 @@ LSH_HD void filtro(double w[6], double dt, const Consts& c) {
         const double d = fmad(x2, x2, kEps);
         // exp(-dt/d) is exactly 1 once dt/d < 2^-54: skip the division below a
         // bound that holds with ample margin over the roundings
-        if (dt < d * 0x1.fp-55) continue;
+        if (lt_pos(dt, d * 0x1.fp-55)) continue;  // d >= EPSILON: the bound is positive
         const double aux = exp_neg(dt * (1.0 / d));
         w[k + 1] = w[k + 1] * aux;
         w[k + 2] = w[k + 2] * aux;
@@ -399,13 +424,13 @@ LSH_HD void filtro(double w[6], double dt, const Consts& c) {
 #pragma unroll
     for (int layer = 0; layer < 2; ++layer) {
         const double vmax = layer ? c.vmax2 : c.vmax1;
-        if (vmax > 0.0) {
+        if (gt0(vmax)) {
             const int k = 3 * layer;
             const double h = w[k];
             const double f = vfac(h, c.eps_h);
             double ux = f * w[k + 1], uy = f * w[k + 2];
             const double u = sqrt(fmad(ux, ux, uy * uy));
-            if (u > vmax) {
+            if (gt_pos(u, vmax)) {
                 const double s = vmax / u;
                 ux = ux * s; uy = uy * s;
                 w[k + 1] = ux * h; w[k + 2] = uy * h;
@@ -420,8 +445,8 @@ LSH_HD void filtro(double w[6], double dt, const Consts& c) {
 template <bool L2>
 LSH_HD void dis_implicita(const double wo[6], double w[6], double dt, const Consts& c,
                                               double fo1) {
-    if (w[0] < 0.0) w[0] = 0.0;
-    if (w[3] < 0.0) w[3] = 0.0;
+    if (lt0(w[0])) w[0] = 0.0;
+    if (lt0(w[3])) w[3] = 0.0;
     const double eps = c.eps_h;
     const double h1 = w[0], h2 = L2 ? w[3] : 0.0;
     const double uo1x = fo1 * wo[1], uo1y = fo1 * wo[2];
@@ -429,10 +454,10 @@ LSH_HD void dis_implicita(const double wo[6], double w[6], double dt, const Cons
     if (!L2) {
         // bottom friction h u / (1 + c1), 1/(1 + X/Y) = Y/(Y + X); above
         // eps_h, h u is q itself
-        if (h1 > 0.0) {
+        if (gt0(h1)) {
             const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1;
             const double inv = Y / (Y + X);
-            if (h1 > eps) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
+            if (gt_pos(h1, eps)) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
             else {
                 const double f1 = vfac(h1, eps);
                 w[1] = (h1 * (f1 * w[1])) * inv;
@@ -450,9 +475,9 @@ LSH_HD void dis_implicita(const double wo[6], double w[6], double dt, const Cons
     const double dx = uo1x - uo2x, dy = uo1y - uo2y;
     const double du = sqrt(fmad(dx, dx, dy * dy));
     const double u2 = sqrt(fmad(uo2x, uo2x, uo2y * uo2y));
-    if ((h1 > 0.0) && (h2 > 0.0)) {
+    if (gt0(h1) && gt0(h2)) {
         const double hmod = fmad(c.r, h1, h2);
-        const double m = (hmod > c.eps_1r) ? hmod : c.eps_1r;
+        const double m = gt_pos(hmod, c.eps_1r) ? hmod : c.eps_1r;
         const double hm2 = hmod * hmod, m2 = m * m;
         const double hh = hmod / sqrt(fmad(hm2, hm2, m2 * m2));
         const double k12 = ((dt * kSqrt2) * hh) * (c.mfc * du);
@@ -466,23 +491,23 @@ LSH_HD void dis_implicita(const double wo[6], double w[6], double dt, const Cons
         w[2] = (h1 * fmad(u1y, e2, c1 * u2y)) * det;
         w[5] = (h2 * fmad(u2y, e1, c2 * u1y)) * det;
     }
-    if ((h1 > 0.0) && (h2 < eps)) {
+    if (gt0(h1) && lt_pos(h2, eps)) {
         const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1;
         const double inv = Y / (Y + X);
-        if (h1 > eps) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
+        if (gt_pos(h1, eps)) { w[1] = w[1] * inv; w[2] = w[2] * inv; }
         else { w[1] = (h1 * (f1 * w[1])) * inv; w[2] = (h1 * (f1 * w[2])) * inv; }
     }
-    if ((h2 > 0.0) && (h1 < eps)) {
+    if (gt0(h2) && lt_pos(h1, eps)) {
         const double Y = pow43(h2) + kEps, X = (dt * c.g_mfs2) * u2;
         const double inv = Y / (Y + X);
-        if (h2 > eps) { w[4] = w[4] * inv; w[5] = w[5] * inv; }
+        if (gt_pos(h2, eps)) { w[4] = w[4] * inv; w[5] = w[5] * inv; }
         else { w[4] = (h2 * (f2 * w[4])) * inv; w[5] = (h2 * (f2 * w[5])) * inv; }
     }
 }
 
 // coulomb (Volumen_kernel.cu:7-26)
 LSH_HD void coulomb(double w[6], double dt, const Consts& c) {
-    if (!(w[3] > 0.0)) {
+    if (!gt0(w[3])) {
         w[4] = w[4] * 0.0;
         w[5] = w[5] * 0.0;
         return;
@@ -496,7 +521,7 @@ LSH_HD void coulomb(double w[6], double dt, const Consts& c) {
     const double sc = ((((fsc_of(w[0], c) * mu) * c.g) * w[3]) * dt);
     const double normq = sqrt(fmad(w[4], w[4], w[5] * w[5]));
     double aux = 0.0;
-    if ((normq + sc >= kEps) && (normq >= sc)) aux = normq / (normq + sc);
+    if (!lt_pos(normq + sc, kEps) && !lt(normq, sc)) aux = normq / (normq + sc);
     w[4] = w[4] * aux;
     w[5] = w[5] * aux;
 }
@@ -508,12 +533,12 @@ LSH_HD void coulomb(double w[6], double dt, const Consts& c) {
 // (Volumen_kernel.cu:256) with one division per step.
 LSH_HD void volume_update(const double wo[6], const double acc[7], double w[6], double& rate,
                                               double inv_area, double tanR, double dt, const Consts& c) {
-    rate = (acc[6] < kEps) ? 0.0 : acc[6] * inv_area;
+    rate = lt_pos(acc[6], kEps) ? 0.0 : acc[6] * inv_area;
     const double b = dt * inv_area;
 #pragma unroll
     for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
     const double fo1 = vfac(wo[0], c.eps_h);
-    if (tanR != 0.0) {
+    if (!is_zero(tanR)) {
 #pragma unroll
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
