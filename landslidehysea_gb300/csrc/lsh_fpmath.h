@@ -81,6 +81,23 @@ LSH_HD void halves(double x, uint32_t& lo, uint32_t& hi) {
 #endif
 }
 
+LSH_HD double from_halves(uint32_t lo, uint32_t hi) {
+#if defined(__CUDA_ARCH__)
+    double x;
+    asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lo), "r"(hi));
+    return x;
+#else
+    return from_bits(((uint64_t)hi << 32) | lo);
+#endif
+}
+
+// c ? -x : x by flipping the sign bit (integer pipe): the bits of -x
+LSH_HD double neg_if(double x, bool c) {
+    uint32_t lo, hi;
+    halves(x, lo, hi);
+    return from_halves(lo, hi ^ ((uint32_t)c << 31));
+}
+
 // 2^k for -1022 <= k <= 1023
 LSH_HD double pow2i(int k) { return from_bits((uint64_t)(k + 1023) << 52); }
 

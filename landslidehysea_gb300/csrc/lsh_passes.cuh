@@ -51,9 +51,10 @@ LSH_HD void face_depths(const KArgs& a, int id, int side, double& h1, double& h2
     if (ORDER == 2) {
         const double* const* s = (side < 2) ? a.sx : a.sy;
         const double d1 = s[0][id] - s[3][id], d2 = s[3][id] + s[6][id];
-        // side & 1: the +slope face (E or N); the sign is a negation, not a multiply
-        h1 = h1 + ((side & 1) ? d1 : -d1);
-        h2 = h2 + ((side & 1) ? d2 : -d2);
+        // side & 1: the +slope face (E or N); the sign is a sign-bit flip
+        const bool neg = !(side & 1);
+        h1 = h1 + lshm::neg_if(d1, neg);
+        h2 = h2 + lshm::neg_if(d2, neg);
     }
 }
 
@@ -66,20 +67,21 @@ LSH_HD void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Fa
     double qx1 = a.W[1][id], qy1 = a.W[2][id], qx2 = a.W[4][id], qy2 = a.W[5][id], H = a.W[6][id];
     if (ORDER == 2) {
         const double* const* s = (side < 2) ? a.sx : a.sy;
-        const bool pos = (side & 1);
-        const double s1 = s[1][id], s2 = s[2][id], s4 = s[4][id], s5 = s[5][id], sH = s[6][id];
-        qx1 = qx1 + (pos ? s1 : -s1);
-        qy1 = qy1 + (pos ? s2 : -s2);
-        qx2 = qx2 + (pos ? s4 : -s4);
-        qy2 = qy2 + (pos ? s5 : -s5);
-        H = H + (pos ? sH : -sH);
+        using lshm::neg_if;
+        const bool neg = !(side & 1);
+        qx1 = qx1 + neg_if(s[1][id], neg);
+        qy1 = qy1 + neg_if(s[2][id], neg);
+        qx2 = qx2 + neg_if(s[4][id], neg);
+        qy2 = qy2 + neg_if(s[5][id], neg);
+        H = H + neg_if(s[6][id], neg);
     }
+    using lshm::neg_if;
     if (DIR == 1) {
-        f.qn1 = pos_normal ? qx1 : -qx1; f.qt1 = pos_normal ? qy1 : -qy1;
-        f.qn2 = pos_normal ? qx2 : -qx2; f.qt2 = pos_normal ? qy2 : -qy2;
+        f.qn1 = neg_if(qx1, !pos_normal); f.qt1 = neg_if(qy1, !pos_normal);
+        f.qn2 = neg_if(qx2, !pos_normal); f.qt2 = neg_if(qy2, !pos_normal);
     } else {
-        f.qn1 = pos_normal ? qy1 : -qy1; f.qt1 = pos_normal ? -qx1 : qx1;
-        f.qn2 = pos_normal ? qy2 : -qy2; f.qt2 = pos_normal ? -qx2 : qx2;
+        f.qn1 = neg_if(qy1, !pos_normal); f.qt1 = neg_if(qx1, pos_normal);
+        f.qn2 = neg_if(qy2, !pos_normal); f.qt2 = neg_if(qx2, pos_normal);
     }
     f.H = H;
 }
@@ -162,16 +164,17 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
         const int k = 3 * l;
         d0[k] = o.m[k];
         d1[k] = o.p[k];
+        using lshm::neg_if;
         if (DIR == 1) {
-            d0[k + 1] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
-            d0[k + 2] = pos_normal ? o.m[k + 2] : -o.m[k + 2];
-            d1[k + 1] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
-            d1[k + 2] = pos_normal ? o.p[k + 2] : -o.p[k + 2];
+            d0[k + 1] = neg_if(o.m[k + 1], !pos_normal);
+            d0[k + 2] = neg_if(o.m[k + 2], !pos_normal);
+            d1[k + 1] = neg_if(o.p[k + 1], !pos_normal);
+            d1[k + 2] = neg_if(o.p[k + 2], !pos_normal);
         } else {
-            d0[k + 1] = pos_normal ? -o.m[k + 2] : o.m[k + 2];
-            d0[k + 2] = pos_normal ? o.m[k + 1] : -o.m[k + 1];
-            d1[k + 1] = pos_normal ? -o.p[k + 2] : o.p[k + 2];
-            d1[k + 2] = pos_normal ? o.p[k + 1] : -o.p[k + 1];
+            d0[k + 1] = neg_if(o.m[k + 2], pos_normal);
+            d0[k + 2] = neg_if(o.m[k + 1], !pos_normal);
+            d1[k + 1] = neg_if(o.p[k + 2], pos_normal);
+            d1[k + 2] = neg_if(o.p[k + 1], !pos_normal);
         }
     }
     if (FIRST) {

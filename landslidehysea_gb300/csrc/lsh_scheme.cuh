@@ -268,7 +268,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     const double umax = L2 ? tmax(abs_bits(u1ij), abs_bits(u2ij)) : abs_bits(u1ij);
     if (lt(lmax, umax)) lmax = umax;
     double aut2 = tmax(abs_bits(D.y), abs_bits(D.z));
-    if (sgn(aut1 + aut3) < 0) aut2 = -aut2;
+    aut2 = lshm::neg_if(aut2, sgn(aut1 + aut3) < 0);
 
     double a0, a1, a2 = 0.0;
     if (!abs_lt(aut1 - aut3, kEps) && !abs_lt(aut1 - aut2, kEps) && !abs_lt(aut2 - aut3, kEps)) {
