@@ -35,11 +35,13 @@ struct ConstBar {
 
 LSH_HD void cb_zero(ConstBar& b) { b.r = b.omr = b.gp = b.inv_gp = b.mu = b.g_mf02 = b.g_mfs2 = b.eps_1r = 0.0; }
 
-LSH_HD double sgn1(double x) { return (x < 0.0) ? -1.0 : 1.0; }
+LSH_HD double sgn1(double x) { return lt0(x) ? -1.0 : 1.0; }
+// x * sgn1(s) as a sign-bit flip (integer pipe; the same bits)
+LSH_HD double times_sgn1(double x, double s) { return lshm::neg_if(x, lt0(s)); }
 
 // d vfac / dh
 LSH_HD double vfac_d(double h, double eps_h) {
-    if (h > eps_h) { const double v = 1.0 / h; return -(v * v); }
+    if (gt_pos(h, eps_h)) { const double v = 1.0 / h; return -(v * v); }
     const double h2 = h * h, m2 = eps_h * eps_h;
     const double q = fmad(h2, h2, m2 * m2);
     const double s = sqrt(q);
@@ -49,25 +51,25 @@ LSH_HD double vfac_d(double h, double eps_h) {
 
 // d (h cbrt h) / dh = (4/3) cbrt h; 0 at h = 0
 LSH_HD double pow43_d(double h) {
-    if (!(h > 0.0)) return 0.0;
+    if (!gt0(h)) return 0.0;
     const double c = lshm::cbrt_pos(h);
     return c + c / 3.0;
 }
 
-LSH_HD double sqrt_bar(double s, double sb) { return (s > 0.0) ? sb / (2.0 * s) : 0.0; }
+LSH_HD double sqrt_bar(double s, double sb) { return gt0(s) ? sb / (2.0 * s) : 0.0; }
 
 // The compare-and-swap network of sort_eig on values, carrying the labels
 // of the unsorted entries: after the call D[k] = entry perm[k].
 LSH_HD void sort_eig_perm(double D[4], int perm[4], int full) {
     auto cs = [&](int a, int b) {
-        if (D[a] > D[b]) {
+        if (lt(D[b], D[a])) {
             double t = D[b]; D[b] = D[a]; D[a] = t;
             int u = perm[b]; perm[b] = perm[a]; perm[a] = u;
         }
     };
     cs(0, 1); cs(0, 2); cs(0, 3); cs(1, 2); cs(1, 3);
     if (full) cs(1, 2);
-    else if (D[2] > D[1]) {
+    else if (lt(D[1], D[2])) {
         double t = D[1]; D[1] = D[2]; D[2] = t;
         int u = perm[1]; perm[1] = perm[2]; perm[2] = u;
     }
@@ -81,10 +83,10 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
                     double sqrt_h, const V4& Db, double& h1b, double& h2b, double& u1b, double& u2b, double& qb,
                     double& Fknownb, double& sqrt_hb, ConstBar& cb) {
     const double h = L2 ? h1 + h2 : h1;
-    const bool useFk = (!L2 && Fknown >= 0.0);
+    const bool useFk = (!L2 && !lt0(Fknown));
     const double F = useFk ? Fknown : vfac(h, c.eps_h);
     const double u = q * F;
-    const bool useSh = (sqrt_h >= 0.0);
+    const bool useSh = !lt0(sqrt_h);
     const double cg = useSh ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     double uu = 0.0, ci = 0.0, d = 0.0, aux = 0.0, P = 0.0;
     if (L2) {
@@ -92,7 +94,7 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
         d = u1 - u2;
         aux = fmad(-((d * d) * F), c.inv_gp, 1.0);
         P = (((c.gp * h1) * h2) * F);
-        ci = sqrt(P * fabs(aux));
+        ci = sqrt(P * abs_bits(aux));
     }
     double e[4] = {u - cg, uu - ci, uu + ci, u + cg};
     int perm[4] = {0, 1, 2, 3};
@@ -109,9 +111,9 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
         const double uub = eb[1] + eb[2];
         const double cib = eb[2] - eb[1];
         const double Xb = sqrt_bar(ci, cib);
-        const double A = fabs(aux);
+        const double A = abs_bits(aux);
         const double Pb = Xb * A;
-        const double auxb = (Xb * P) * sgn1(aux);
+        const double auxb = times_sgn1(Xb * P, aux);
         cb.gp += Pb * ((h1 * h2) * F);
         h1b += Pb * ((c.gp * h2) * F);
         h2b += Pb * ((c.gp * h1) * F);
@@ -132,7 +134,7 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
         h1b += nb * u2;
     }
     if (useSh) sqrt_hb += cgb * c.sqrt_g;
-    else if (cg > 0.0) hb += (cgb * c.g) / (2.0 * cg);
+    else if (gt0(cg)) hb += (cgb * c.g) / (2.0 * cg);
     qb += ub * F;
     Fb += ub * q;
     if (useFk) Fknownb += Fb;
@@ -172,15 +174,15 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     const double h2ij = L2 ? 0.5 * (Ah2 + Bh2) : 0.0;
     bool zA1 = false, zA2 = false, zB1 = false, zB2 = false;
     if (L2) {
-        if ((Ah2 < eps) && (H1 - Bh2 > H0)) zB2 = true;
-        if ((Bh2 < eps) && (H0 - Ah2 > H1)) zA2 = true;
-        if ((Ah1 < eps) && (H1 - Bh1 - Bh2 > H0 - Ah2)) zB1 = true;
-        if ((Bh1 < eps) && (H0 - Ah1 - Ah2 > H1 - Bh2)) zA1 = true;
-        if ((Ah2 + Ah1 < eps) && (H1 - Bh1 - Bh2 > H0)) { zB1 = true; zB2 = true; }
-        if ((Bh2 + Bh1 < eps) && (H0 - Ah1 - Ah2 > H1)) { zA1 = true; zA2 = true; }
+        if (lt_pos(Ah2, eps) && lt(H0, H1 - Bh2)) zB2 = true;
+        if (lt_pos(Bh2, eps) && lt(H1, H0 - Ah2)) zA2 = true;
+        if (lt_pos(Ah1, eps) && lt(H0 - Ah2, H1 - Bh1 - Bh2)) zB1 = true;
+        if (lt_pos(Bh1, eps) && lt(H1 - Bh2, H0 - Ah1 - Ah2)) zA1 = true;
+        if (lt_pos(Ah2 + Ah1, eps) && lt(H0, H1 - Bh1 - Bh2)) { zB1 = true; zB2 = true; }
+        if (lt_pos(Bh2 + Bh1, eps) && lt(H1, H0 - Ah1 - Ah2)) { zA1 = true; zA2 = true; }
     } else {
-        if ((Ah1 < eps) && (H1 - Bh1 > H0)) zB1 = true;
-        if ((Bh1 < eps) && (H0 - Ah1 > H1)) zA1 = true;
+        if (lt_pos(Ah1, eps) && lt(H0, H1 - Bh1)) zB1 = true;
+        if (lt_pos(Bh1, eps) && lt(H1, H0 - Ah1)) zA1 = true;
     }
     if (zA1) Aq1 = 0.0;
     if (zA2) Aq2 = 0.0;
@@ -200,7 +202,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         den2 = sa2 + sb2 + kEps;
         u2ij = num2 / den2;
     }
-    const bool oneA = !L2 || (Ah2 == 0.0), oneB = !L2 || (Bh2 == 0.0);
+    const bool oneA = !L2 || is_zero(Ah2), oneB = !L2 || is_zero(Bh2);
 
     const double Hm = tmin(H0, H1);
     const double P1 = L2 ? Bh1 + Bh2 - H1 + Hm : Bh1 - H1 + Hm;
@@ -217,7 +219,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     if (L2) {
         const double mu = friction_mu(h1ij, u1ij, h2ij, u2ij, c);
         const double sc = ((fsc_of(h1ij, c) * mu) * c.g) * h2ij;
-        coul = fabs(h2ij * u2ij) < (c.peso * sc) * dt;
+        coul = lt(abs_bits(h2ij * u2ij), (c.peso * sc) * dt);
         if (coul) tp2.w = (gh2 * c.r) * deta1;
     }
 
@@ -232,19 +234,19 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     const double aut1 = tmin(D.x, m01);
     const double M01 = tmax(E0.w, E1.w);
     const double aut3 = tmax(D.w, M01);
-    const double lmax0 = tmax(fabs(aut3), fabs(aut1));
-    const double umax = L2 ? tmax(fabs(u1ij), fabs(u2ij)) : fabs(u1ij);
-    const bool lm_u = (umax > lmax0);
+    const double lmax0 = tmax(abs_bits(aut3), abs_bits(aut1));
+    const double umax = L2 ? tmax(abs_bits(u1ij), abs_bits(u2ij)) : abs_bits(u1ij);
+    const bool lm_u = lt(lmax0, umax);
     double lmax = lm_u ? umax : lmax0;
-    const double aut2u = tmax(fabs(D.y), fabs(D.z));
+    const double aut2u = tmax(abs_bits(D.y), abs_bits(D.z));
     const bool neg2 = (sgn(aut1 + aut3) < 0);
-    const double aut2 = neg2 ? -aut2u : aut2u;
+    const double aut2 = lshm::neg_if(aut2u, neg2);
 
     int branch;  // 0: three waves, 1: two waves, 2: degenerate (a0 = lmax)
     double a0, a1, a2 = 0.0;
     double d12 = 0.0, d13 = 0.0, d23 = 0.0, inv = 0.0, aa = 0.0, bb = 0.0, cc = 0.0;
-    if ((fabs(aut1 - aut3) >= kEps) && (fabs(aut1 - aut2) >= kEps) && (fabs(aut2 - aut3) >= kEps)) {
-        if (L2 && (h1ij >= eps) && (h2ij >= eps)) {
+    if (!abs_lt(aut1 - aut3, kEps) && !abs_lt(aut1 - aut2, kEps) && !abs_lt(aut2 - aut3, kEps)) {
+        if (L2 && !lt_pos(h1ij, eps) && !lt_pos(h2ij, eps)) {
             branch = 0;
             d12 = aut1 - aut2; d13 = aut1 - aut3; d23 = aut2 - aut3;
             inv = 1.0 / ((d12 * d13) * d23);
@@ -265,11 +267,11 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         a0 = lmax; a1 = 0.0;
     }
 
-    const bool fAy = !(Ah1 < kEps), fBy = !(Bh1 < kEps);
+    const bool fAy = !lt_pos(Ah1, kEps), fBy = !lt_pos(Bh1, kEps);
     const double FAy = fAy ? uA1 * Aq1 : 0.0, FBy = fBy ? uB1 * Bq1 : 0.0;
     const double dFx = Bq1 - Aq1, dFy = FBy - FAy;
     double dFz = 0.0, dFw = 0.0, FAw = 0.0, FBw = 0.0;
-    const bool fAw = L2 && !(Ah2 < kEps), fBw = L2 && !(Bh2 < kEps);
+    const bool fAw = L2 && !lt_pos(Ah2, kEps), fBw = L2 && !lt_pos(Bh2, kEps);
     if (L2) {
         FAw = fAw ? uA2 * Aq2 : 0.0;
         FBw = fBw ? uB2 * Bq2 : 0.0;
@@ -280,7 +282,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     const double Atx = T2.y;
     const double Aty = fmad(gh1, T2.z, fmad(u1ij + u1ij, T2.y, fmad(-u1ij, u1ij, gh1) * T2.x));
     V4 I{deta1, Bq1 - Aq1, 0.0, Bq2 - Aq2};
-    const bool icx = !coul && (Ah1 > eps) && (Bh1 > eps);
+    const bool icx = !coul && gt_pos(Ah1, eps) && gt_pos(Bh1, eps);
     if (!coul) {
         if (icx) I.x = I.x - deta2;
         I.z = deta2;
@@ -296,7 +298,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     const double half_x = 0.5 * (dFx + tp.x), half_y = 0.5 * (dFy + tp.y);
     const double Fmx = half_x + (Aq1 - Qx), Fmy = half_y + (FAy - Qy);
     const double Fpx = half_x + (Qx - Bq1), Fpy = half_y + (Qy - FBy);
-    const int t1 = (fabs(Fmx) < kEps) ? 0 : ((Fmx > 0.0) ? 1 : 2);
+    const int t1 = abs_lt(Fmx, kEps) ? 0 : (gt0(Fmx) ? 1 : 2);
     const double u1t = (t1 == 0) ? 0.0 : ((t1 == 1) ? fA1 * e.A.qt1 : fB1 * e.B.qt1);
     const double s1 = Fmx * u1t;
     double M[6] = {Fmx, Fmy, s1, 0.0, 0.0, 0.0};
@@ -314,7 +316,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         Fmz = half_z + (Aq2 - Qz);
         const double Fmw = half_w + (FAw - Qw);
         const double Fpz = half_z + (Qz - Bq2), Fpw = half_w + (Qw - FBw);
-        t2 = (fabs(Fmz) < kEps) ? 0 : ((Fmz > 0.0) ? 1 : 2);
+        t2 = abs_lt(Fmz, kEps) ? 0 : (gt0(Fmz) ? 1 : 2);
         u2t = (t2 == 0) ? 0.0 : ((t2 == 1) ? fA2 * e.A.qt2 : fB2 * e.B.qt2);
         const double s2 = Fmz * u2t;
         M[3] = Fmz; M[4] = Fmw; M[5] = s2;
@@ -338,12 +340,12 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     for (int k = 0; k < 6; ++k) { Mpre[k] = M[k]; Ppre[k] = P[k]; }
     for (int layer = 0; layer < (L2 ? 2 : 1); ++layer) {
         const int k = 3 * layer;
-        useA[layer] = (M[k] > 0.0);
-        useB[layer] = e.interior && (P[k] > 0.0);
+        useA[layer] = gt0(M[k]);
+        useB[layer] = e.interior && gt0(P[k]);
         const double ha = hp0[layer] * e.area0, hb = hp1[layer] * e.area1;
         if (useA[layer]) denA[layer] = fmad(factor, M[k], kEps);
         if (useB[layer]) denB[layer] = fmad(factor, P[k], kEps);
-        lim[layer] = (useA[layer] && !(dt * denA[layer] <= ha)) || (useB[layer] && !(dt * denB[layer] <= hb));
+        lim[layer] = (useA[layer] && lt(ha, dt * denA[layer])) || (useB[layer] && lt(hb, dt * denB[layer]));
         if (lim[layer]) {
             if (useA[layer]) dta[layer] = ha / denA[layer];
             if (useB[layer]) dtbv[layer] = hb / denB[layer];
@@ -351,14 +353,12 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
             alpha[layer] = dtl[layer] / (dt + kEps);
         }
     }
-    const bool lm_eps = (lmax < eps);
-    (void)lm_eps;
 
     // ---------------------------------------------------------------- reverse
     double mb[6], pb[6];
     for (int k = 0; k < 6; ++k) { mb[k] = ob.m[k]; pb[k] = ob.p[k]; }
     double wb = ob.wave;
-    if (c.peso != 1.0) {
+    if (lshm::bits_of(c.peso) != lshm::bits_of(1.0)) {
         wb = wb * c.inv_peso;
         for (int k = 0; k < 6; ++k) { mb[k] = c.peso * mb[k]; pb[k] = c.peso * pb[k]; }
     }
@@ -377,7 +377,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         const double dtlb = alb / (dt + kEps);
         dtb += -alb * (alpha[layer] / (dt + kEps));
         // tmin(dta, dtb) = (dtb < dta) ? dtb : dta
-        if (dtbv[layer] < dta[layer]) {
+        if (lt(dtbv[layer], dta[layer])) {
             // dtb = hp1 area1 / (beta P + eps)
             hp1b[layer] += dtlb * (e.area1 / denB[layer]);
             pb[k] += (-dtlb * (dtbv[layer] / denB[layer])) * factor;
@@ -497,9 +497,9 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         aut2b += a0b * (aa * aut3 + cc * aut1) - a1b * (aa + cc);
         aut3b += a0b * (aa * aut2 + bb * aut1) - a1b * (aa + bb);
         double d12b = 0.0, d13b = 0.0, d23b = 0.0, invb = 0.0;
-        aut1b += ab_ * sgn1(aut1) * d23 * inv; d23b += ab_ * fabs(aut1) * inv; invb += ab_ * fabs(aut1) * d23;
-        aut2b -= bb_ * sgn1(aut2) * d13 * inv; d13b -= bb_ * fabs(aut2) * inv; invb -= bb_ * fabs(aut2) * d13;
-        aut3b += cb_ * sgn1(aut3) * d12 * inv; d12b += cb_ * fabs(aut3) * inv; invb += cb_ * fabs(aut3) * d12;
+        aut1b += times_sgn1(ab_, aut1) * d23 * inv; d23b += ab_ * fabs(aut1) * inv; invb += ab_ * fabs(aut1) * d23;
+        aut2b -= times_sgn1(bb_, aut2) * d13 * inv; d13b -= bb_ * fabs(aut2) * inv; invb -= bb_ * fabs(aut2) * d13;
+        aut3b += times_sgn1(cb_, aut3) * d12 * inv; d12b += cb_ * fabs(aut3) * inv; invb += cb_ * fabs(aut3) * d12;
         const double Pb = -invb * (inv * inv);
         d12b += Pb * (d13 * d23); d13b += Pb * (d12 * d23); d23b += Pb * (d12 * d13);
         aut1b += d12b + d13b;
@@ -510,8 +510,8 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         const double n1 = fabs(aut3) - fabs(aut1);
         const double n0b = a0b * inv, n1b = a1b * inv;
         const double invb = a0b * n0 + a1b * n1;
-        aut3b += n0b * (fabs(aut1) - aut1 * sgn1(aut3)) + n1b * sgn1(aut3);
-        aut1b += n0b * (aut3 * sgn1(aut1) - fabs(aut3)) - n1b * sgn1(aut1);
+        aut3b += n0b * (fabs(aut1) - times_sgn1(aut1, aut3)) + times_sgn1(n1b, aut3);
+        aut1b += n0b * (times_sgn1(aut3, aut1) - fabs(aut3)) - times_sgn1(n1b, aut1);
         const double denb = -invb * (inv * inv);
         aut3b += denb;
         aut1b -= denb;
@@ -519,22 +519,22 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
         lmaxb += a0b;
     }
     // signed aut2
-    const double aut2ub = neg2 ? -aut2b : aut2b;
+    const double aut2ub = lshm::neg_if(aut2b, neg2);
     V4 Db{0.0, 0.0, 0.0, 0.0}, E0b{0.0, 0.0, 0.0, 0.0}, E1b{0.0, 0.0, 0.0, 0.0};
-    if (fabs(D.z) > fabs(D.y)) Db.z += aut2ub * sgn1(D.z);
-    else Db.y += aut2ub * sgn1(D.y);
+    if (abs_lt(D.y, D.z)) Db.z += times_sgn1(aut2ub, D.z);
+    else Db.y += times_sgn1(aut2ub, D.y);
     // lmax
     if (lm_u) {
-        if (L2 && (fabs(u2ij) > fabs(u1ij))) u2b += lmaxb * sgn1(u2ij);
-        else u1b += lmaxb * sgn1(u1ij);
+        if (L2 && abs_lt(u1ij, u2ij)) u2b += times_sgn1(lmaxb, u2ij);
+        else u1b += times_sgn1(lmaxb, u1ij);
     } else {
-        if (fabs(aut1) > fabs(aut3)) aut1b += lmaxb * sgn1(aut1);
-        else aut3b += lmaxb * sgn1(aut3);
+        if (abs_lt(aut3, aut1)) aut1b += times_sgn1(lmaxb, aut1);
+        else aut3b += times_sgn1(lmaxb, aut3);
     }
     // aut1 = tmin(D.x, tmin(E0.x, E1.x)); aut3 = tmax(D.w, tmax(E0.w, E1.w))
-    if (m01 < D.x) { if (E1.x < E0.x) E1b.x += aut1b; else E0b.x += aut1b; }
+    if (lt(m01, D.x)) { if (lt(E1.x, E0.x)) E1b.x += aut1b; else E0b.x += aut1b; }
     else Db.x += aut1b;
-    if (M01 > D.w) { if (E1.w > E0.w) E1b.w += aut3b; else E0b.w += aut3b; }
+    if (lt(D.w, M01)) { if (lt(E0.w, E1.w)) E1b.w += aut3b; else E0b.w += aut3b; }
     else Db.w += aut3b;
     // eigenvalue bounds
     double h1ijb = 0.0, h2ijb = 0.0, qDb = 0.0, dummyF = 0.0, dummyS = 0.0;
@@ -547,10 +547,10 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     {
         double shb = 0.0;
         eig_adj<L2>(Ah1, Ah2, uA1, uA2, qA, c, fA1, shA, E0b, Ah1b, Ah2b, uA1b, uA2b, qAb, fA1b, shb, cb);
-        if (shA >= 0.0) sa1b += shb;
+        if (!lt0(shA)) sa1b += shb;
         shb = 0.0;
         eig_adj<L2>(Bh1, Bh2, uB1, uB2, qB, c, fB1, shB, E1b, Bh1b, Bh2b, uB1b, uB2b, qBb, fB1b, shb, cb);
-        if (shB >= 0.0) sb1b += shb;
+        if (!lt0(shB)) sb1b += shb;
     }
     Aq1b += qAb; Bq1b += qBb;
     if (L2) { Aq2b += qAb; Bq2b += qBb; }
@@ -574,11 +574,11 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     h1ijb += gh1b * c.g;
     h2ijb += gh2b * c.g;
     if (L2) {
-        if (Q1 > 0.0) Bh2b += deta2b;
-        if (Q0 > 0.0) Ah2b -= deta2b;
+        if (gt0(Q1)) Bh2b += deta2b;
+        if (gt0(Q0)) Ah2b -= deta2b;
     }
-    if (P1 > 0.0) { Bh1b += deta1b; if (L2) Bh2b += deta1b; }
-    if (P0 > 0.0) { Ah1b -= deta1b; if (L2) Ah2b -= deta1b; }
+    if (gt0(P1)) { Bh1b += deta1b; if (L2) Bh2b += deta1b; }
+    if (gt0(P0)) { Ah1b -= deta1b; if (L2) Ah2b -= deta1b; }
     // Roe-type velocities
     {
         const double num1b = u1b / den1;
@@ -643,11 +643,11 @@ LSH_HD void edge_initial_wave_adj(const Face& A, const Face& B, double len, cons
     const double lmaxb = len * wb;
     double u1b = 0.0, u2b = 0.0;
     V4 Db{0.0, 0.0, 0.0, 0.0};
-    if (bmax > lm0) {
-        if (fabs(u2ij) > fabs(u1ij)) u2b += lmaxb * sgn1(u2ij);
-        else u1b += lmaxb * sgn1(u1ij);
+    if (lt(lm0, bmax)) {
+        if (abs_lt(u1ij, u2ij)) u2b += times_sgn1(lmaxb, u2ij);
+        else u1b += times_sgn1(lmaxb, u1ij);
     } else {
-        if (D.w > D.x) Db.w += lmaxb;
+        if (lt(D.x, D.w)) Db.w += lmaxb;
         else Db.x += lmaxb;
     }
     double h1ijb = 0.0, h2ijb = 0.0, qb = 0.0, fk = 0.0, sh = 0.0;
@@ -676,7 +676,7 @@ LSH_HD void bottom_friction_adj(double h, double un, double gm, double dt, doubl
     const double Y = pow43(h) + kEps, X = (dt * gm) * un;
     const double inv = Y / (Y + X);
     double invb = 0.0;
-    if (h > eps) {
+    if (gt_pos(h, eps)) {
         invb = wbar[0] * win[0] + wbar[1] * win[1];
         wbar[0] = wbar[0] * inv;
         wbar[1] = wbar[1] * inv;
@@ -717,7 +717,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     const double fo1 = vfac(wo[0], eps);
     bool sph[2] = {false, false};
     double Fs[2] = {0.0, 0.0}, uxs[2] = {0.0, 0.0}, ss[2] = {0.0, 0.0};
-    if (tanR != 0.0) {
+    if (!is_zero(tanR)) {
         for (int layer = 0; layer < 2; ++layer) {
             const int k = 3 * layer;
             if (is_zero(wo[k]) && is_zero(wo[k + 1]) && is_zero(wo[k + 2])) continue;
@@ -735,7 +735,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     // filtro: clamp, damping, vmax caps
     double wc[6];
     for (int k = 0; k < 6; ++k) wc[k] = w1[k];
-    const bool cl0 = (wc[0] < 0.0), cl3 = (wc[3] < 0.0);
+    const bool cl0 = lt0(wc[0]), cl3 = lt0(wc[3]);
     if (cl0) wc[0] = 0.0;
     if (cl3) wc[3] = 0.0;
     double wd[6];
@@ -747,7 +747,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         xx[layer] = wd[k] * c.inv_eps;
         x2s[layer] = xx[layer] * xx[layer];
         dd[layer] = fmad(x2s[layer], x2s[layer], kEps);
-        if (dt < dd[layer] * 0x1.fp-55) continue;
+        if (lt_pos(dt, dd[layer] * 0x1.fp-55)) continue;  // dd >= EPSILON: the bound is positive
         damp[layer] = true;
         auxs[layer] = exp_neg(dt * (1.0 / dd[layer]));
         wd[k + 1] = wd[k + 1] * auxs[layer];
@@ -759,14 +759,14 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     double vf[2] = {0.0, 0.0}, vux[2] = {0.0, 0.0}, vuy[2] = {0.0, 0.0}, vu[2] = {0.0, 0.0}, vs[2] = {0.0, 0.0};
     for (int layer = 0; layer < 2; ++layer) {
         const double vmax = layer ? c.vmax2 : c.vmax1;
-        if (!(vmax > 0.0)) continue;
+        if (!gt0(vmax)) continue;
         const int k = 3 * layer;
         const double h = wv[k];
         vf[layer] = vfac(h, eps);
         vux[layer] = vf[layer] * wv[k + 1];
         vuy[layer] = vf[layer] * wv[k + 2];
         vu[layer] = sqrt(fmad(vux[layer], vux[layer], vuy[layer] * vuy[layer]));
-        if (vu[layer] > vmax) {
+        if (gt_pos(vu[layer], vmax)) {
             cap[layer] = true;
             vs[layer] = vmax / vu[layer];
             wv[k + 1] = (vux[layer] * vs[layer]) * h;
@@ -782,9 +782,9 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     const double ddx = uo1x - uo2x, ddy = uo1y - uo2y;
     const double du = sqrt(fmad(ddx, ddx, ddy * ddy));
     const double u2o = sqrt(fmad(uo2x, uo2x, uo2y * uo2y));
-    const bool blkA = !single && (h1 > 0.0) && (h2 > 0.0);
-    const bool blkB = (h1 > 0.0) && (h2 < eps);
-    const bool blkC = !single && (h2 > 0.0) && (h1 < eps);
+    const bool blkA = !single && gt0(h1) && gt0(h2);
+    const bool blkB = gt0(h1) && lt_pos(h2, eps);
+    const bool blkC = !single && gt0(h2) && lt_pos(h1, eps);
     double wa[6];  // after block A
     for (int k = 0; k < 6; ++k) wa[k] = wv[k];
     const double f1 = vfac(h1, eps), f2 = single ? 0.0 : vfac(h2, eps);
@@ -795,7 +795,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         u1x = f1 * wv[1]; u1y = f1 * wv[2];
         u2x = f2 * wv[4]; u2y = f2 * wv[5];
         hmod = fmad(c.r, h1, h2);
-        mm = (hmod > c.eps_1r) ? hmod : c.eps_1r;
+        mm = gt_pos(hmod, c.eps_1r) ? hmod : c.eps_1r;
         hm2 = hmod * hmod; m2 = mm * mm;
         Sq = sqrt(fmad(hm2, hm2, m2 * m2));
         hh = hmod / Sq;
@@ -818,7 +818,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     if (blkB) {
         const double Y = pow43(h1) + kEps, X = (dt * c.g_mf02) * u1o;
         const double inv = Y / (Y + X);
-        if (h1 > eps) { wbk[1] = wa[1] * inv; wbk[2] = wa[2] * inv; }
+        if (gt_pos(h1, eps)) { wbk[1] = wa[1] * inv; wbk[2] = wa[2] * inv; }
         else { wbk[1] = (h1 * (f1 * wa[1])) * inv; wbk[2] = (h1 * (f1 * wa[2])) * inv; }
     }
     double wcc[6];  // after block C (= dis_implicita's output)
@@ -826,7 +826,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     if (blkC) {
         const double Y = pow43(h2) + kEps, X = (dt * c.g_mfs2) * u2o;
         const double inv = Y / (Y + X);
-        if (h2 > eps) { wcc[4] = wbk[4] * inv; wcc[5] = wbk[5] * inv; }
+        if (gt_pos(h2, eps)) { wcc[4] = wbk[4] * inv; wcc[5] = wbk[5] * inv; }
         else { wcc[4] = (h2 * (f2 * wbk[4])) * inv; wcc[5] = (h2 * (f2 * wbk[5])) * inv; }
     }
 
@@ -834,7 +834,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     double g[6];
     for (int k = 0; k < 6; ++k) g[k] = wbar_in[k];
     // coulomb (or, single layer, q2 * 0)
-    if (single || !(wcc[3] > 0.0)) {
+    if (single || !gt0(wcc[3])) {
         g[4] = 0.0;
         g[5] = 0.0;
     } else {
@@ -844,7 +844,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         const double fsc = 1.0 - c.r * (1.0 - ex);
         const double sc = (((fsc * c.mu) * c.g) * hc2) * dt;
         const double nq = sqrt(fmad(wcc[4], wcc[4], wcc[5] * wcc[5]));
-        const bool act = (nq + sc >= kEps) && (nq >= sc);
+        const bool act = !lt_pos(nq + sc, kEps) && !lt(nq, sc);
         const double aux = act ? nq / (nq + sc) : 0.0;
         const double auxb = g[4] * wcc[4] + g[5] * wcc[5];
         g[4] = g[4] * aux;
@@ -853,7 +853,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
             const double s2 = (nq + sc) * (nq + sc);
             const double nqb = auxb * (sc / s2);
             const double scb = -auxb * (nq / s2);
-            if (nq > 0.0) { g[4] += nqb * (wcc[4] / nq); g[5] += nqb * (wcc[5] / nq); }
+            if (gt0(nq)) { g[4] += nqb * (wcc[4] / nq); g[5] += nqb * (wcc[5] / nq); }
             const double fscb = scb * (((c.mu * c.g) * hc2) * dt);
             cb.mu += scb * (((fsc * c.g) * hc2) * dt);
             g[3] += scb * (((fsc * c.mu) * c.g) * dt);
@@ -921,12 +921,12 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         const double hm2b = Qb * (2.0 * hm2), m2b = Qb * (2.0 * m2);
         hmodb += hm2b * (2.0 * hmod);
         const double mb = m2b * (2.0 * mm);
-        if (hmod > c.eps_1r) hmodb += mb;
+        if (gt_pos(hmod, c.eps_1r)) hmodb += mb;
         else cb.eps_1r += mb;
         cb.r += hmodb * h1;
         h1b += hmodb * c.r;
         h2b += hmodb;
-        if (du > 0.0) {
+        if (gt0(du)) {
             const double dxb = dub * (ddx / du), dyb = dub * (ddy / du);
             uo1xb += dxb; uo2xb -= dxb;
             uo1yb += dyb; uo2yb -= dyb;
@@ -940,8 +940,8 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         h2b += f2b * vfac_d(h2, eps);
     }
     // old speeds
-    if (u1o > 0.0) { uo1xb += u1ob * (uo1x / u1o); uo1yb += u1ob * (uo1y / u1o); }
-    if (!single && u2o > 0.0) { uo2xb += u2ob * (uo2x / u2o); uo2yb += u2ob * (uo2y / u2o); }
+    if (gt0(u1o)) { uo1xb += u1ob * (uo1x / u1o); uo1yb += u1ob * (uo1y / u1o); }
+    if (!single && gt0(u2o)) { uo2xb += u2ob * (uo2x / u2o); uo2yb += u2ob * (uo2y / u2o); }
     const double fo1b = uo1xb * wo[1] + uo1yb * wo[2];
     wob[1] += uo1xb * fo1;
     wob[2] += uo1yb * fo1;
@@ -965,7 +965,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
         double hb = oxb * (vux[layer] * vs[layer]) + oyb * (vuy[layer] * vs[layer]);
         const double vmax = layer ? c.vmax2 : c.vmax1;
         const double ub = -sb * (vmax / (vu[layer] * vu[layer]));
-        if (vu[layer] > 0.0) { uxb += ub * (vux[layer] / vu[layer]); uyb += ub * (vuy[layer] / vu[layer]); }
+        if (gt0(vu[layer])) { uxb += ub * (vux[layer] / vu[layer]); uyb += ub * (vuy[layer] / vu[layer]); }
         const double fb = uxb * wd[k + 1] + uyb * wd[k + 2];
         g[k + 1] = uxb * vf[layer];
         g[k + 2] = uyb * vf[layer];
@@ -1013,7 +1013,7 @@ LSH_HD void volume_update_adj(const double wo[6], const double acc[7], double in
     }
     dtb += bb * inv_area;
     // rate = acc_w / area (0 below EPSILON)
-    if (!(acc[6] < kEps)) accb[6] += rateb * inv_area;
+    if (!lt_pos(acc[6], kEps)) accb[6] += rateb * inv_area;
 }
 
 }  // namespace lsh
@@ -1053,12 +1053,12 @@ LSH_HD void face_scatter(const AdjArgs& a, int id, int side, bool pos_normal, co
     // back to x / y components (face_rest's selections reversed)
     double qx1b, qy1b, qx2b, qy2b;
     if (DIR == 1) {
-        qx1b = pos_normal ? fb.qn1 : -fb.qn1; qy1b = pos_normal ? fb.qt1 : -fb.qt1;
-        qx2b = pos_normal ? fb.qn2 : -fb.qn2; qy2b = pos_normal ? fb.qt2 : -fb.qt2;
+        qx1b = lshm::neg_if(fb.qn1, !pos_normal); qy1b = lshm::neg_if(fb.qt1, !pos_normal);
+        qx2b = lshm::neg_if(fb.qn2, !pos_normal); qy2b = lshm::neg_if(fb.qt2, !pos_normal);
     } else {
         // qn = sg qy, qt = -sg qx
-        qy1b = pos_normal ? fb.qn1 : -fb.qn1; qx1b = pos_normal ? -fb.qt1 : fb.qt1;
-        qy2b = pos_normal ? fb.qn2 : -fb.qn2; qx2b = pos_normal ? -fb.qt2 : fb.qt2;
+        qy1b = lshm::neg_if(fb.qn1, !pos_normal); qx1b = lshm::neg_if(fb.qt1, pos_normal);
+        qy2b = lshm::neg_if(fb.qn2, !pos_normal); qx2b = lshm::neg_if(fb.qt2, pos_normal);
     }
     a.Wbar[0][id] += fb.h1;
     a.Wbar[1][id] += qx1b;
@@ -1068,14 +1068,16 @@ LSH_HD void face_scatter(const AdjArgs& a, int id, int side, bool pos_normal, co
     a.Wbar[5][id] += qy2b;
     if (ORDER == 2) {
         double* const* s = (side < 2) ? a.sxb : a.syb;
-        const double sg = (side & 1) ? 1.0 : -1.0;
-        // h1 = W0 + sg (s0 - s3), h2 = W3 + sg (s3 + s6), q = W + sg s
-        s[0][id] += sg * fb.h1;
-        s[3][id] += sg * (fb.h2 - fb.h1);
-        s[1][id] += sg * qx1b;
-        s[2][id] += sg * qy1b;
-        s[4][id] += sg * qx2b;
-        s[5][id] += sg * qy2b;
+        // h1 = W0 + sg (s0 - s3), h2 = W3 + sg (s3 + s6), q = W + sg s, sg = +-1:
+        // the products by sg are sign-bit flips
+        const bool neg = !(side & 1);
+        using lshm::neg_if;
+        s[0][id] += neg_if(fb.h1, neg);
+        s[3][id] += neg_if(fb.h2 - fb.h1, neg);
+        s[1][id] += neg_if(qx1b, neg);
+        s[2][id] += neg_if(qy1b, neg);
+        s[4][id] += neg_if(qx2b, neg);
+        s[5][id] += neg_if(qy2b, neg);
     }
 }
 
@@ -1116,7 +1118,7 @@ LSH_HD void edge_adj_body(const AdjArgs& a, int x, int y, double& dtb, ConstBar&
     face_depths<ORDER>(f, id0, side0, e.A.h1, e.A.h2);
     if (e.interior) face_depths<ORDER>(f, id1, side1, e.B.h1, e.B.h2);
     else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
-    if (!((0.5 * (e.A.h1 + e.B.h1) >= kEps) || (0.5 * (e.A.h2 + e.B.h2) >= kEps))) return;  // dry edge
+    if (lt_pos(0.5 * (e.A.h1 + e.B.h1), kEps) && lt_pos(0.5 * (e.A.h2 + e.B.h2), kEps)) return;  // dry edge
     face_rest<DIR, ORDER>(f, id0, side0, pos_normal, e.A);
     e.area0 = a.geo.area[row0];
     e.inv_area0 = a.geo.inv_area[row0];
@@ -1145,23 +1147,30 @@ LSH_HD void edge_adj_body(const AdjArgs& a, int x, int y, double& dtb, ConstBar&
     EdgeOut ob;
     for (int l = 0; l < 2; ++l) {
         const int k = 3 * l;
-        const double g0[3] = {-a.accb[k][id0], -a.accb[k + 1][id0], -a.accb[k + 2][id0]};
+        // negations as sign-bit flips (integer pipe; the bits of -x)
+        using lshm::neg_if;
+        const double g0[3] = {neg_if(a.accb[k][id0], true), neg_if(a.accb[k + 1][id0], true),
+                              neg_if(a.accb[k + 2][id0], true)};
         double g1[3] = {0.0, 0.0, 0.0};
-        if (e.interior) { g1[0] = -a.accb[k][id1]; g1[1] = -a.accb[k + 1][id1]; g1[2] = -a.accb[k + 2][id1]; }
+        if (e.interior) {
+            g1[0] = neg_if(a.accb[k][id1], true);
+            g1[1] = neg_if(a.accb[k + 1][id1], true);
+            g1[2] = neg_if(a.accb[k + 2][id1], true);
+        }
         ob.m[k] = g0[0];
         ob.p[k] = g1[0];
         if (DIR == 1) {
             // d[k+1] = sg m[k+1], d[k+2] = sg m[k+2]
-            ob.m[k + 1] = pos_normal ? g0[1] : -g0[1];
-            ob.m[k + 2] = pos_normal ? g0[2] : -g0[2];
-            ob.p[k + 1] = pos_normal ? g1[1] : -g1[1];
-            ob.p[k + 2] = pos_normal ? g1[2] : -g1[2];
+            ob.m[k + 1] = neg_if(g0[1], !pos_normal);
+            ob.m[k + 2] = neg_if(g0[2], !pos_normal);
+            ob.p[k + 1] = neg_if(g1[1], !pos_normal);
+            ob.p[k + 2] = neg_if(g1[2], !pos_normal);
         } else {
             // d[k+1] = -sg m[k+2], d[k+2] = sg m[k+1]
-            ob.m[k + 1] = pos_normal ? g0[2] : -g0[2];
-            ob.m[k + 2] = pos_normal ? -g0[1] : g0[1];
-            ob.p[k + 1] = pos_normal ? g1[2] : -g1[2];
-            ob.p[k + 2] = pos_normal ? -g1[1] : g1[1];
+            ob.m[k + 1] = neg_if(g0[2], !pos_normal);
+            ob.m[k + 2] = neg_if(g0[1], pos_normal);
+            ob.p[k + 1] = neg_if(g1[2], !pos_normal);
+            ob.p[k + 2] = neg_if(g1[1], pos_normal);
         }
     }
     ob.wave = 0.0;
@@ -1275,9 +1284,14 @@ LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) 
         if (k == 3) return W[3][q] - W[6][q];
         return W[k][q];
     };
+    // minmod's choice (0: neither, 1: a, 2: b), on the bit patterns like minmod
     auto choice = [](double a, double b, double& v) -> unsigned {
-        if (a > 0.0 && b > 0.0) { if (a < b) { v = a; return 1u; } v = b; return 2u; }
-        if (a < 0.0 && b < 0.0) { if (a > b) { v = a; return 1u; } v = b; return 2u; }
+        const uint64_t ua = lshm::bits_of(a), ub = lshm::bits_of(b);
+        if (((ua << 1) != 0) && ((ub << 1) != 0) && ((ua ^ ub) >> 63) == 0) {
+            if ((ua & lshm::kMag) < (ub & lshm::kMag)) { v = a; return 1u; }
+            v = b;
+            return 2u;
+        }
         v = 0.0;
         return 0u;
     };
@@ -1295,8 +1309,9 @@ LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) 
     const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
     const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
     const double g1 = kReconThin * h1, g2 = kReconThin * h2;
-    const bool bad = (h1 + dh1x < g1) || (h1 - dh1x < g1) || (h2 + dh2x < g2) || (h2 - dh2x < g2) ||
-                     (h1 + dh1y < g1) || (h1 - dh1y < g1) || (h2 + dh2y < g2) || (h2 - dh2y < g2);
+    const int64_t k1 = okey(g1), k2 = okey(g2);
+    const bool bad = okey(h1 + dh1x) < k1 || okey(h1 - dh1x) < k1 || okey(h2 + dh2x) < k2 || okey(h2 - dh2x) < k2 ||
+                     okey(h1 + dh1y) < k1 || okey(h1 - dh1y) < k1 || okey(h2 + dh2y) < k2 || okey(h2 - dh2y) < k2;
     if (bad) return 1u << 28;
     return t;
 }
