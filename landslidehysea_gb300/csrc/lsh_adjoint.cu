@@ -48,38 +48,66 @@ namespace {
 constexpr int kAdjEdgeBlock = 128;
 constexpr int kAdjCellBlock = 128;
 // Blocks per SM the edge and volume adjoint kernels are compiled for (their
-// register budget), and whether they run as SM-sized persistent grids or
-// with one edge / cell per thread (the hardware then balances the wet
-// region's blocks across SMs).
+// register budget).  One edge or cell per thread: the hardware balances the
+// wet region's blocks across SMs.
 #ifndef LSH_ADJ_MINBLOCKS
 #define LSH_ADJ_MINBLOCKS 4
 #endif
-#ifndef LSH_ADJ_PERSISTENT
-#define LSH_ADJ_PERSISTENT 0
-#endif
+
+// 2-D tiles, as the forward kernels use: a warp covers a compact patch of
+// the grid, so fewer warps straddle a wet/dry boundary and run half empty.
+// Horizontal edges: 16 along x by 8 edge rows (warps of 16 x 2); vertical
+// edges: 8 edge columns by 16 rows (warps of 8 x 4); cells: 16 x 8.
+dim3 adj_edge_block(int dir) { return dir == 0 ? dim3(16, 8) : dim3(8, 16); }
+dim3 adj_edge_grid(int nx, int ny, int dir, int par) {
+    if (dir == 0) {
+        const int nl = (ny - par) / 2 + 1;
+        return dim3((unsigned)((nx + 15) / 16), (unsigned)((nl + 7) / 8));
+    }
+    const int nl = (nx - par) / 2 + 1;
+    return dim3((unsigned)((nl + 7) / 8), (unsigned)((ny + 15) / 16));
+}
+dim3 adj_cell_block() { return dim3(16, 8); }
+dim3 adj_cell_grid(int nx, int ny) { return dim3((unsigned)((nx + 15) / 16), (unsigned)((ny + 7) / 8)); }
+long long blocks_of(dim3 g) { return (long long)g.x * g.y; }
 constexpr int kRed = 9;        // dt adjoint + the 8 constant adjoints
 constexpr int kPartSlots = 11;  // partial-sum launches per reversed step (2 stages x 5, + initial dt)
 
 // ------------------------------------------------------------------ device helpers
 
+// Block sums of the 9 partials into out[0..8].  The partials start at +0
+// and stay +0 where nothing contributed, so an all-zero block writes +0 and
+// an all-zero component of a warp keeps its +0 without the FP64 shuffle
+// tree: the same sums, without the adds over the dry region.
 template <int BLOCK>
 __device__ void block_sum9(double v[kRed], double* out) {
     __shared__ double sh[BLOCK / 32][kRed];
+    // linear thread index (blocks are 2-D; warps are x-fastest)
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    bool nz = false;
+#pragma unroll
+    for (int k = 0; k < kRed; ++k) nz |= !lsh::is_zero(v[k]);
+    if (!__syncthreads_or(nz)) {
+        if (tid < kRed) out[tid] = 0.0;
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < kRed; ++k) {
+        if (__any_sync(0xffffffffu, !lsh::is_zero(v[k]))) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < kRed; ++k) sh[warp][k] = v[k];
     }
     __syncthreads();
-    if (threadIdx.x < kRed) {
+    if (tid < kRed) {
         double s = 0.0;
-        for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][threadIdx.x];
-        out[threadIdx.x] = s;
+        for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][tid];
+        out[tid] = s;
     }
 }
 
@@ -94,50 +122,47 @@ struct RateSel {
     double bar;
 };
 
+// One edge per thread over a 2-D tile (adj_edge_block); one partial-sum row
+// per block.
 template <int DIR, bool FIRST, int ORDER>
 __global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_MINBLOCKS) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const int nx = a.c.nx, ny = a.c.ny;
-    const int nlines = (DIR == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
-    const long long E = (DIR == 0) ? (long long)nlines * nx : (long long)nlines * ny;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x, w = blockIdx.y * blockDim.y + threadIdx.y;
     double dtb = 0.0;
     ConstBar cb;
     lsh::cb_zero(cb);
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < E;
-         idx += (long long)gridDim.x * blockDim.x) {
-        if (DIR == 0) {
-            const int t = (int)(idx / nx), x = (int)(idx - (long long)t * nx);
-            lsh::edge_adj_body<0, FIRST, ORDER>(a, x, par + 2 * t, dtb, cb);
-        } else {
-            const int y = (int)(idx / nlines), t = (int)(idx - (long long)y * nlines);
-            lsh::edge_adj_body<1, false, ORDER>(a, par + 2 * t, y, dtb, cb);
-        }
+    if (DIR == 0) {
+        // u: x along the edge row, w: edge row index t (y = par + 2 t)
+        if (u < nx && w < (ny - par) / 2 + 1) lsh::edge_adj_body<0, FIRST, ORDER>(a, u, par + 2 * w, dtb, cb);
+    } else {
+        // u: edge column index t (x = par + 2 t), w: row y
+        if (u < (nx - par) / 2 + 1 && w < ny) lsh::edge_adj_body<1, false, ORDER>(a, par + 2 * u, w, dtb, cb);
     }
     double v[kRed];
     pack9(dtb, cb, v);
-    block_sum9<kAdjEdgeBlock>(v, part + (size_t)blockIdx.x * kRed);
+    block_sum9<kAdjEdgeBlock>(v, part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * kRed);
 }
 
+// One cell per thread over 16 x 8 tiles.
 template <int MODE>
 __global__ void __launch_bounds__(kAdjCellBlock, LSH_ADJ_MINBLOCKS) k_adj_volume(AdjArgs a, const RateSel* rs, double* part) {
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
-    const long long N = (long long)a.c.nx * a.c.ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double dtb = 0.0;
     ConstBar cb;
     lsh::cb_zero(cb);
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
-        lsh::volume_adj_body<MODE>(a, (int)id, dtb, cb);
+    if (i < a.c.nx && j < a.c.ny) lsh::volume_adj_body<MODE>(a, j * a.c.nx + i, dtb, cb);
     double v[kRed];
     pack9(dtb, cb, v);
-    block_sum9<kAdjCellBlock>(v, part + (size_t)blockIdx.x * kRed);
+    block_sum9<kAdjCellBlock>(v, part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * kRed);
 }
 
 __global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
-    const long long N = (long long)a.c.nx * a.c.ny;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
-        lsh::recon_adj_cell(a, (int)id);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i < a.c.nx && j < a.c.ny) lsh::recon_adj_cell(a, j * a.c.nx + i);
 }
 
 // The recomputation's reconstruction: slopes (bit-identical to k_recon's)
@@ -443,43 +468,32 @@ AdjArgs adj_args(const lsh_adjoint* A, const double* const* W, const double* con
     return a;
 }
 
-// Blocks of an adjoint launch over `items` edges or cells.
-int adj_blocks(const lsh_adjoint* A, long long items, int block) {
-    if (LSH_ADJ_PERSISTENT) return A->grid;
-    return (int)std::max(1LL, (items + block - 1) / block);
-}
-
 // Reverse of one stage: volume (MODE), passes last-first, reconstruction.
 // Each launch writes one partial-sum row per block at A->part + *nparts;
 // *nparts advances by the blocks launched.
 template <int ORDER, int MODE>
 void rev_stage(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, long long* nparts, cudaStream_t s) {
     const int nx = A->p.nx, ny = A->p.ny;
-    const long long N = (long long)A->N;
-    auto edges = [&](int dir, int par) -> long long {
-        const int nl = (dir == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
-        return (long long)nl * ((dir == 0) ? nx : ny);
-    };
-    int g = adj_blocks(A, N, kAdjCellBlock);
-    k_adj_volume<MODE><<<g, kAdjCellBlock, 0, s>>>(a, rs, A->part + *nparts * kRed);
-    *nparts += g;
+    dim3 g = adj_cell_grid(nx, ny);
+    k_adj_volume<MODE><<<g, adj_cell_block(), 0, s>>>(a, rs, A->part + *nparts * kRed);
+    *nparts += blocks_of(g);
     a.snap[0] = snaps[2][0]; a.snap[1] = snaps[2][1];
-    g = adj_blocks(A, edges(1, 1), kAdjEdgeBlock);
-    k_adj_edges<1, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
-    *nparts += g;
+    g = adj_edge_grid(nx, ny, 1, 1);
+    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    *nparts += blocks_of(g);
     a.snap[0] = snaps[1][0]; a.snap[1] = snaps[1][1];
-    g = adj_blocks(A, edges(1, 0), kAdjEdgeBlock);
-    k_adj_edges<1, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
-    *nparts += g;
+    g = adj_edge_grid(nx, ny, 1, 0);
+    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    *nparts += blocks_of(g);
     a.snap[0] = snaps[0][0]; a.snap[1] = snaps[0][1];
-    g = adj_blocks(A, edges(0, 1), kAdjEdgeBlock);
-    k_adj_edges<0, false, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
-    *nparts += g;
+    g = adj_edge_grid(nx, ny, 0, 1);
+    k_adj_edges<0, false, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    *nparts += blocks_of(g);
     a.snap[0] = a.snap[1] = nullptr;
-    g = adj_blocks(A, edges(0, 0), kAdjEdgeBlock);
-    k_adj_edges<0, true, ORDER><<<g, kAdjEdgeBlock, 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
-    *nparts += g;
-    if (ORDER == 2) k_adj_recon<<<adj_blocks(A, N, kAdjCellBlock), kAdjCellBlock, 0, s>>>(a);
+    g = adj_edge_grid(nx, ny, 0, 0);
+    k_adj_edges<0, true, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    *nparts += blocks_of(g);
+    if (ORDER == 2) k_adj_recon<<<adj_cell_grid(nx, ny), adj_cell_block(), 0, s>>>(a);
 }
 
 void zero6(double* const* v, size_t N, cudaStream_t s) {
@@ -896,8 +910,11 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
         if (e == cudaSuccess) e = cudaMalloc(&A->argmax, sizeof(long long));
         if (e == cudaSuccess) e = cudaMalloc(&A->rsel, sizeof(RateSel));
         // partial-sum rows of one reversed step: 2 volume + 8 edge launches (+1 for dt_0)
-        const long long ecap = (N / 2 + params->nx + params->ny + kAdjEdgeBlock) / kAdjEdgeBlock + 1;
-        const long long vcap = (N + kAdjCellBlock - 1) / kAdjCellBlock;
+        long long ecap = 0;
+        for (int dir = 0; dir < 2; ++dir)
+            for (int par = 0; par < 2; ++par)
+                ecap = std::max(ecap, blocks_of(adj_edge_grid(params->nx, params->ny, dir, par)));
+        const long long vcap = blocks_of(adj_cell_grid(params->nx, params->ny));
         A->part_rows = std::max<long long>((long long)kPartSlots * A->grid, 2 * vcap + 8 * ecap + 1);
         if (e == cudaSuccess) e = cudaMalloc(&A->part, sizeof(double) * kRed * A->part_rows);
         if (e == cudaSuccess) e = cudaMalloc(&A->part2, sizeof(double) * kRed * 128);

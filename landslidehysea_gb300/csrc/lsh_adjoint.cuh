@@ -1210,9 +1210,19 @@ LSH_HD void volume_adj_body(const AdjArgs& a, int id, double& dtb, ConstBar& cb)
     const int nx = a.c.nx;
     const int j = id / nx;
     double wo[6], acc[7], wbar[6];
+    for (int k = 0; k < 6; ++k) wbar[k] = a.wbar[k][id];
+    bool any = (a.rate_cell == (long long)id);
+    for (int k = 0; k < 6; ++k) any |= !is_zero(wbar[k]);
+    if (!any) {
+        // a zero adjoint (every dry cell under the thin-layer projection):
+        // zero accumulator and slope adjoints, nothing to add upstream
+        if (a.c.order == 2)
+            for (int k = 0; k < 7; ++k) { a.sxb[k][id] = 0.0; a.syb[k][id] = 0.0; }
+        for (int k = 0; k < 7; ++k) a.accb[k][id] = 0.0;
+        return;
+    }
     for (int k = 0; k < 6; ++k) wo[k] = a.W[k][id];
     for (int k = 0; k < 7; ++k) acc[k] = a.acc[k][id];
-    for (int k = 0; k < 6; ++k) wbar[k] = a.wbar[k][id];
     if (MODE == 2) {
         for (int k = 0; k < 6; ++k) {
             a.Xbar[k][id] += 0.5 * wbar[k];
@@ -1230,8 +1240,6 @@ LSH_HD void volume_adj_body(const AdjArgs& a, int id, double& dtb, ConstBar& cb)
         acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
         acc[5] -= a.c.peso * ((gh2 * fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
     }
-    bool any = (a.rate_cell == (long long)id);
-    for (int k = 0; k < 6; ++k) any |= !is_zero(wbar[k]);
     double wob[6] = {0, 0, 0, 0, 0, 0}, accb[7] = {0, 0, 0, 0, 0, 0, 0};
     if (any) {
         const double rateb = (a.rate_cell == (long long)id && MODE != 2) ? a.rate_bar : 0.0;
@@ -1367,13 +1375,17 @@ LSH_HD void recon_adj_cell(const AdjArgs& a, int id) {
                 const unsigned ch = (t >> (2 * (7 * d + k))) & 3u;
                 if (ch == 0u) continue;
                 const double g = 0.5 * sb[k][q];
-                if (m == 0) vb[k] += (ch == 1u) ? g : -g;          // a = pc - back, b = fwd - pc
+                if (m == 0) vb[k] += lshm::neg_if(g, ch != 1u);    // a = pc - back, b = fwd - pc
                 else if (m == 1 || m == 3) { if (ch == 1u) vb[k] -= g; }  // id is q's backward neighbour
                 else { if (ch == 2u) vb[k] += g; }                 // id is q's forward neighbour
             }
         }
     }
     // recon variables: eta1 = h1 + h2 - H, eta2 = h2 - H, the discharges
+    // (no slope read by this cell carries an adjoint: nothing to add)
+    bool any = false;
+    for (int k = 0; k < 6; ++k) any |= !is_zero(vb[k]);
+    if (!any) return;
     a.Wbar[0][id] += vb[0];
     a.Wbar[3][id] += vb[0] + vb[3];
     a.Wbar[1][id] += vb[1];
