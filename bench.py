@@ -43,15 +43,29 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # per cell-update) are not counted.  tests/test_oracle_opcount.py recomputes it.
 FJORD2048_FLOPS_PER_CELL_STEP = 804.5
 
+# FP64-pipe thread instructions the step kernels execute per cell-update of
+# the 2048^2 fjord (the 12 launches of one step inside the timed range:
+# stage 2 of step 21, stage 1 of step 22), from one ncu capture
+# (profiles/fjord2048_order2_fp64_pipe.md):
+#   ncu --clock-control none --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,... \
+#       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
+#       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
+# 1.0142e9 per step / 4,194,304 cells.  The FP64 pipe takes one such
+# instruction per lane as the measured peak's DFMA does, so the peak
+# instruction rate is the measured FP64 FLOP/s / 2.
+FJORD2048_FP64_INSTR_PER_CELL_STEP = 241.81
+
 
 # DRAM bytes (read + write) per launch of each step kernel on the 2048^2
-# fjord, from one ncu capture (profiles/fjord2048_order2_dram_traffic.md):
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
-#       --clock-control none -k regex:"k_volume|k_edges|k_recon" -s 26 -c 13 \
-#       python bench.py --steps 2 --warmup 1 --no-cpu-baseline --no-e2e
+# fjord (the 12 launches of one step inside the timed range), from one ncu
+# capture (profiles/fjord2048_order2_dram_traffic.md):
+#   ncu --clock-control none --metrics dram__bytes_read.sum,dram__bytes_write.sum,... \
+#       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
+#       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
+# edge_h0 is the first (accumulator-writing) horizontal pass.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
-    "recon": 501.1e6, "edge_h0": 262.6e6, "edge_h1": 394.9e6, "edge_v0": 262.2e6, "edge_v1": 261.5e6,
-    "volume1": 625.9e6, "volume2": 827.7e6,
+    "recon": 125.95e6, "edge_h0": 397.36e6, "edge_h1": 265.34e6, "edge_v0": 266.52e6, "edge_v1": 264.58e6,
+    "volume1": 627.20e6, "volume2": 830.03e6,
 }
 
 
@@ -338,11 +352,19 @@ def run_ours(args):
                  "clock": "k_advance"}
     fp64 = None
     if fp64_peak and args.n == 2048:
-        ach = FJORD2048_FLOPS_PER_CELL_STEP * value / world / 1e9
-        fp64 = {"bound": "fp64", "achieved": round(ach, 1), "peak": round(fp64_peak, 1), "unit": "GFLOP/s",
-                "frac": round(ach / fp64_peak, 4), "flops_per_cell_step": FJORD2048_FLOPS_PER_CELL_STEP,
-                "what": "the reference scheme's FP64 operations per cell-update (oracle count, FMA = 2) x "
-                        "cell-updates/s, over the measured FP64 FMA peak (lsh_probe_fp64_peak)"}
+        rate = value / world
+        ach = FJORD2048_FP64_INSTR_PER_CELL_STEP * rate / 1e9
+        peak_i = fp64_peak / 2.0
+        fp64 = {"bound": "fp64", "achieved": round(ach, 1), "peak": round(peak_i, 1), "unit": "G FP64 instr/s",
+                "frac": round(ach / peak_i, 4), "instr_per_cell_step": FJORD2048_FP64_INSTR_PER_CELL_STEP,
+                "what": "FP64-pipe thread instructions the step kernels execute per cell-update (ncu count on "
+                        "this workload) x cell-updates/s, over the measured FP64 instruction rate "
+                        "(lsh_probe_fp64_peak DFMA GFLOP/s / 2): how busy the FP64 pipe is over the step",
+                "scheme_gflops": round(FJORD2048_FLOPS_PER_CELL_STEP * rate / 1e9, 1),
+                "scheme_flops_per_cell_step": FJORD2048_FLOPS_PER_CELL_STEP,
+                "scheme_note": "the reference scheme's FP64 operations (oracle count, FMA = 2) at this rate; "
+                               "the kernels skip exact-zero work on dry cells and single-layer edges, so this "
+                               "can exceed the FLOP peak"}
     traffic = FJORD2048_DRAM_BYTES_PER_LAUNCH.get(dom_name) if args.n == 2048 else None
     roofline = {"bound": "hbm", "kernel": f"{kernel_of[dom_name]} ({dom_name})", "achieved": round(achieved, 2),
                 "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": traffic,
