@@ -95,6 +95,9 @@ def native_lib(name):
         lib.adjl_set_component.argtypes = [ctypes.c_int]
         lib.adjl_set_bor.argtypes = [ctypes.c_double]
         lib.adjl_initial_wave_empty.restype = ctypes.c_int
+    elif name == "cmp_check":
+        lib.cmpc_check.restype = ctypes.c_longlong
+        lib.cmpc_check.argtypes = [P, ctypes.c_longlong]
     elif name == "adj_host":
         lib.adjh_run.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P, D, P, P, ctypes.c_double]
         lib.adjh_recon_check.restype = ctypes.c_longlong
