@@ -50,8 +50,10 @@ struct Item {
 // One persistent pass.  KIND 0: horizontal edges (x along the tile),
 // 1: vertical edges (edge column index along the tile), 2: cells (recon),
 // 3: cells (volume stage, MODE), per = tiles of BLOCK * per units.
+// Register caps as the single-grid kernels have them: edge passes for 5
+// resident CTAs per SM (the FP64 latency needs the warps), cell passes for 4.
 template <int KIND, bool FIRST, int ORDER, int MODE, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
+__global__ void __launch_bounds__(BLOCK, (KIND <= 1) ? 5 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
                                                        int n_items, unsigned int* counter, int par, int per) {
     __shared__ int s_item;
     for (;;) {
@@ -477,7 +479,7 @@ int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune) {
 int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best_out) {
     if (!b || trial_steps < 1) return LSH_ERR_INVALID;
     static const int edge_tiles[] = {1, 2, 4};
-    static const int edge_ctas[] = {2, 3, 4};
+    static const int edge_ctas[] = {2, 3, 4, 5, 6};
     static const int cell_tiles[] = {1, 2, 4};
     static const int cell_ctas[] = {2, 4, 8};
     cudaEvent_t e0, e1;
@@ -487,8 +489,9 @@ int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best_out) {
     best.ms_per_step = INFINITY;
     // edge configuration first (with the current cell configuration), then cells
     for (int phase = 0; phase < 2; ++phase) {
+        const int nj = (phase == 0) ? (int)(sizeof(edge_ctas) / sizeof(int)) : (int)(sizeof(cell_ctas) / sizeof(int));
         for (int i = 0; i < 3; ++i) {
-            for (int j = 0; j < 3; ++j) {
+            for (int j = 0; j < nj; ++j) {
                 lsh_tune t = best;
                 if (phase == 0) { t.edge_tile = edge_tiles[i]; t.edge_ctas_per_sm = edge_ctas[j]; }
                 else { t.cell_tile = cell_tiles[i]; t.cell_ctas_per_sm = cell_ctas[j]; }

@@ -31,12 +31,34 @@ using lsh::kRateInitBits;
 #ifndef LSH_EDGE_V_BX
 #define LSH_EDGE_V_BX 8
 #endif
+// Blocks per SM the edge and cell kernels are compiled for: a register cap
+// of 65536 / (threads * MINB).  The FP64 unit returns results through the
+// short scoreboard, and at the compiler's choice (128-168 registers, 3
+// blocks) too few warps were resident to cover that latency.  Measured on
+// the 2048^2 fjord (ms per step): edges 3 blocks 2.46, 4 2.33, 5 2.26,
+// 6 2.27.  1: the compiler's choice.
+#ifndef LSH_EDGE_MINB
+#define LSH_EDGE_MINB 5
+#endif
+#ifndef LSH_CELL_MINB
+#define LSH_CELL_MINB 1
+#endif
+#if LSH_EDGE_MINB > 1
+#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeBlock, LSH_EDGE_MINB)
+#else
+#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeBlock)
+#endif
+#if LSH_CELL_MINB > 1
+#define LSH_CELL_BOUNDS __launch_bounds__(kCellBlock, LSH_CELL_MINB)
+#else
+#define LSH_CELL_BOUNDS __launch_bounds__(kCellBlock)
+#endif
 constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeBlock / LSH_EDGE_H_BX;
 constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeBlock / LSH_EDGE_V_BX;
 
 // Horizontal edges of parity `par`: x along threadIdx.x, edge rows par, par+2, ... along threadIdx.y / blocks.y.
 template <bool FIRST, int ORDER>
-__global__ void __launch_bounds__(kEdgeBlock) k_edges_h(KArgs a, int par) {
+__global__ void LSH_EDGE_BOUNDS k_edges_h(KArgs a, int par) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
     const int x = blockIdx.x * kEdgeHBX + threadIdx.x;
@@ -49,7 +71,7 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edges_h(KArgs a, int par) {
 
 // Vertical edges of parity `par`: edge columns par, par+2, ... along threadIdx.x, rows along threadIdx.y / blocks.y.
 template <int ORDER>
-__global__ void __launch_bounds__(kEdgeBlock) k_edges_v(KArgs a, int par) {
+__global__ void LSH_EDGE_BOUNDS k_edges_v(KArgs a, int par) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
     const int t = blockIdx.x * kEdgeVBX + threadIdx.x;
@@ -90,7 +112,7 @@ __device__ __forceinline__ int cell_of_thread(int nx, int ny) {
 // Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
 // with a first-order fallback where a reconstructed depth would fall below
 // kReconThin of the cell depth.
-__global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
+__global__ void LSH_CELL_BOUNDS k_recon(KArgs a) {
     if (a.tm->done) return;
     const int id = cell_of_thread(a.c.nx, a.c.ny);
     if (id < 0) return;
@@ -100,7 +122,7 @@ __global__ void __launch_bounds__(kCellBlock) k_recon(KArgs a) {
 // MODE 0: order 1, in place; per-cell dt min.  MODE 1: order 2 stage 1
 // (W -> Wout), per-cell dt min.  MODE 2: order 2 stage 2, Wout = (Xavg + E(W)) / 2.
 template <int MODE>
-__global__ void __launch_bounds__(kCellBlock) k_volume(KArgs a) {
+__global__ void LSH_CELL_BOUNDS k_volume(KArgs a) {
     if (a.tm->done) return;
     const int id = cell_of_thread(a.c.nx, a.c.ny);
     const double dt = a.tm->dt;

@@ -178,8 +178,15 @@ class Solver:
                "lsh_set_state_device")
         return dt.value
 
-    def get_state(self):
-        out = {v: np.empty((self.ny, self.nx), dtype=np.float64) for v in VARS}
+    def get_state(self, out=None):
+        """The state as host arrays.  `out`: a dict of C-contiguous float64
+        (ny, nx) arrays to fill (e.g. pinned buffers reused across calls)."""
+        if out is None:
+            out = {v: np.empty((self.ny, self.nx), dtype=np.float64) for v in VARS}
+        for v in VARS:
+            a = out[v]
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != self.nx * self.ny:
+                raise ValueError(f"get_state: out[{v!r}] must be a C-contiguous float64 array of ny*nx values")
         _check(self.lib.lsh_get_state(self._ctx, _ptr_array([out[v].ctypes.data for v in VARS])), "lsh_get_state")
         return out
 

@@ -55,9 +55,16 @@ LSH_HD long long check_one(double x) {
     }
     bad += lsh::is_zero(x) != (x == 0.0);
     bad += lsh::is_bad(x) != !(fabs(x) <= 1.79769313486231570815e308);
-    bad += !same_bits(lshm::neg_if(x, true), -x);
     bad += !same_bits(lshm::neg_if(x, false), x);
-    bad += !same_bits(lshm::abs_bits(x), fabs(x));
+    if (!nan) {
+        bad += !same_bits(lshm::neg_if(x, true), -x);
+        bad += !same_bits(lshm::abs_bits(x), fabs(x));
+    } else {
+        // IEEE negate and abs change only the sign bit, NaN included (the
+        // device's -x and fabs may return another NaN payload)
+        bad += (bits_of(lshm::neg_if(x, true)) ^ bits_of(x)) != 0x8000000000000000ULL;
+        bad += bits_of(lshm::abs_bits(x)) != (bits_of(x) & lshm::kMag);
+    }
     // exp_neg and cbrt_pos: NaN stays NaN, the ends as before
     const double e = lshm::exp_neg(x), c = lshm::cbrt_pos(x);
     if (nan) {

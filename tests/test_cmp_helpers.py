@@ -50,7 +50,10 @@ def test_integer_pipe_helpers_equal_the_float_compares_on_the_device(gpu_lib, tm
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "--fmad=false", "-shared",
                     "-Xcompiler", "-fPIC", os.path.join(HERE, "native", "cmp_check_gpu.cu"), "-o", out], check=True)
     lib = ctypes.CDLL(out)
-    lib.cmpc_check_gpu.restype = ctypes.c_longlong
-    lib.cmpc_check_gpu.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cmpc_check_gpu.restype = ctypes.c_int
+    lib.cmpc_check_gpu.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     v = special_values()
-    assert lib.cmpc_check_gpu(v.ctypes.data, v.size) == 0
+    per = np.zeros(v.size, dtype=np.int64)
+    assert lib.cmpc_check_gpu(v.ctypes.data, v.size, per.ctypes.data) == 0
+    bad = {f"{x!r} ({np.float64(x).view(np.uint64):#018x})": int(c) for x, c in zip(v, per) if c}
+    assert not bad, bad
