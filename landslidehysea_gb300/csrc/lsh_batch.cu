@@ -314,7 +314,9 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
     }
     b->total = cells;
     const int arrays = 7 + 6 + 7 + 2 + ((b->order == 2) ? 14 : 0);
-    const size_t bytes = (size_t(arrays) * cells + geo) * sizeof(double);
+    // order 2: one slope-zero flag byte per cell after the geometry
+    const size_t flag_bytes = (b->order == 2) ? ((cells + 7) & ~size_t(7)) : 0;
+    const size_t bytes = (size_t(arrays) * cells + geo) * sizeof(double) + flag_bytes;
     { cudaError_t e = cudaMalloc(&b->slab, bytes); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc batch slab")); }
     { cudaError_t e = cudaMalloc(&b->d_tm, sizeof(lsh::TimeRec) * n); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc")); }
     { cudaError_t e = cudaMalloc(&b->d_counters, sizeof(unsigned int) * kPasses); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc")); }
@@ -325,6 +327,9 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
     double* slab = static_cast<double*>(b->slab);
     auto arr = [&](int k) { return slab + size_t(k) * cells; };
     double* geo_base = slab + size_t(arrays) * cells;
+    unsigned char* flags = reinterpret_cast<unsigned char*>(geo_base + geo);
+    // no slope is known to be zero yet (ordered before the blocking copies below)
+    if (flag_bytes) cudaMemset(flags, 0, flag_bytes);
     b->h_args.assign(nargs, KArgs{});
     for (int s = 0; s < n; ++s) {
         const lsh_params& p = params[s];
@@ -349,6 +354,7 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
                 a.sy[k] = a.syw[k] = arr(29 + k) + o;
             }
             for (int k = 0; k < 6; ++k) a.Wout[k] = arr(7 + k) + o;  // stage 1: X -> Y
+            a.szero = flags + o;  // both stages share the slopes and their flags
         }
         a.tm = b->d_tm + s;
         b->h_args[s] = a;

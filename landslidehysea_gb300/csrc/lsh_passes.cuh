@@ -110,6 +110,26 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
     }
     e.interior = (id1 >= 0);
     const int side1 = (DIR == 0) ? 2 : 0;
+    // Both cells empty (h1 = h2 = 0) with zero stored slopes (second order:
+    // the slope-zero flags): every face depth is exactly 0, so the dry test
+    // below would find the edge dry.  Integer tests only, and no slope loads:
+    // most edges of a flooded-coast grid are such edges.
+    if (ORDER == 1 || a.szero) {
+        using lsh::is_zero;
+        bool empty = is_zero(a.W[0][id0]) && is_zero(a.W[3][id0]) && (ORDER == 1 || a.szero[id0]);
+        if (empty && e.interior) empty = is_zero(a.W[0][id1]) && is_zero(a.W[3][id1]) && (ORDER == 1 || a.szero[id1]);
+        if (empty) {
+            if (FIRST) {
+#pragma unroll
+                for (int k = 0; k < 7; ++k) a.acc[k][id0] = 0.0;
+                if (e.interior) {
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) a.acc[k][id1] = 0.0;
+                }
+            }
+            return;
+        }
+    }
     face_depths<ORDER>(a, id0, side0, e.A.h1, e.A.h2);
     if (e.interior) face_depths<ORDER>(a, id1, side1, e.B.h1, e.B.h2);
     else { e.B.h1 = e.A.h1; e.B.h2 = e.A.h2; }
