@@ -338,6 +338,7 @@ struct lsh_adjoint {
     double* sxb[7] = {}, *syb[7] = {}, *accb[7] = {};
     double* eta_dummy = nullptr;
     unsigned* tape1 = nullptr, *tape2 = nullptr;
+    unsigned char* szero1 = nullptr, *szero2 = nullptr;  // slope-zero flags of s1x/s1y and s2x/s2y
     double* geo_buf = nullptr;
     Geo geo{};
     lsh::TimeRec* tm = nullptr;
@@ -395,6 +396,8 @@ KArgs fwd_args(const lsh_adjoint* A, const double* const* W, double* const* Wout
     a.eta_max = A->eta_dummy;
     a.eta_time = A->eta_dummy;
     a.tm = A->tm;
+    // each stage's slope set has its own flags (the edges' empty-cell test reads them)
+    a.szero = (sx == A->s1x) ? A->szero1 : (sx == A->s2x) ? A->szero2 : nullptr;
     return a;
 }
 
@@ -868,7 +871,7 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     const int narr = 7 + 6 + 28 + 14 + 12 + 18 + 21 + 1 + 2;
     const size_t geo_n = 7 * size_t(params->ny + 1);
     const size_t bytes = (size_t(narr) * A->npad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) +
-                         2 * A->npad * sizeof(unsigned);
+                         2 * A->npad * sizeof(unsigned) + 2 * A->npad;
     { cudaError_t e = cudaMalloc(&A->slab, bytes); if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint work arrays")); }
     {
         // zero the work arrays and wait: the geometry and gauge copies below go
@@ -894,6 +897,8 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     cur += (geo_n + 31) & ~size_t(31);
     A->tape1 = reinterpret_cast<unsigned*>(cur);
     A->tape2 = A->tape1 + A->npad;
+    A->szero1 = reinterpret_cast<unsigned char*>(A->tape2 + A->npad);  // zeroed with the slab
+    A->szero2 = A->szero1 + A->npad;
     {
         std::vector<double> g(geo_n, 0.0);
         const size_t st = size_t(params->ny + 1);

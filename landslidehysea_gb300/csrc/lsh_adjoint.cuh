@@ -1332,9 +1332,14 @@ LSH_HD unsigned recon_cell_tape(const KArgs& a, int id) {
     const int nx = a.c.nx, ny = a.c.ny;
     const int j = id / nx, i = id - j * nx;
     if (t & (1u << 28)) {
+        // zero slopes; with slope-zero flags (as recon_cell keeps them) a cell
+        // whose stored slopes are already zero skips the stores
+        if (a.szero && a.szero[id]) return t;
         for (int k = 0; k < 7; ++k) { a.sxw[k][id] = 0.0; a.syw[k][id] = 0.0; }
+        if (a.szero) a.szero[id] = 1;
         return t;
     }
+    if (a.szero) a.szero[id] = 0;
     auto rv = [&](int q, int k) -> double {
         if (k == 0) return (a.W[0][q] + a.W[3][q]) - a.W[6][q];
         if (k == 3) return a.W[3][q] - a.W[6][q];
