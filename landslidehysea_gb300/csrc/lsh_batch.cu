@@ -50,10 +50,11 @@ struct Item {
 // One persistent pass.  KIND 0: horizontal edges (x along the tile),
 // 1: vertical edges (edge column index along the tile), 2: cells (recon),
 // 3: cells (volume stage, MODE), per = tiles of BLOCK * per units.
-// Register caps as the single-grid kernels have them: edge passes for 5
-// resident CTAs per SM (the FP64 latency needs the warps), cell passes for 4.
+// Register caps like the single-grid kernels': edge passes at 64 registers
+// (8 resident CTAs of 128 per SM: the FP64 and load latencies need the
+// warps), cell passes for 4 CTAs.
 template <int KIND, bool FIRST, int ORDER, int MODE, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (KIND <= 1) ? 5 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
+__global__ void __launch_bounds__(BLOCK, (KIND <= 1) ? 8 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
                                                        int n_items, unsigned int* counter, int par, int per) {
     __shared__ int s_item;
     for (;;) {
@@ -485,7 +486,7 @@ int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune) {
 int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best_out) {
     if (!b || trial_steps < 1) return LSH_ERR_INVALID;
     static const int edge_tiles[] = {1, 2, 4};
-    static const int edge_ctas[] = {2, 3, 4, 5, 6};
+    static const int edge_ctas[] = {2, 4, 6, 8};
     static const int cell_tiles[] = {1, 2, 4};
     static const int cell_ctas[] = {2, 4, 8};
     cudaEvent_t e0, e1;

@@ -21,7 +21,7 @@ using lsh::kEdgeBlock;
 using lsh::kRateInitBits;
 
 // Thread-block shapes of the edge passes (x along threadIdx.x, lines along
-// threadIdx.y; kEdgeBlock threads): a warp spans LSH_EDGE_H_BX cells of an
+// threadIdx.y; kEdgeTile threads, below): a warp spans LSH_EDGE_H_BX cells of an
 // edge row, or LSH_EDGE_V_BX edge columns (2 LSH_EDGE_V_BX cells) of a row,
 // and 32 / BX lines, so fewer warps straddle a wet/dry front than with
 // one-line warps, while each row segment stays one contiguous load.
@@ -33,28 +33,38 @@ using lsh::kRateInitBits;
 #endif
 // Blocks per SM the edge and cell kernels are compiled for: a register cap
 // of 65536 / (threads * MINB).  The FP64 unit returns results through the
-// short scoreboard, and at the compiler's choice (128-168 registers, 3
-// blocks) too few warps were resident to cover that latency.  Measured on
-// the 2048^2 fjord (ms per step): edges 3 blocks 2.46, 4 2.33, 5 2.26,
-// 6 2.27.  1: the compiler's choice.
+// short scoreboard, and the edge passes also wait on their loads; at the
+// compiler's choice (128-168 registers, 3 blocks of 128) too few warps were
+// resident to cover both.  Measured on the 2048^2 fjord, ms per step
+// (threads x blocks per SM: registers):
+//   before the empty-edge test: 128x3 2.46, 128x4 (128) 2.33, 128x5 (96) 2.26, 128x6 2.27;
+//   after it: 128x5 2.09, 128x6 (85) 2.03, 128x7 (73) 2.01, 64x12 (85) 2.03,
+//   64x14 (73) 2.00, 64x16 (64) 1.98-1.99, 64x20 (48) 2.00, 64x24 (40) 2.13, 256x2 2.40.
+// The spills of 64 registers (a few hundred bytes) stay in L1.  1: the
+// compiler's choice.
 #ifndef LSH_EDGE_MINB
-#define LSH_EDGE_MINB 5
+#define LSH_EDGE_MINB 16
 #endif
 #ifndef LSH_CELL_MINB
 #define LSH_CELL_MINB 1
 #endif
+// Threads per edge-pass block (a tile of LSH_EDGE_H_BX x threads / BX).
+#ifndef LSH_EDGE_THREADS
+#define LSH_EDGE_THREADS 64
+#endif
+constexpr int kEdgeTile = LSH_EDGE_THREADS;
 #if LSH_EDGE_MINB > 1
-#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeBlock, LSH_EDGE_MINB)
+#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeTile, LSH_EDGE_MINB)
 #else
-#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeBlock)
+#define LSH_EDGE_BOUNDS __launch_bounds__(kEdgeTile)
 #endif
 #if LSH_CELL_MINB > 1
 #define LSH_CELL_BOUNDS __launch_bounds__(kCellBlock, LSH_CELL_MINB)
 #else
 #define LSH_CELL_BOUNDS __launch_bounds__(kCellBlock)
 #endif
-constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeBlock / LSH_EDGE_H_BX;
-constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeBlock / LSH_EDGE_V_BX;
+constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeTile / LSH_EDGE_H_BX;
+constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeTile / LSH_EDGE_V_BX;
 
 // Horizontal edges of parity `par`: x along threadIdx.x, edge rows par, par+2, ... along threadIdx.y / blocks.y.
 template <bool FIRST, int ORDER>

@@ -362,8 +362,14 @@ LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
         lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
     }
     if (MODE == 2) {
+        // the TVD-RK2 average; where both terms are zero (every dry cell) it is
+        // the AND of their patterns (+0 unless both are -0), without the FP64 pipe
 #pragma unroll
-        for (int k = 0; k < 6; ++k) w[k] = 0.5 * (a.Xavg[k][id] + w[k]);
+        for (int k = 0; k < 6; ++k) {
+            const double x = a.Xavg[k][id];
+            w[k] = (lsh::is_zero(x) && lsh::is_zero(w[k])) ? lshm::from_bits(lshm::bits_of(x) & lshm::bits_of(w[k]))
+                                                          : 0.5 * (x + w[k]);
+        }
     }
     bool bad = false;
 #pragma unroll
