@@ -361,16 +361,29 @@ LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
         }
         lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
     }
+    // A still cell whose output is the very bits already stored where it goes
+    // skips the stores: order 1 updates in place (w == wo); stage 2 writes back
+    // into the step's initial state, and the average of two equal zeros is
+    // that zero.
+    bool keep = false;
+    if (MODE == 0 && still) {
+        keep = true;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) keep &= (a.Wout[k] == a.W[k]);
+    }
     if (MODE == 2) {
         // the TVD-RK2 average; where both terms are zero (every dry cell) it is
         // the AND of their patterns (+0 unless both are -0), without the FP64 pipe
+        keep = still;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const double x = a.Xavg[k][id];
+            keep &= (a.Wout[k] == a.Xavg[k]) && (lshm::bits_of(x) == lshm::bits_of(w[k]));
             w[k] = (lsh::is_zero(x) && lsh::is_zero(w[k])) ? lshm::from_bits(lshm::bits_of(x) & lshm::bits_of(w[k]))
                                                           : 0.5 * (x + w[k]);
         }
     }
+    if (keep) return (unsigned long long)lshm::bits_of(rate);
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < 6; ++k) { a.Wout[k][id] = w[k]; bad |= lsh::is_bad(w[k]); }
