@@ -125,6 +125,11 @@ __device__ __forceinline__ int cell_of_thread(int nx, int ny) {
 // Second order: halved minmod slopes of (eta1, q1x, q1y, eta2, q2x, q2y, H)
 // with a first-order fallback where a reconstructed depth would fall below
 // kReconThin of the cell depth.
+//
+// (A variant that staged the block's 16 x 16 cells and a halo in shared
+// memory, the depths first and the other variables only for tiles with a
+// wet cell, measured 2.00 ms per 2048^2 step against 1.97 for this one: the
+// stencil's neighbour loads already hit in L1.)
 __global__ void LSH_CELL_BOUNDS k_recon(KArgs a) {
     if (a.tm->done) return;
     const int id = cell_of_thread(a.c.nx, a.c.ny);

@@ -237,21 +237,24 @@ LSH_HD double recon_var(const KArgs& a, int id, int k) {
     return a.W[k][id];
 }
 
-// One cell of the second-order reconstruction (k_recon).
-LSH_HD void recon_cell(const KArgs& a, int id) {
+// One cell of the second-order reconstruction, its inputs read through an
+// accessor w(k, di, dj) = W[k] at cell (i + di, j + dj): global memory
+// (recon_cell) or a shared-memory tile (k_recon).  Neighbours are read only
+// inside the grid.
+template <class Acc>
+LSH_HD void recon_cell_from(const KArgs& a, int id, int i, int j, const Acc& w) {
     const int nx = a.c.nx, ny = a.c.ny;
-    const int j = id / nx, i = id - j * nx;
     // A cell whose own and 4 neighbours' depths are all zero only meets dry
     // edges (a dry cell's faces always have zero depth: any nonzero depth
     // slope would make one face negative and trigger the fallback), so its
     // slopes are never read: store zeros and skip the FP64 work.
     {
         using lsh::is_zero;
-        bool dry = is_zero(a.W[0][id]) && is_zero(a.W[3][id]);
-        if (dry && i > 0) dry = is_zero(a.W[0][id - 1]) && is_zero(a.W[3][id - 1]);
-        if (dry && i < nx - 1) dry = is_zero(a.W[0][id + 1]) && is_zero(a.W[3][id + 1]);
-        if (dry && j > 0) dry = is_zero(a.W[0][id - nx]) && is_zero(a.W[3][id - nx]);
-        if (dry && j < ny - 1) dry = is_zero(a.W[0][id + nx]) && is_zero(a.W[3][id + nx]);
+        bool dry = is_zero(w(0, 0, 0)) && is_zero(w(3, 0, 0));
+        if (dry && i > 0) dry = is_zero(w(0, -1, 0)) && is_zero(w(3, -1, 0));
+        if (dry && i < nx - 1) dry = is_zero(w(0, 1, 0)) && is_zero(w(3, 1, 0));
+        if (dry && j > 0) dry = is_zero(w(0, 0, -1)) && is_zero(w(3, 0, -1));
+        if (dry && j < ny - 1) dry = is_zero(w(0, 0, 1)) && is_zero(w(3, 0, 1));
         if (dry) {
             // zero slopes; a cell whose stored slopes are already zero (and stays
             // dry, the common case far from the flow) skips the 14 stores
@@ -262,14 +265,20 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
             return;
         }
     }
+    // the reconstructed variables: eta1 = h1 + h2 - H, eta2 = h2 - H, the discharges, H
+    auto rv = [&](int k, int di, int dj) -> double {
+        if (k == 0) return (w(0, di, dj) + w(3, di, dj)) - w(6, di, dj);
+        if (k == 3) return w(3, di, dj) - w(6, di, dj);
+        return w(k, di, dj);
+    };
     double sx[7], sy[7];
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
-        const double pc = recon_var(a, id, k);
-        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - recon_var(a, id - 1, k), recon_var(a, id + 1, k) - pc) : 0.0;
-        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - recon_var(a, id - nx, k), recon_var(a, id + nx, k) - pc) : 0.0;
+        const double pc = rv(k, 0, 0);
+        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - rv(k, -1, 0), rv(k, 1, 0) - pc) : 0.0;
+        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - rv(k, 0, -1), rv(k, 0, 1) - pc) : 0.0;
     }
-    const double h1 = a.W[0][id], h2 = a.W[3][id];
+    const double h1 = w(0, 0, 0), h2 = w(3, 0, 0);
     const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
     const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
     // first order where a reconstructed depth would fall below kReconThin of
@@ -287,6 +296,13 @@ LSH_HD void recon_cell(const KArgs& a, int id) {
         a.syw[k][id] = bad ? 0.0 : sy[k];
     }
     if (a.szero) a.szero[id] = 0;  // conservative: only the dry path marks zeros
+}
+
+// One cell of the second-order reconstruction from global memory.
+LSH_HD void recon_cell(const KArgs& a, int id) {
+    const int nx = a.c.nx;
+    const int j = id / nx, i = id - j * nx;
+    recon_cell_from(a, id, i, j, [&](int k, int di, int dj) -> double { return a.W[k][id + di + dj * nx]; });
 }
 
 #if defined(__CUDACC__)
