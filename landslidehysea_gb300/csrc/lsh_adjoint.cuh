@@ -81,11 +81,13 @@ LSH_HD void sort_eig_perm(double D[4], int perm[4], int full) {
 template <bool L2>
 LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const Consts& c, double Fknown,
                     double sqrt_h, const V4& Db, double& h1b, double& h2b, double& u1b, double& u2b, double& qb,
-                    double& Fknownb, double& sqrt_hb, ConstBar& cb) {
+                    double& Fknownb, double& sqrt_hb, ConstBar& cb, bool mean_u = false) {
     const double h = L2 ? h1 + h2 : h1;
     const bool useFk = (!L2 && !lt0(Fknown));
+    // as eig: the edge average's u is u1 itself with no granular layer and h > eps_h
+    const bool direct = mean_u && is_zero(h2) && gt_pos(h, c.eps_h);
     const double F = useFk ? Fknown : vfac(h, c.eps_h);
-    const double u = q * F;
+    const double u = direct ? u1 : q * F;
     const bool useSh = !lt0(sqrt_h);
     const double cg = useSh ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     double uu = 0.0, ci = 0.0, d = 0.0, aux = 0.0, P = 0.0;
@@ -135,8 +137,12 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
     }
     if (useSh) sqrt_hb += cgb * c.sqrt_g;
     else if (gt0(cg)) hb += (cgb * c.g) / (2.0 * cg);
-    qb += ub * F;
-    Fb += ub * q;
+    if (direct) {
+        u1b += ub;
+    } else {
+        qb += ub * F;
+        Fb += ub * q;
+    }
     if (useFk) Fknownb += Fb;
     else hb += Fb * vfac_d(h, c.eps_h);
     h1b += hb;
@@ -227,7 +233,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     const double uA1 = fA1 * Aq1, uA2 = fA2 * Aq2, uB1 = fB1 * Bq1, uB2 = fB2 * Bq2;
     const double qA = L2 ? Aq1 + Aq2 : Aq1, qB = L2 ? Bq1 + Bq2 : Bq1;
     const double shA = oneA ? sa1 : -1.0, shB = oneB ? sb1 : -1.0;
-    const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, qD, c);
+    const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, qD, c, -1.0, -1.0, true);
     const V4 E0 = eig<L2>(Ah1, Ah2, uA1, uA2, qA, c, fA1, shA);
     const V4 E1 = eig<L2>(Bh1, Bh2, uB1, uB2, qB, c, fB1, shB);
     const double m01 = tmin(E0.x, E1.x);
@@ -538,7 +544,7 @@ LSH_HD void edge_flux_adj(const EdgeIn& e, double dt, const Consts& c, const Edg
     else Db.w += aut3b;
     // eigenvalue bounds
     double h1ijb = 0.0, h2ijb = 0.0, qDb = 0.0, dummyF = 0.0, dummyS = 0.0;
-    eig_adj<L2>(h1ij, h2ij, u1ij, u2ij, qD, c, -1.0, -1.0, Db, h1ijb, h2ijb, u1b, u2b, qDb, dummyF, dummyS, cb);
+    eig_adj<L2>(h1ij, h2ij, u1ij, u2ij, qD, c, -1.0, -1.0, Db, h1ijb, h2ijb, u1b, u2b, qDb, dummyF, dummyS, cb, true);
     h1ijb += qDb * u1ij;
     u1b += qDb * h1ij;
     if (L2) { h2ijb += qDb * u2ij; u2b += qDb * h2ij; }

@@ -143,11 +143,17 @@ LSH_HD void sort_eig(V4& D, int full) {
 // zero and its square root is skipped.
 template <bool L2>
 LSH_HD V4 eig(double h1, double h2, double u1, double u2, double q, const Consts& c,
-                                  double Fknown = -1.0, double sqrt_h = -1.0) {
+                                  double Fknown = -1.0, double sqrt_h = -1.0, bool mean_u = false) {
     const double h = L2 ? h1 + h2 : h1;
+    // mean_u (the edge average, q = h1 u1 + h2 u2): with no granular layer and
+    // h > eps_h, u = q vfac(h) = (h1 u1) / h1 is u1 itself -- an exact
+    // restatement the CPU oracle makes too; the single-layer edge then skips
+    // the division
+    const bool direct = mean_u && is_zero(h2) && gt_pos(h, c.eps_h);
+    double F = 0.0;
     // single layer: vfac(h1 + 0) is vfac(h1), which the caller may already hold
-    const double F = (!L2 && !lt0(Fknown)) ? Fknown : vfac(h, c.eps_h);
-    const double u = q * F;
+    if (L2 || !direct) F = (!L2 && !lt0(Fknown)) ? Fknown : vfac(h, c.eps_h);
+    const double u = direct ? u1 : q * F;
     // sqrt_h >= 0: sqrt(h1) is known and h2 == 0, so sqrt(g h) = sqrt(g) sqrt(h1)
     const double cg = !lt0(sqrt_h) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     double uu = 0.0, ci = 0.0;
@@ -259,7 +265,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         if (coul) tp2.w = (gh2 * c.r) * deta1;
     }
 
-    const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, L2 ? fmad(h1ij, u1ij, h2ij * u2ij) : h1ij * u1ij, c);
+    const V4 D = eig<L2>(h1ij, h2ij, u1ij, u2ij, L2 ? fmad(h1ij, u1ij, h2ij * u2ij) : h1ij * u1ij, c, -1.0, -1.0, true);
     const V4 E0 = eig<L2>(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, L2 ? Aq1 + Aq2 : Aq1, c, fA1, oneA ? sa1 : -1.0);
     const V4 E1 = eig<L2>(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, L2 ? Bq1 + Bq2 : Bq1, c, fB1, oneB ? sb1 : -1.0);
     const double aut1 = tmin(D.x, tmin(E0.x, E1.x));

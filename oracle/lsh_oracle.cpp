@@ -221,10 +221,13 @@ inline void sort_eig(V4<T>& D, int full) {
 // external u -+ sqrt(g h), internal uu -+ sqrt(g' h1 h2 F |1 - (u1-u2)^2 F / g'|).
 // sqrt_h >= 0: sqrt(h1) is known and h2 == 0, so sqrt(g h) = sqrt(g) sqrt(h1).
 template <class T>
-inline V4<T> eig(T h1, T h2, T u1, T u2, T q, const ConstsT<T>& c, T sqrt_h = -1.0) {
+inline V4<T> eig(T h1, T h2, T u1, T u2, T q, const ConstsT<T>& c, T sqrt_h = -1.0, bool mean_u = false) {
     const T h = h1 + h2;
     const T F = vfac(h, c.eps_h);
-    const T u = q * F;
+    // mean_u (the edge average, q = h1 u1 + h2 u2): with no granular layer and
+    // h > eps_h, u = q vfac(h) = (h1 u1) / h1 is u1 itself (an exact
+    // restatement of Arista_kernel.cu's u = q F there)
+    const T u = (mean_u && h2 == 0.0 && h > c.eps_h) ? u1 : q * F;
     const T cg = (sqrt_h >= 0.0) ? c.sqrt_g * sqrt_h : sqrt(c.g * h);
     const T uu = fmad(u1, h2, u2 * h1) * F;
     const T d = u1 - u2;
@@ -347,7 +350,7 @@ bool edge_flux(const EdgeIn<T>& e, T dt, const ConstsT<T>& c, EdgeOut<T>& o) {
     if (coul) tp2.w = (gh2 * c.r) * deta1;
 
     // eigenvalue bounds (:427-444)
-    const V4<T> D = eig(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c);
+    const V4<T> D = eig(h1ij, h2ij, u1ij, u2ij, fmad(h1ij, u1ij, h2ij * u2ij), c, T(-1.0), true);
     const V4<T> E0 = eig(Ah1, Ah2, fA1 * Aq1, fA2 * Aq2, Aq1 + Aq2, c, oneA ? sa1 : -1.0);
     const V4<T> E1 = eig(Bh1, Bh2, fB1 * Bq1, fB2 * Bq2, Bq1 + Bq2, c, oneB ? sb1 : -1.0);
     const T aut1 = tmin(D.x, tmin(E0.x, E1.x));
