@@ -615,10 +615,7 @@ int Ops::reverse_step(int n) {
 // The initial-dt wave pass over X (the same kernels as lsh_set_state).
 void init_wave_pass(const lsh_adjoint* A, const KArgs& a, cudaStream_t s) {
     const int nx = A->p.nx, ny = A->p.ny;
-    k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-    k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-    k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-    k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+    launch_init_wave(a, nx, ny, s);
 }
 
 // The steps after which the forward sweep stores a checkpoint: the binomial

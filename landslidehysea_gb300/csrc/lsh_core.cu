@@ -213,10 +213,7 @@ int upload_state(lsh_ctx* ctx, const double* const src[LSH_NVARS], cudaMemcpyKin
     init.t_end = INFINITY;
     init.dt_min = ctx->p.dt_min;
     LSH_CUDA(cudaMemcpyAsync(ctx->tm, &init, sizeof(TimeRec), cudaMemcpyHostToDevice, s));
-    k_init_wave<0, true><<<dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ctx->p.ny) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-    k_init_wave<0, false><<<dim3((ctx->p.nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ctx->p.ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-    k_init_wave<1, false><<<dim3(((ctx->p.nx) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-    k_init_wave<1, false><<<dim3(((ctx->p.nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ctx->p.ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+    launch_init_wave(a, ctx->p.nx, ctx->p.ny, s);
     k_cell_dt<<<nbc, cell_block(), 0, s>>>(a);
     k_init_finish<<<1, 1, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl);
     ctx->launches += 7;
@@ -670,10 +667,7 @@ extern "C" int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH
     const dim3 nbc = cell_grid(nx, ny);
     if (!(*dt_io > 0.0)) {
         // initial dt (ShallowWater.cu:236-257) into the time record
-        k_init_wave<0, true><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min(ny / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<0, false><<<dim3((nx + kEdgeBlock - 1) / kEdgeBlock, std::min((ny - 1) / 2 + 1, 65535)), kEdgeBlock, 0, s>>>(a, 1);
-        k_init_wave<1, false><<<dim3((nx / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 0);
-        k_init_wave<1, false><<<dim3(((nx - 1) / 2 + 1 + kEdgeBlock - 1) / kEdgeBlock, std::min(ny, 65535)), kEdgeBlock, 0, s>>>(a, 1);
+        launch_init_wave(a, nx, ny, s);
         k_cell_dt<<<nbc, cell_block(), 0, s>>>(a);
         k_noalloc_take_dt<<<1, 1, 0, s>>>(tm, 2.0 * p->cfl);
     }

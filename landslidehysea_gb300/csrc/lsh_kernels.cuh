@@ -163,18 +163,33 @@ __global__ void k_advance(TimeRec* tm, double two_cfl) {
     if (tm->err) tm->done = 1;
 }
 
-// Initial-dt edge pass (procesarAristasDeltaTInicialGPU), writing acc[6].
+// Initial-dt edge pass (procesarAristasDeltaTInicialGPU), writing acc[6]:
+// the step's edge tiles (edge_block_h/v, edge_grid_h/v).
 template <int DIR, bool FIRST>
-__global__ void __launch_bounds__(kEdgeBlock) k_init_wave(KArgs a, int par) {
+__global__ void LSH_EDGE_BOUNDS k_init_wave(KArgs a, int par) {
     const int nx = a.c.nx, ny = a.c.ny;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nlines = (DIR == 0) ? (ny - par) / 2 + 1 : (nx - par) / 2 + 1;
-    const int nalong = (DIR == 0) ? nx : ny;
-    // DIR 0: threads along x, lines along blocks.y; DIR 1: threads along edge columns
-    for (int bl = blockIdx.y; bl < ((DIR == 0) ? nlines : nalong); bl += gridDim.y) {
-        if (DIR == 0) { if (tid >= nx) return; lsh::init_wave_edge<0, FIRST>(a, tid, par + 2 * bl); }
-        else { if (tid >= nlines) return; lsh::init_wave_edge<1, FIRST>(a, par + 2 * tid, bl); }
+    if (DIR == 0) {
+        const int x = blockIdx.x * kEdgeHBX + threadIdx.x;
+        if (x >= nx) return;
+        const int nlines = (ny - par) / 2 + 1;
+        for (int t = blockIdx.y * kEdgeHBY + threadIdx.y; t < nlines; t += gridDim.y * kEdgeHBY)
+            lsh::init_wave_edge<0, FIRST>(a, x, par + 2 * t);
+    } else {
+        const int t = blockIdx.x * kEdgeVBX + threadIdx.x;
+        const int x = par + 2 * t;
+        if (x > nx) return;
+        for (int y = blockIdx.y * kEdgeVBY + threadIdx.y; y < ny; y += gridDim.y * kEdgeVBY)
+            lsh::init_wave_edge<1, FIRST>(a, x, y);
     }
+}
+
+// The four passes of the initial-dt wave sum, in the reference's order (the
+// first writes acc[6], the others add).
+inline void launch_init_wave(const KArgs& a, int nx, int ny, cudaStream_t s) {
+    k_init_wave<0, true><<<edge_grid_h(nx, ny, 0), edge_block_h(), 0, s>>>(a, 0);
+    k_init_wave<0, false><<<edge_grid_h(nx, ny, 1), edge_block_h(), 0, s>>>(a, 1);
+    k_init_wave<1, false><<<edge_grid_v(nx, ny, 0), edge_block_v(), 0, s>>>(a, 0);
+    k_init_wave<1, false><<<edge_grid_v(nx, ny, 1), edge_block_v(), 0, s>>>(a, 1);
 }
 
 // Per-cell rate of the initial wave pass (obtenerDeltaTVolumenesGPU) and its max.
