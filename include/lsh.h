@@ -271,8 +271,9 @@ int lsh_adjoint_get_times(lsh_adjoint* a, double* t_out);
  * valid after lsh_adjoint_forward, before lsh_adjoint_gradient */
 int lsh_adjoint_get_state(lsh_adjoint* a, double* const host_state[6]);
 /* ------------------------------------------------------------------------
- * Batched adjoint: n scenarios (uneven grids, each with its own parameters
- * and gauges) run forward and reversed together, for one step count.  One
+ * Batched adjoint (no counterpart in the reference): n scenarios (uneven
+ * grids, each with its own parameters and gauges) run forward and reversed
+ * together, for one step count.  One
  * checkpoint schedule drives every member with the same slot count, taken
  * from a joint budget (default 180 GB, capped by free device memory) over
  * the members' summed slot bytes; each member's kernels run on its own
