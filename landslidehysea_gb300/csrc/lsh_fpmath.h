@@ -11,8 +11,9 @@
 //       exactly 0 for x > 746 (what a correctly rounded exp returns there).
 //   cbrt_pos(x) = x^(1/3), x >= 0.  x = m 2^(3q + rem) with m in [1, 2);
 //       z ~ (m 2^rem)^(-1/3) from a quadratic first guess (4.4% error),
-//       5 Newton steps on f(z) = z^-3 - a (z <- z (4 - a z^3) / 3, no
-//       division), then a^(1/3) = a z^2 (within a few ulp, no division).
+//       4 Newton steps on f(z) = z^-3 - a (z <- z (4 - a z^3) / 3, no
+//       division; the error squares each step), then a^(1/3) = a z^2
+//       (within a few ulp, no division).
 //   log_pos(x) = ln x, x > 0.  x = m 2^e with m in [sqrt(1/2), sqrt(2)),
 //       ln m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^23.
 // Accuracy: a few ulp (tests/test_fpmath.py checks them against the C
@@ -186,7 +187,8 @@ LSH_HD double cbrt_pos(double x) {
     const double a = m * pow2i(rem);  // [1, 8)
     double z = fmad(fmad(0.0115, a, -0.1656), a, 1.1098);
     const double third = 1.0 / 3.0;
-    for (int i = 0; i < 5; ++i) {
+    // relative error 0.044 -> 4e-3 -> 3e-5 -> 2e-9 -> 1e-17: four steps
+    for (int i = 0; i < 4; ++i) {
         const double z3 = z * z * z;
         z = z * ((4.0 - a * z3) * third);
     }
