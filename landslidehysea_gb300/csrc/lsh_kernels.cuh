@@ -63,6 +63,17 @@ constexpr int kEdgeTile = LSH_EDGE_THREADS;
 #else
 #define LSH_CELL_BOUNDS __launch_bounds__(kCellBlock)
 #endif
+// The reconstruction alone: 8 blocks of 256 (32 registers) hide its load
+// latency best (2048^2 step: 1.940 ms at the compiler's 48 registers, 1.929
+// at 6 blocks, 1.921 at 8).
+#ifndef LSH_RECON_MINB
+#define LSH_RECON_MINB 8
+#endif
+#if LSH_RECON_MINB > 1
+#define LSH_RECON_BOUNDS __launch_bounds__(kCellBlock, LSH_RECON_MINB)
+#else
+#define LSH_RECON_BOUNDS __launch_bounds__(kCellBlock)
+#endif
 constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeTile / LSH_EDGE_H_BX;
 constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeTile / LSH_EDGE_V_BX;
 
@@ -130,7 +141,7 @@ __device__ __forceinline__ int cell_of_thread(int nx, int ny) {
 // memory, the depths first and the other variables only for tiles with a
 // wet cell, measured 2.00 ms per 2048^2 step against 1.97 for this one: the
 // stencil's neighbour loads already hit in L1.)
-__global__ void LSH_CELL_BOUNDS k_recon(KArgs a) {
+__global__ void LSH_RECON_BOUNDS k_recon(KArgs a) {
     if (a.tm->done) return;
     const int id = cell_of_thread(a.c.nx, a.c.ny);
     if (id < 0) return;
