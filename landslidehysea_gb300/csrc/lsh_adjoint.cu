@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
 
 // The recomputation's reconstruction: slopes (bit-identical to k_recon's)
 // and the branch tape the reconstruction adjoint replays.
-__global__ void __launch_bounds__(kCellBlock) k_recon_tape(KArgs a, unsigned* tape) {
+__global__ void __launch_bounds__(kCellBlock, 8) k_recon_tape(KArgs a, unsigned* tape) {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= a.c.nx * a.c.ny) return;
     tape[id] = lsh::recon_cell_tape(a, id);

@@ -52,9 +52,9 @@ struct Item {
 // 3: cells (volume stage, MODE), per = tiles of BLOCK * per units.
 // Register caps like the single-grid kernels': edge passes at 64 registers
 // (8 resident CTAs of 128 per SM: the FP64 and load latencies need the
-// warps), cell passes for 4 CTAs.
+// warps), the reconstruction at 32 (8 CTAs of 256), the volume update for 4.
 template <int KIND, bool FIRST, int ORDER, int MODE, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (KIND <= 1) ? 8 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
+__global__ void __launch_bounds__(BLOCK, (KIND <= 2) ? 8 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
                                                        int n_items, unsigned int* counter, int par, int per) {
     __shared__ int s_item;
     for (;;) {
