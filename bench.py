@@ -50,10 +50,10 @@ FJORD2048_FLOPS_PER_CELL_STEP = 804.0
 #   ncu --clock-control none --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,... \
 #       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
 #       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
-# 7.016e8 per step / 4,194,304 cells.  The FP64 pipe takes one such
+# 7.060e8 per step / 4,194,304 cells.  The FP64 pipe takes one such
 # instruction per lane as the measured peak's DFMA does, so the peak
 # instruction rate is the measured FP64 FLOP/s / 2.
-FJORD2048_FP64_INSTR_PER_CELL_STEP = 167.28
+FJORD2048_FP64_INSTR_PER_CELL_STEP = 168.33
 
 
 # DRAM bytes (read + write) per launch of each step kernel on the 2048^2
@@ -64,8 +64,8 @@ FJORD2048_FP64_INSTR_PER_CELL_STEP = 167.28
 #       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
 # edge_h0 is the first (accumulator-writing) horizontal pass.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
-    "recon": 141.07e6, "edge_h0": 349.59e6, "edge_h1": 198.28e6, "edge_v0": 198.31e6, "edge_v1": 192.94e6,
-    "volume1": 627.42e6, "volume2": 680.74e6,
+    "recon": 141.21e6, "edge_h0": 349.19e6, "edge_h1": 197.94e6, "edge_v0": 198.42e6, "edge_v1": 193.08e6,
+    "volume1": 627.86e6, "volume2": 679.87e6,
 }
 
 

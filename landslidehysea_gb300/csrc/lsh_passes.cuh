@@ -26,6 +26,15 @@ LSH_HD void err_or(int* word, int bit) {
 #endif
 }
 
+// p on every active lane of the warp (the thread's own p in host code).
+LSH_HD bool warp_all(bool p) {
+#if defined(__CUDA_ARCH__)
+    return __all_sync(__activemask(), p);
+#else
+    return p;
+#endif
+}
+
 struct KArgs {
     Consts c;
     Geo geo;
@@ -388,15 +397,26 @@ LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
         for (int k = 0; k < 6; ++k) keep &= (a.Wout[k] == a.W[k]);
     }
     if (MODE == 2) {
-        // the TVD-RK2 average; where both terms are zero (every dry cell) it is
-        // the AND of their patterns (+0 unless both are -0), without the FP64 pipe
+        // the TVD-RK2 average 0.5 (x + w).  Where both terms are zero (every dry
+        // cell) it is the AND of their patterns (+0 unless both are -0: the sum
+        // of opposite zeros is +0).  A warp whose cells all have only zero terms
+        // takes the AND as a whole: a per-variable select is if-converted, and
+        // its predicated-off FP64 instructions still hold the FP64 pipe.
+        double x[6];
+        bool z = true;
         keep = still;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            const double x = a.Xavg[k][id];
-            keep &= (a.Wout[k] == a.Xavg[k]) && (lshm::bits_of(x) == lshm::bits_of(w[k]));
-            w[k] = (lsh::is_zero(x) && lsh::is_zero(w[k])) ? lshm::from_bits(lshm::bits_of(x) & lshm::bits_of(w[k]))
-                                                          : 0.5 * (x + w[k]);
+            x[k] = a.Xavg[k][id];
+            z &= lsh::is_zero(x[k]) && lsh::is_zero(w[k]);
+            keep &= (a.Wout[k] == a.Xavg[k]) && (lshm::bits_of(x[k]) == lshm::bits_of(w[k]));
+        }
+        if (warp_all(z)) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = lshm::from_bits(lshm::bits_of(x[k]) & lshm::bits_of(w[k]));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = 0.5 * (x[k] + w[k]);
         }
     }
     if (keep) return (unsigned long long)lshm::bits_of(rate);
