@@ -1283,7 +1283,8 @@ LSH_HD void volume_adj_body(const AdjArgs& a, int id, double& dtb, ConstBar& cb)
 // direction d (0 x, 1 y) bits 2 (7 d + k) .. +1 hold the minmod choice (0
 // zero, 1 the backward difference, 2 the forward one); bit 28: slopes zeroed
 // (a reconstructed depth below kReconThin of the cell's, or the dry shortcut).
-LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) {
+// Without bit 28, sx and sy hold the cell's slopes (recon_cell's values).
+LSH_HD unsigned recon_tape_slopes(const double* const* W, int nx, int ny, int id, double sx[7], double sy[7]) {
     const int j = id / nx, i = id - j * nx;
     {
         bool dry = is_zero(W[0][id]) && is_zero(W[3][id]);
@@ -1310,7 +1311,6 @@ LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) 
         return 0u;
     };
     unsigned t = 0;
-    double sx[7], sy[7];
     for (int k = 0; k < 7; ++k) {
         const double pc = rv(id, k);
         double v = 0.0;
@@ -1330,13 +1330,18 @@ LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) 
     return t;
 }
 
+LSH_HD unsigned recon_tape_cell(const double* const* W, int nx, int ny, int id) {
+    double sx[7], sy[7];
+    return recon_tape_slopes(W, nx, ny, id, sx, sy);
+}
+
 // The reconstruction of recon_cell (lsh_passes.cuh) writing its slopes and
-// returning the branch tape of recon_tape_cell in one pass: the same
-// operations, so the slopes are bit-identical to recon_cell's.
+// returning the branch tape of recon_tape_cell in one pass: the slopes are
+// the halved minmod choices, the operations recon_cell performs, so they are
+// bit-identical to recon_cell's.
 LSH_HD unsigned recon_cell_tape(const KArgs& a, int id) {
-    const unsigned t = recon_tape_cell(a.W, a.c.nx, a.c.ny, id);
-    const int nx = a.c.nx, ny = a.c.ny;
-    const int j = id / nx, i = id - j * nx;
+    double sx[7], sy[7];
+    const unsigned t = recon_tape_slopes(a.W, a.c.nx, a.c.ny, id, sx, sy);
     if (t & (1u << 28)) {
         // zero slopes; with slope-zero flags (as recon_cell keeps them) a cell
         // whose stored slopes are already zero skips the stores
@@ -1346,19 +1351,10 @@ LSH_HD unsigned recon_cell_tape(const KArgs& a, int id) {
         return t;
     }
     if (a.szero) a.szero[id] = 0;
-    auto rv = [&](int q, int k) -> double {
-        if (k == 0) return (a.W[0][q] + a.W[3][q]) - a.W[6][q];
-        if (k == 3) return a.W[3][q] - a.W[6][q];
-        return a.W[k][q];
-    };
     for (int k = 0; k < 7; ++k) {
-        const double pc = rv(id, k);
-        const unsigned cx = (t >> (2 * k)) & 3u, cy = (t >> (2 * (7 + k))) & 3u;
-        // choice 1: the backward difference pc - back; 2: the forward one fwd - pc
-        a.sxw[k][id] = (cx == 0u) ? 0.0 : 0.5 * ((cx == 1u) ? pc - rv(id - 1, k) : rv(id + 1, k) - pc);
-        a.syw[k][id] = (cy == 0u) ? 0.0 : 0.5 * ((cy == 1u) ? pc - rv(id - nx, k) : rv(id + nx, k) - pc);
+        a.sxw[k][id] = sx[k];
+        a.syw[k][id] = sy[k];
     }
-    (void)ny; (void)i; (void)j;
     return t;
 }
 
@@ -1373,6 +1369,25 @@ LSH_HD void recon_adj_cell(const AdjArgs& a, int id) {
     const int nq[5] = {id, id + 1, id - 1, id + nx, id - nx};
     const int nd[5] = {-1, 0, 0, 1, 1};
     const bool ok[5] = {true, i < nx - 1, i > 0, j < ny - 1, j > 0};
+    // A warp none of whose cells is read by a slope with a nonzero adjoint
+    // skips the sums below (integer tests only): the per-slope updates are
+    // if-converted, so without the vote every warp would issue them.  In a
+    // warp that runs them, a cell without such a slope adds zeros to +0 and
+    // leaves below like a skipped one.
+    bool need = false;
+    for (int m = 0; m < 5; ++m) {
+        if (!ok[m]) continue;
+        const int q = nq[m];
+        const unsigned t = a.tape[q];
+        if (t & (1u << 28)) continue;
+        for (int d = 0; d < 2; ++d) {
+            if (m > 0 && nd[m] != d) continue;
+            const double* const* sb = d ? a.syb : a.sxb;
+            for (int k = 0; k < 6; ++k)
+                if ((t >> (2 * (7 * d + k))) & 3u) need |= !is_zero(sb[k][q]);
+        }
+    }
+    if (!warp_any(need)) return;
     for (int m = 0; m < 5; ++m) {
         if (!ok[m]) continue;
         const int q = nq[m];

@@ -35,6 +35,15 @@ LSH_HD bool warp_all(bool p) {
 #endif
 }
 
+// p on some active lane of the warp (the thread's own p in host code).
+LSH_HD bool warp_any(bool p) {
+#if defined(__CUDA_ARCH__)
+    return __any_sync(__activemask(), p);
+#else
+    return p;
+#endif
+}
+
 struct KArgs {
     Consts c;
     Geo geo;
