@@ -53,6 +53,15 @@ constexpr int kAdjCellBlock = 128;
 #ifndef LSH_ADJ_MINBLOCKS
 #define LSH_ADJ_MINBLOCKS 4
 #endif
+// The edge adjoint alone.  Its FP64 unit is busy about 40% of the time with
+// the adjoint nonzero over a wet channel, but spills, not warps, limit it:
+// a reverse sweep of 200 steps of the 1024^2 fjord (s, blocks of 128 per SM:
+// registers, stack frame) took 0.89 at 2 (255, 64-96 B), 0.83 at 3 (168,
+// 448 B), 0.84 at 4 (128, 640-700 B), 0.87 at 5, 0.89 at 6 and 0.90 at 8
+// (64, 1 KB).
+#ifndef LSH_ADJ_EDGE_MINB
+#define LSH_ADJ_EDGE_MINB LSH_ADJ_MINBLOCKS
+#endif
 
 // 2-D tiles, as the forward kernels use: a warp covers a compact patch of
 // the grid, so fewer warps straddle a wet/dry boundary and run half empty.
@@ -125,7 +134,7 @@ struct RateSel {
 // One edge per thread over a 2-D tile (adj_edge_block); one partial-sum row
 // per block.
 template <int DIR, bool FIRST, int ORDER>
-__global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_MINBLOCKS) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
+__global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_EDGE_MINB) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const int nx = a.c.nx, ny = a.c.ny;
