@@ -101,11 +101,15 @@ LSH_HD void eig_adj(double h1, double h2, double u1, double u2, double q, const 
     double e[4] = {u - cg, uu - ci, uu + ci, u + cg};
     int perm[4] = {0, 1, 2, 3};
     sort_eig_perm(e, perm, c.eig_sort);
-    double eb[4] = {0.0, 0.0, 0.0, 0.0};
-    eb[perm[0]] += Db.x;
-    eb[perm[1]] += Db.y;
-    eb[perm[2]] += Db.z;
-    eb[perm[3]] += Db.w;
+    // eb[perm[k]] = 0 + Db_k: each entry takes the one sorted adjoint whose
+    // label it is (selections on the integer pipe; a store through perm would
+    // put eb in local memory), then the same addition to +0
+    double eb[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const double v = (perm[0] == j) ? Db.x : (perm[1] == j) ? Db.y : (perm[2] == j) ? Db.z : Db.w;
+        eb[j] = 0.0 + v;
+    }
     const double ub = eb[0] + eb[3];
     const double cgb = eb[3] - eb[0];
     double Fb = 0.0, hb = 0.0;
