@@ -113,8 +113,10 @@ def fjord(n=2048, seed=0, dcell_deg=0.0002, lat_c=60.0, lon_c=10.0, r=0.48, angl
     A, lam, phi, walls sloping at wall_deg up to land at +land metres.  The
     slide is a seeded elliptic cap of `volume` m^3 on one wall at half the
     axis depth (footprint 1 - 1.2 km by 0.5 - 0.7 km, shrunk to 1/20 of a
-    small domain; thickness at most 0.9 of the local depth, so the slide
-    starts submerged; meta["volume"] is what it holds); 16 gauges sit on the
+    small domain; thickness at most 0.9 of the depth at its centre, so the
+    centre starts submerged while the upslope rim can stand above the water
+    on the steep wall -- 715 of the 2685 slide cells at 2048^2; meta["volume"]
+    is what it holds); 16 gauges sit on the
     channel axis."""
     rng = np.random.default_rng(seed)
     nx = ny = n
@@ -153,7 +155,7 @@ def fjord(n=2048, seed=0, dcell_deg=0.0002, lat_c=60.0, lon_c=10.0, r=0.48, angl
     area_row = EARTH_RADIUS ** 2 * (dcell_deg * d2r) * (np.sin(lat_e[1:] * d2r) - np.sin(lat_e[:-1] * d2r))
     vol_unit = float((shape * area_row[:, None]).sum())
     thick = volume / vol_unit if vol_unit > 0 else 0.0
-    # a submerged slide: at most 0.9 of the water depth where it is centred
+    # at most 0.9 of the water depth where it is centred (its centre submerged)
     # (half the axis depth); a thinner cap carries less than `volume`
     thick = min(thick, 0.9 * 0.5 * daxis[js])
     volume = thick * vol_unit
