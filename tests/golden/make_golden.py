@@ -4,7 +4,7 @@ for the host by oracle/build_ref.sh and driven by oracle/ref_driver.cpp,
 which replays shallowWater()'s launch order for one rank).
 
 Run here, where the reference sources exist:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]      (all cases by default)
 Each fixture (ref_<case>.npz) holds the float32 inputs, the parameters, the
 initial dt, and the reference's state, dt trace and time after each listed
 number of steps.  The reference has no tests or golden vectors of its own,
@@ -104,16 +104,34 @@ def case_slope():
     return p, st, (1, 10)
 
 
+def case_film(vmax=0.0):
+    """A 1 mm water film on a 0.1 m granular layer, moving at 100 m/s, in a
+    cell walled in by higher dry ground.  With no interlayer friction (mfc =
+    0) and no speed cap nothing damps it: the wet/dry fix zeroes its normal
+    discharge at every face, and Manning friction acts on the water only where
+    the granular layer is empty.  With vmax the filter caps it."""
+    n = 5
+    H = np.full((n, n), 5.0)
+    H[2, 2] = 10.0
+    z = np.zeros((n, n))
+    h1, h2, q1x = z.copy(), z.copy(), z.copy()
+    h1[2, 2], h2[2, 2], q1x[2, 2] = 1e-3, 0.1, 0.1
+    st = {"h1": f32(h1), "q1x": f32(q1x), "q1y": f32(z), "h2": f32(h2), "q2x": f32(z), "q2y": f32(z), "H": f32(H)}
+    p = default_params(n, n, dx=10.0, dy=10.0, cfl=0.5, r=0.5, angle_deg=10.0, mf0=0.025, mfs=0.025, eps_h=1e-5,
+                       gravity=9.81, vmax1=vmax, vmax2=vmax)
+    return p, st, (1, 50)
+
+
 CASES = {"shelf40": case_shelf, "random17x9": case_random, "dam1d": case_dam1d, "column": case_column,
-         "slope": case_slope}
+         "slope": case_slope, "film": case_film, "film_vmax20": lambda: case_film(20.0)}
 
 
-def main():
+def main(names):
     if pyoracle.build_ref() is None:
         print("reference sources not available; fixtures unchanged")
         return 1
-    for name, fn in CASES.items():
-        p, st, steps_list = fn()
+    for name in names or list(CASES):
+        p, st, steps_list = CASES[name]()
         out = {"nx": p.nx, "ny": p.ny, "steps": np.array(steps_list)}
         for k in PARAM_KEYS:
             out["p_" + k] = getattr(p, k)
@@ -132,4 +150,4 @@ def main():
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv[1:]))

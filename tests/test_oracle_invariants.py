@@ -4,6 +4,7 @@ rest, mirror symmetry, and the convergence orders of the first- and
 second-order schemes.  Run on the CPU oracle (the GPU path is bit-identical
 to it, tests/test_gpu_parity.py)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -60,6 +61,38 @@ def test_reference_sort_network_leaks_at_walls(oracle):
         out.append(abs(masses(sc.params, arrs)[1] - m0[1]) / m0[1])
     assert out[0] > 1e-12 and out[0] < 1e-9
     assert out[1] <= 1e-13
+
+
+def test_reference_keeps_a_walled_in_film_on_the_granular_layer(oracle):
+    """A water film on the granular layer, in a cell walled in by higher dry
+    ground, keeps its discharge.  The wet/dry fix zeroes its normal
+    discharge at every face (Arista_kernel.cu:301-321).  Manning friction
+    acts on the water only where h2 < eps_h (Volumen_kernel.cu:75-82), and
+    the interlayer term is proportional to mfc (:64-74).  The reference's
+    own kernels do the same (tests/golden/ref_film.npz); its speed cap
+    (:150-179) is the remedy (ref_film_vmax20.npz).  In the 2048^2 fjord,
+    films left on the slide thin towards eps_h with their discharge, and
+    u = q/h collapses dt."""
+    from gpu_cases import golden_case
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    for name, q_after in (("film", 0.1), ("film_vmax20", 0.02)):
+        ref = np.load(os.path.join(here, f"ref_{name}.npz"))["out50_q1x"][2, 2]
+        assert abs(ref - q_after) <= 1e-6 * q_after, (name, ref)
+        p, st = golden_case(name)
+        arrs = oracle.state_arrays(st)
+        oracle.run(p, arrs, 50)
+        assert abs(arrs[1][2, 2] - q_after) <= 1e-5 * q_after, (name, arrs[1][2, 2])
+        assert arrs[0][2, 2] == st["h1"][2, 2]
+    # interlayer friction damps it; without the granular layer Manning friction does
+    for change in ("mfc", "no_layer2"):
+        p, st = golden_case("film")
+        if change == "mfc":
+            p.mfc = 0.01
+        else:
+            st["h2"][2, 2] = 0.0
+        arrs = oracle.state_arrays(st)
+        oracle.run(p, arrs, 50)
+        assert abs(arrs[1][2, 2]) < 1e-2 * 0.1, (change, arrs[1][2, 2])
 
 
 @pytest.mark.parametrize("order", [1, 2])
