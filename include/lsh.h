@@ -75,7 +75,7 @@ typedef struct lsh_params {
     int32_t eig_sort;        /* 0: the reference's compare-and-swap sequence for the  */
                              /*    eigenvalue bounds (Arista_kernel.cu:193-234, with  */
                              /*    its (2,1) compare: not a full sort); 1: a true     */
-                             /*    ascending sort (mass-exact at walls, see DESIGN)   */
+                             /*    ascending sort (conserves mass at wall edges)      */
     double dx, dy;           /* Cartesian cell width / height (ancho_vol, alto_vol)   */
     double lon0, lat0;       /* spherical: corner longitude / latitude, degrees       */
     double dlon, dlat;       /* spherical: cell size, degrees                         */
@@ -155,24 +155,32 @@ int lsh_get_launch_count(lsh_ctx* ctx, long long* launches);
 
 /* Allocation-free stepping.  No counterpart in the reference.
  * For hosts that cannot allocate device memory: a coupling framework or plugin
- * host that owns every byte of GPU memory through its own pool, code running
- * while a stream is being captured into a CUDA graph (where cudaMalloc is not
- * allowed), or a real-time loop that must not pay for an allocation.  The
- * caller owns the state; this call only launches kernels.
+ * host that owns every byte of GPU memory through its own pool (a
+ * cudaMalloc behind its back would break its accounting or fail against its
+ * reservation), or a real-time loop that must not pay for an allocation.
+ * The caller owns the state.  The call allocates nothing and calls no
+ * allocating routine, but it is not launch-only: every call copies the
+ * per-row geometry and the time record (t, dt) from host memory to the
+ * device on `cuda_stream`, launches the step's kernels, copies the time
+ * record back and synchronises `cuda_stream` to read it.
  * Advances the FIRST-ORDER step (order must be 1) `nsteps` times on the
  * caller's DEVICE arrays dev_state[7] (h1 q1x q1y h2 q2x q2y H, nx*ny each,
  * updated in place) on `cuda_stream` (NULL: the legacy default stream).
  * *dt_io: the dt of the first step; <= 0 means "run the initial-dt pass
- * first".  On return *t_io and *dt_io hold the time and the next step's dt
- * (the call synchronises the stream to read them).  eta1 max is not tracked.
+ * first".  On return *t_io and *dt_io hold the time and the next step's dt.
+ * eta1 max is not tracked.
  * Its accumulators, per-row geometry and time record live in one file-scope
  * __device__ array sized for LSH_NOALLOC_MAX_CELLS cells and
  * LSH_NOALLOC_MAX_ROWS rows (about 3.9 MB), which every GPU that loads the
  * library holds until the process exits.  Larger grids are rejected with
  * LSH_ERR_INVALID.  The first call on a device looks that array's device
- * address up (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array, so calls that overlap on the GPU
- * (other streams, other host threads) race: serialise them. */
+ * address up (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  The accumulators are written, not
+ * added to, by the step's first edge pass, and the time record is rewritten
+ * by every call, so nothing left by an earlier call is read.  All calls of
+ * one process share the one array (each process has its own copy), so calls
+ * that overlap on the GPU (on other streams, or from other host threads)
+ * race: serialise them. */
 #define LSH_NOALLOC_MAX_CELLS 65536
 #define LSH_NOALLOC_MAX_ROWS  4096
 int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], int nsteps,

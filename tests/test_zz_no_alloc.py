@@ -1,7 +1,7 @@
 """lsh_step_noalloc: the entry point for callers that cannot allocate device
-memory (a host framework that owns all GPU memory through its own pool, code
-running under stream capture, a real-time loop).  It keeps its scratch in a
-static device array instead of allocating.
+memory (a host framework that owns all GPU memory through its own pool, a
+real-time loop that must not allocate).  It keeps its scratch in a static
+device array instead of allocating.
 
 Checked through the C ABI against the context API (lsh_create / lsh_set_state
 / lsh_step) on two calls in a row -- the second continues from the first, so
