@@ -16,9 +16,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liblsh_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblsh_ref.so")
+# the same kernels built with the Pouliquen friction law (COULOMB undefined)
+REF_POULIQUEN_SO = os.path.join(HERE, "_ref", "liblsh_ref_pouliquen.so")
 
 _lib = None
-_ref = None
+_ref = {}
 
 
 def build(force=False):
@@ -31,9 +33,13 @@ def build(force=False):
     return ORACLE_SO
 
 
-def build_ref(reference_root="/root/reference"):
-    """Compile the reference's kernels for the host when its sources exist."""
-    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), reference_root], check=True)
+def build_ref(reference_root=None):
+    """Compile the reference's kernels for the host when its sources exist
+    (reference_root: default $LSH_REFERENCE_ROOT, else build_ref.sh's own)."""
+    cmd = ["sh", os.path.join(HERE, "build_ref.sh")]
+    if reference_root:
+        cmd.append(reference_root)
+    subprocess.run(cmd, check=True)
     return REF_SO if os.path.exists(REF_SO) else None
 
 
@@ -61,16 +67,19 @@ def ref_available():
     return os.path.exists(REF_SO)
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        if not os.path.exists(REF_SO):
-            raise FileNotFoundError(REF_SO)
-        _ref = ctypes.CDLL(REF_SO)
+def ref_lib(pouliquen=False):
+    """The reference's kernels on the host: as shipped (Coulomb law), or
+    with the Pouliquen law."""
+    path = REF_POULIQUEN_SO if pouliquen else REF_SO
+    if path not in _ref:
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib_ = ctypes.CDLL(path)
         f = ctypes.c_float
         P = ctypes.c_void_p
-        _ref.lsh_ref_run.argtypes = [ctypes.c_int, ctypes.c_int, P] + [f] * 21 + [ctypes.c_int, P, P, P, P]
-    return _ref
+        lib_.lsh_ref_run.argtypes = [ctypes.c_int, ctypes.c_int, P] + [f] * 24 + [ctypes.c_int, P, P, P, P]
+        _ref[path] = lib_
+    return _ref[path]
 
 
 def _ptrs(arrays):
@@ -129,8 +138,9 @@ def masks(params, arrays):
 
 
 def ref_run(params, state, nsteps, eta=None):
-    """Run the reference's FP32 kernels (host build).  `state`: dict or list
-    of 7 arrays.  Returns (float32 arrays list, dt_trace, t)."""
+    """Run the reference's FP32 kernels (host build; the Pouliquen build when
+    params.friction_law is 1).  `state`: dict or list of 7 arrays.  Returns
+    (float32 arrays list, dt_trace, t)."""
     from landslidehysea_gb300._abi import VARS
     if isinstance(state, dict):
         arrs = [np.ascontiguousarray(state[v], dtype=np.float32).copy() for v in VARS]
@@ -141,8 +151,10 @@ def ref_run(params, state, nsteps, eta=None):
     p = params
     em = eta[0].ctypes.data if eta is not None else None
     et = eta[1].ctypes.data if eta is not None else None
-    ref_lib().lsh_ref_run(p.nx, p.ny, _ptrs(arrs), p.borde_sup, p.borde_inf, p.borde_izq, p.borde_der,
-                          p.dx, p.dy, p.dx * p.dy, p.cfl, p.r, p.angle1, p.peso, p.beta, p.mfc, p.mf0, p.mfs,
+    ref_lib(p.friction_law == 1).lsh_ref_run(
+                          p.nx, p.ny, _ptrs(arrs), p.borde_sup, p.borde_inf, p.borde_izq, p.borde_der,
+                          p.dx, p.dy, p.dx * p.dy, p.cfl, p.r, p.angle1, p.angle2, p.angle3, p.angle4,
+                          p.peso, p.beta, p.mfc, p.mf0, p.mfs,
                           p.vmax1, p.vmax2, p.gravity, p.eps_h, p.L, p.H, int(nsteps), trace.ctypes.data,
                           ctypes.byref(t), em, et)
     return arrs, trace, t.value

@@ -47,15 +47,18 @@ extern "C" {
 //   eta_max / eta_time: nx*ny floats each (may be NULL), initialised by the
 //             caller (Problema.cxx:542-546) and updated before every step.
 // Parameters are those of shallowWater() for one rank (id_hebra 0,
-// ultima_hebra 1) with the angle in radians.
+// ultima_hebra 1) with the angles in radians.  angulo2..4 reach the kernels
+// only in the Pouliquen build (ref_driver_pouliquen.cpp); the Coulomb law
+// reads angulo1 alone (Arista_kernel.cu:11-16).
 int lsh_ref_run(int nx, int ny, float* const* state, float borde_sup, float borde_inf, float borde_izq,
                 float borde_der, float ancho_vol, float alto_vol, float area, float CFL, float r,
-                float angulo1, float peso, float beta, float mfc, float mf0, float mfs, float vmax1, float vmax2,
+                float angulo1, float angulo2, float angulo3, float angulo4, float peso, float beta, float mfc,
+                float mf0, float mfs, float vmax1, float vmax2,
                 float gravedad, float epsilon_h, float L, float H, int nsteps, float* dt_trace, float* t_out,
                 float* eta_max, float* eta_time) {
     const int N = nx * ny;
     const int id_hebra = 0, ultima_hebra = 1;
-    const float ang = angulo1, unused = 0.0f;
+    const float ang = angulo1, ang2 = angulo2, ang3 = angulo3, ang4 = angulo4;
     std::vector<float4> tex1(size_t(ny + 2) * nx), tex2(size_t(ny + 2) * nx);
     std::vector<float4> acc1(N), acc2(N);
     std::vector<float> dtv(N);
@@ -104,12 +107,12 @@ int lsh_ref_run(int nx, int ny, float* const* state, float borde_sup, float bord
     float t = 0.0f;
     for (int it = 0; it < nsteps; ++it) {
         if (eta_max) launch(gEst, bEst, [&] { actualizarEta1MaximaGPU(etam.data(), nx, ny, t); });
-        launch(gH1, blk, [&] { procesarAristasNoComGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, unused, unused, unused, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 3, id_hebra, ultima_hebra); });
-        launch(gCom, bCom, [&] { procesarAristasComGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, unused, unused, unused, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 3, id_hebra, ultima_hebra); });
-        launch(gH2, blk, [&] { procesarAristasGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, unused, unused, unused, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 4, id_hebra, ultima_hebra); });
-        launch(gV1, blk, [&] { procesarAristasGPU(nx, ny, N, borde_izq, borde_der, alto_vol, area, r, delta_T, ang, unused, unused, unused, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 1, id_hebra, ultima_hebra); });
-        launch(gV2, blk, [&] { procesarAristasGPU(nx, ny, N, borde_izq, borde_der, alto_vol, area, r, delta_T, ang, unused, unused, unused, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 2, id_hebra, ultima_hebra); });
-        launch(gEst, bEst, [&] { obtenerEstadoYDeltaTVolumenesGPU(a1, a2, dtv.data(), nx, ny, area, CFL, r, delta_T, ang, unused, unused, unused, mfc, mf0, mfs, vmax1, vmax2, gravedad, epsilon_h, L, H); });
+        launch(gH1, blk, [&] { procesarAristasNoComGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, ang2, ang3, ang4, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 3, id_hebra, ultima_hebra); });
+        launch(gCom, bCom, [&] { procesarAristasComGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, ang2, ang3, ang4, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 3, id_hebra, ultima_hebra); });
+        launch(gH2, blk, [&] { procesarAristasGPU(nx, ny, N, borde_sup, borde_inf, ancho_vol, area, r, delta_T, ang, ang2, ang3, ang4, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 4, id_hebra, ultima_hebra); });
+        launch(gV1, blk, [&] { procesarAristasGPU(nx, ny, N, borde_izq, borde_der, alto_vol, area, r, delta_T, ang, ang2, ang3, ang4, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 1, id_hebra, ultima_hebra); });
+        launch(gV2, blk, [&] { procesarAristasGPU(nx, ny, N, borde_izq, borde_der, alto_vol, area, r, delta_T, ang, ang2, ang3, ang4, peso, beta, a1, a2, gravedad, epsilon_h, L, H, 2, id_hebra, ultima_hebra); });
+        launch(gEst, bEst, [&] { obtenerEstadoYDeltaTVolumenesGPU(a1, a2, dtv.data(), nx, ny, area, CFL, r, delta_T, ang, ang2, ang3, ang4, mfc, mf0, mfs, vmax1, vmax2, gravedad, epsilon_h, L, H); });
         t += delta_T;
         delta_T = fmin_all();
         if (dt_trace) dt_trace[it + 1] = delta_T;

@@ -29,6 +29,8 @@ from landslidehysea_gb300._abi import VARS, default_params  # noqa: E402
 
 PARAM_KEYS = ("borde_sup", "borde_inf", "borde_izq", "borde_der", "dx", "dy", "cfl", "r", "angle1",
               "mfc", "mf0", "mfs", "vmax1", "vmax2", "gravity", "eps_h", "peso", "beta", "L", "H")
+# stored only for the Pouliquen cases (the Coulomb fixtures keep their keys)
+POULIQUEN_KEYS = ("friction_law", "angle2", "angle3", "angle4")
 
 
 def f32(a):
@@ -122,8 +124,22 @@ def case_film(vmax=0.0):
     return p, st, (1, 50)
 
 
+def pouliquen(case, angles_deg):
+    """A case run with the Pouliquen friction law (Arista_kernel.cu:20-58):
+    angles (delta1..delta4) in degrees, read like Problema.cxx:246-255."""
+    p, st, steps = case()
+    p.friction_law = 1
+    p.angle1, p.angle2, p.angle3, p.angle4 = (math.radians(a) for a in angles_deg)
+    return p, st, steps
+
+
 CASES = {"shelf40": case_shelf, "random17x9": case_random, "dam1d": case_dam1d, "column": case_column,
-         "slope": case_slope, "film": case_film, "film_vmax20": lambda: case_film(20.0)}
+         "slope": case_slope, "film": case_film, "film_vmax20": lambda: case_film(20.0),
+         # the slide starts at rest (Froude number 0: the law's fr < EPSILON
+         # branch), then creeps (0 < fr < beta: the power-law branch)
+         "pouliquen_slope": lambda: pouliquen(case_slope, (4.0, 12.0, 6.0, 14.0)),
+         # granular discharges up to 1 m^2/s on 0-3 m layers (fr > beta)
+         "pouliquen_random": lambda: pouliquen(case_random, (18.0, 30.0, 21.0, 33.0))}
 
 
 def main(names):
@@ -133,7 +149,7 @@ def main(names):
     for name in names or list(CASES):
         p, st, steps_list = CASES[name]()
         out = {"nx": p.nx, "ny": p.ny, "steps": np.array(steps_list)}
-        for k in PARAM_KEYS:
+        for k in PARAM_KEYS + (POULIQUEN_KEYS if p.friction_law == 1 else ()):
             out["p_" + k] = getattr(p, k)
         for v in VARS:
             out["in_" + v] = st[v]

@@ -18,7 +18,7 @@ def golden_case(name):
     p = default_params(int(d["nx"]), int(d["ny"]))
     for k in d.files:
         if k.startswith("p_"):
-            setattr(p, k[2:], float(d[k]))
+            setattr(p, k[2:], int(d[k]) if k == "p_friction_law" else float(d[k]))
     state = {v: d["in_" + v].astype(np.float64) for v in VARS}
     return p, state
 
@@ -53,15 +53,20 @@ def case(name):
         sc.params.eig_sort = 1
         return sc.params, sc.state, 60
     if name == "pouliquen":
-        p, st = golden_case("slope")
-        p.friction_law = 1
-        p.angle1, p.angle2, p.angle3, p.angle4 = np.radians([4.0, 12.0, 6.0, 14.0])
+        # the slope fixture with the angles of ref_pouliquen_slope.npz, run longer
+        p, st = golden_case("pouliquen_slope")
+        return p, st, 20
+    if name == "pouliquen_random_o2":
+        p, st = golden_case("pouliquen_random")
+        p.order = 2
+        p.cfl = 0.45
         return p, st, 20
     raise KeyError(name)
 
 
 PARITY_CASES = ["shelf48_o1", "golden_random17x9", "golden_dam1d", "golden_column", "golden_slope",
-                "golden_shelf40", "shelf40x24_o2", "random_o2", "fjord64_o2", "fjord64_o1_sph", "pouliquen", "shelf48_o2_fullsort"]
+                "golden_shelf40", "shelf40x24_o2", "random_o2", "fjord64_o2", "fjord64_o1_sph", "pouliquen", "golden_pouliquen_random", "pouliquen_random_o2",
+                "shelf48_o2_fullsort"]
 
 
 def rel_linf(a, b):

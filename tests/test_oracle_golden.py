@@ -23,7 +23,7 @@ def load_case(path):
     p = default_params(int(d["nx"]), int(d["ny"]))
     for k in d.files:
         if k.startswith("p_"):
-            setattr(p, k[2:], float(d[k]))
+            setattr(p, k[2:], int(d[k]) if k == "p_friction_law" else float(d[k]))
     return d, p
 
 
@@ -50,3 +50,29 @@ def test_oracle_matches_reference(oracle, path):
             scale = max(np.abs(ref).max(), np.abs(d["in_" + v]).max())
             err = np.abs(arrs[i] - ref).max()
             assert err <= rtol * scale + atol, f"{v} after {n} steps: err {err:.3e} scale {scale:.3e}"
+
+
+POULIQUEN = [g for g in GOLDEN if "pouliquen" in os.path.basename(g)]
+
+
+def test_pouliquen_fixtures_present():
+    assert len(POULIQUEN) >= 2
+
+
+@pytest.mark.parametrize("path", POULIQUEN, ids=[os.path.basename(g)[4:-4] for g in POULIQUEN])
+def test_pouliquen_fixtures_tell_the_laws_apart(oracle, path):
+    """The Pouliquen fixtures come from the reference built with COULOMB
+    undefined (Arista_kernel.cu:20-58).  The oracle on the Coulomb law with
+    the same angle1 misses them by far more than the one-step FP32 bar, so
+    the match above pins the Pouliquen law itself."""
+    d, p = load_case(path)
+    assert p.friction_law == 1
+    p.friction_law = 0
+    arrs = [d["in_" + v].astype(np.float64) for v in VARS]
+    oracle.run(p, arrs, 1, dt=oracle.initial_dt(p, arrs))
+    worst = 0.0
+    for i, v in enumerate(VARS[:6]):
+        ref = d["out1_" + v].astype(np.float64)
+        scale = max(np.abs(ref).max(), np.abs(d["in_" + v]).max())
+        worst = max(worst, (np.abs(arrs[i] - ref).max() - 2e-5) / (scale * 2e-6))
+    assert worst > 10.0, f"the Coulomb law is within {worst:.1f}x of the one-step bar"
