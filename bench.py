@@ -43,30 +43,62 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # per cell-update) are not counted.  tests/test_oracle_opcount.py recomputes it.
 FJORD2048_FLOPS_PER_CELL_STEP = 804.0
 
-# FP64-pipe thread instructions the step kernels execute per cell-update of
-# the 2048^2 fjord (the 12 launches of one step inside the timed range:
-# stage 2 of step 21, stage 1 of step 22), from one ncu capture
-# (profiles/fjord2048_order2_fp64_pipe.md):
-#   ncu --clock-control none --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,... \
+# Counters of the step kernels on the 2048^2 fjord, read from ncu captures
+# (one step inside the timed range: stage 2 of step 21, stage 1 of step 22):
+#   ncu --clock-control none --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,\
+#       dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
 #       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
 #       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
-# 7.060e8 per step / 4,194,304 cells.  The FP64 pipe takes one such
-# instruction per lane as the measured peak's DFMA does, so the peak
-# instruction rate is the measured FP64 FLOP/s / 2.
+# They hold only for the kernel sources and the workload generator they were
+# captured on.  Those files are hashed (COUNTER_SOURCES); when the hash is not
+# COUNTERS_SOURCE_HASH the bench prints null for every figure derived from
+# them until a new capture replaces the numbers and the hash.
+COUNTER_SOURCES = ("landslidehysea_gb300/csrc/lsh_core.cu", "landslidehysea_gb300/csrc/lsh_kernels.cuh",
+                   "landslidehysea_gb300/csrc/lsh_passes.cuh", "landslidehysea_gb300/csrc/lsh_scheme.cuh",
+                   "landslidehysea_gb300/csrc/lsh_fpmath.h", "landslidehysea_gb300/csrc/lsh_setup.h",
+                   "landslidehysea_gb300/build.py", "landslidehysea_gb300/scenarios.py")
+COUNTERS_SOURCE_HASH = "f66c69cba4c7f9bc"
+# FP64-pipe thread instructions per cell-update of one step (7.060e8 per step
+# / 4,194,304 cells).  The FP64 pipe takes one such instruction per lane as
+# the measured peak's DFMA does, so the peak instruction rate is the measured
+# FP64 FLOP/s / 2.
 FJORD2048_FP64_INSTR_PER_CELL_STEP = 168.33
-
-
-# DRAM bytes (read + write) per launch of each step kernel on the 2048^2
-# fjord (the 12 launches of one step inside the timed range), from one ncu
-# capture (profiles/fjord2048_order2_dram_traffic.md):
-#   ncu --clock-control none --metrics dram__bytes_read.sum,dram__bytes_write.sum,... \
-#       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
-#       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
-# edge_h0 is the first (accumulator-writing) horizontal pass.
+# DRAM bytes (read + write) per launch of each step kernel; edge_h0 is the
+# first (accumulator-writing) horizontal pass.  A second-order step launches
+# recon and the four edge passes twice, each volume kernel once.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
     "recon": 141.21e6, "edge_h0": 349.19e6, "edge_h1": 197.94e6, "edge_v0": 198.42e6, "edge_v1": 193.08e6,
     "volume1": 627.86e6, "volume2": 679.87e6,
 }
+# Algorithmic HBM bytes per cell-step (FP64 state with perfect reuse): first
+# order 13 x 8 = 104 B (read 6 state + H, write 6 state); TVD-RK2 104 B for
+# stage 1 plus 152 B for stage 2 (read 6 + H + the step's initial 6, write 6).
+ALGO_BYTES_PER_CELL_STEP = {1: 104, 2: 256}
+
+
+def source_hash(paths=COUNTER_SOURCES):
+    """Short SHA-256 of the files the ncu counters depend on."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in paths:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(rel.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def counters_current():
+    return source_hash() == COUNTERS_SOURCE_HASH
+
+
+def step_dram_bytes():
+    """DRAM bytes of one second-order step from the per-launch counters."""
+    d = FJORD2048_DRAM_BYTES_PER_LAUNCH
+    return 2 * (d["recon"] + d["edge_h0"] + d["edge_h1"] + d["edge_v0"] + d["edge_v1"]) + d["volume1"] + d["volume2"]
+
+
+def edge_dram_bytes():
+    d = FJORD2048_DRAM_BYTES_PER_LAUNCH
+    return 2 * (d["edge_h0"] + d["edge_h1"] + d["edge_v0"] + d["edge_v1"])
 
 
 def flops_per_cell_step(ops):
@@ -238,17 +270,44 @@ def algorithmic_bytes_per_launch(kernel_index, order, cells):
     return nm, per[nm] * d * cells
 
 
-def cpu_baseline_sample(sc, steps):
+def _oracle(threads):
+    """The FP64 CPU oracle with `threads` OpenMP threads (0: every host core)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
-    threads = pyoracle.set_threads(0)
+    used = pyoracle.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
+    return pyoracle, used
+
+
+def time_oracle(sc, steps, warmup, threads=0):
+    """Cell-updates/s of the oracle on scenario `sc`: `warmup` untimed steps
+    from t = 0, then `steps` timed ones."""
+    pyoracle, used = _oracle(threads)
     arrs = pyoracle.state_arrays(sc.state)
-    dt0 = pyoracle.initial_dt(sc.params, arrs)
+    t, dt, _ = pyoracle.run(sc.params, arrs, warmup) if warmup else (0.0, pyoracle.initial_dt(sc.params, arrs), 0)
     t0 = time.perf_counter()
-    pyoracle.run(sc.params, arrs, steps, dt=dt0)
+    pyoracle.run(sc.params, arrs, steps, t=t, dt=dt)
     el = time.perf_counter() - t0
-    return sc.nx * sc.ny * steps / el, threads, el
+    return sc.nx * sc.ny * steps / el, used, el
+
+
+def cpu_baseline(sc, n):
+    """The bounded CPU baseline of the default run (about 15-20 s on 16
+    cores): the bench workload itself for 30 steps after 2 warm-up steps on
+    every host core; beside it the 200^2 first-order shelf of the plain
+    method for its full 1000 steps on every core, and 250 of its steps on one
+    core (the serial transcription)."""
+    from landslidehysea_gb300 import scenarios
+    v, used, el = time_oracle(sc, 30, 2)
+    c0 = scenarios.shelf(n=200)
+    v0, used0, el0 = time_oracle(c0, 1000, 0)
+    v1, _, el1 = time_oracle(c0, 250, 0, threads=1)
+    _oracle(0)
+    return {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+            "sample": f"30 steps of the {n}^2 workload after 2 warm-up steps ({el:.1f} s), FP64 oracle on "
+                      f"{used} threads",
+            "shelf200_order1_1000_steps": {"value": v0, "cores": used0, "seconds": round(el0, 2)},
+            "shelf200_order1_serial_250_steps": {"value": v1, "cores": 1, "seconds": round(el1, 2)}}
 
 
 def run_reference(args):
@@ -256,21 +315,9 @@ def run_reference(args):
     if rank != 0:
         return 0
     sc = workload(args.n)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    pyoracle.build()
-    threads = pyoracle.set_threads(0)
-    arrs = pyoracle.state_arrays(sc.state)
-    dt = pyoracle.initial_dt(sc.params, arrs)
-    t = 0.0
-    steps = max(1, min(args.steps, 12))
-    warm = max(1, min(args.warmup, 3))
-    t, dt, _ = pyoracle.run(sc.params, arrs, warm, t=t, dt=dt)
-    t0 = time.perf_counter()
-    t, dt, _ = pyoracle.run(sc.params, arrs, steps, t=t, dt=dt)
-    el = time.perf_counter() - t0
-    value = sc.nx * sc.ny * steps / el
-    sample = f"{steps} full steps of the {args.n}^2 grid after {warm} warm-up steps"
+    steps, warm = max(1, args.steps), max(1, args.warmup)
+    value, threads, el = time_oracle(sc, steps, warm)
+    sample = f"{steps} full steps of the {args.n}^2 grid after {warm} warm-up steps ({el:.1f} s)"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
             "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -330,7 +377,7 @@ def run_ours(args):
     ms = max_over_ranks(ms, dist, "cuda")
     value = whole_job_rate(world, cells * args.steps, ms * 1e-3)
 
-    # per-kernel event timing of a few extra steps (dominant kernel for the roofline)
+    # per-kernel event timing of a few extra steps (the step's kernel families)
     prof = [s.profile_step() for _ in range(3)]
     nk = len(prof[0])
     mean = [statistics.mean(p[k] for p in prof) for k in range(nk)]
@@ -339,40 +386,54 @@ def run_ours(args):
     for k in range(nk):
         nm, _ = algorithmic_bytes_per_launch(k, order, cells)
         names_ms.setdefault(nm, []).append(mean[k])
-    dom_k = max(range(nk), key=lambda k: mean[k])
-    dom_name, dom_bytes = algorithmic_bytes_per_launch(dom_k, order, cells)
     hbm, peak_kind = peaks()
-    achieved = dom_bytes / (mean[dom_k] * 1e-3) / 1e9
     try:
         fp64_peak = probe_fp64_peak(local)
     except Exception:
         fp64_peak = None
-    kernel_of = {"recon": "k_recon", "edge_h0": "k_edges_h<first>", "edge_h1": "k_edges_h", "edge_v0": "k_edges_v",
-                 "edge_v1": "k_edges_v", "volume": "k_volume<0>", "volume1": "k_volume<1>", "volume2": "k_volume<2>",
-                 "clock": "k_advance"}
+    current = counters_current() and args.n == 2048 and order == 2
+    ms_step = ms / args.steps
+    rate = value / world
     fp64 = None
-    if fp64_peak and args.n == 2048:
-        rate = value / world
-        ach = FJORD2048_FP64_INSTR_PER_CELL_STEP * rate / 1e9
+    if fp64_peak:
         peak_i = fp64_peak / 2.0
-        fp64 = {"bound": "fp64", "achieved": round(ach, 1), "peak": round(peak_i, 1), "unit": "G FP64 instr/s",
-                "frac": round(ach / peak_i, 4), "instr_per_cell_step": FJORD2048_FP64_INSTR_PER_CELL_STEP,
+        ach = FJORD2048_FP64_INSTR_PER_CELL_STEP * rate / 1e9 if current else None
+        fp64 = {"bound": "fp64", "achieved": round(ach, 1) if current else None, "peak": round(peak_i, 1),
+                "unit": "G FP64 instr/s", "frac": round(ach / peak_i, 4) if current else None,
+                "instr_per_cell_step": FJORD2048_FP64_INSTR_PER_CELL_STEP if current else None,
+                "counters_source_hash": source_hash(), "counters_current": current,
                 "what": "FP64-pipe thread instructions the step kernels execute per cell-update (ncu count on "
-                        "this workload) x cell-updates/s, over the measured FP64 instruction rate "
-                        "(lsh_probe_fp64_peak DFMA GFLOP/s / 2): how busy the FP64 pipe is over the step",
-                "scheme_gflops": round(FJORD2048_FLOPS_PER_CELL_STEP * rate / 1e9, 1),
+                        "this workload, valid for the hashed kernel sources only) x cell-updates/s, over the "
+                        "measured FP64 instruction rate (lsh_probe_fp64_peak DFMA GFLOP/s / 2)",
+                "scheme_gflops": round(FJORD2048_FLOPS_PER_CELL_STEP * rate / 1e9, 1) if args.n == 2048 else None,
                 "scheme_flops_per_cell_step": FJORD2048_FLOPS_PER_CELL_STEP,
                 "scheme_note": "the reference scheme's FP64 operations (oracle count, FMA = 2) at this rate; "
                                "the kernels skip exact-zero work on dry cells and single-layer edges, so this "
                                "can exceed the FLOP peak"}
-    traffic = FJORD2048_DRAM_BYTES_PER_LAUNCH.get(dom_name) if args.n == 2048 else None
-    roofline = {"bound": "hbm", "kernel": f"{kernel_of[dom_name]} ({dom_name})", "achieved": round(achieved, 2),
-                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": traffic,
-                "algorithmic_bytes": dom_bytes,
-                "peak_kind": f"{peak_kind} hbm_gbs", "step_kernel_ms": {k: round(statistics.mean(v), 4)
-                                                                        for k, v in names_ms.items()},
+    # the HBM roofline of the step: the algorithmic bytes per cell-step (FP64
+    # state with perfect reuse) over the step time, against the measured copy
+    # bandwidth; traffic is what ncu measured the step's launches move
+    algo = ALGO_BYTES_PER_CELL_STEP[order] * cells
+    achieved = algo / (ms_step * 1e-3) / 1e9
+    edge_ms = sum(sum(v) for k, v in names_ms.items() if k.startswith("edge"))
+    all_ms = sum(mean)
+    edge_traffic = edge_dram_bytes() if current else None
+    roofline = {"bound": "hbm", "kernel": f"whole step ({nk} launches)", "achieved": round(achieved, 2),
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5),
+                "traffic": step_dram_bytes() if current else None,
+                "algorithmic_bytes": algo, "algorithmic_bytes_per_cell_step": ALGO_BYTES_PER_CELL_STEP[order],
+                "peak_kind": f"{peak_kind} hbm_gbs",
+                "dominant_family": {
+                    "kernels": "k_edges_h / k_edges_v (4 colour passes per stage)",
+                    "launches_per_step": sum(1 for k in names_ms for _ in names_ms[k] if k.startswith("edge")),
+                    "share_of_step": round(edge_ms / all_ms, 4), "ms_per_step": round(edge_ms, 4),
+                    "dram_bytes_per_step": edge_traffic,
+                    "dram_gbs": round(edge_traffic / (edge_ms * 1e-3) / 1e9, 1) if current else None,
+                    "dram_frac": round(edge_traffic / (edge_ms * 1e-3) / 1e9 / hbm, 4) if current else None},
+                "step_kernel_ms": {k: round(statistics.mean(v), 4) for k, v in names_ms.items()},
                 "fp64_peak_gflops_measured": round(fp64_peak, 1) if fp64_peak else None,
-                "note": "FP64-pipe bound; see profiles/ for the FP64 instruction roofline"}
+                "counters_current": current,
+                "note": "the step is bound by the FP64 pipe (fp64_roofline), not by HBM"}
     s.close()
 
     e2e = None
@@ -381,16 +442,14 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, threads, el = cpu_baseline_sample(sc, 2)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"2 full steps of the {args.n}^2 grid ({el:.1f} s) with the FP64 oracle, all host threads"}
+        cpu = cpu_baseline(sc, args.n)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": config_dict(sc, args.n, {"sim_time_s": t_sim, "dt_s": dt_next}),
-                "roofline": roofline, "fp64_roofline": fp64, "cpu_baseline": cpu, "e2e": e2e,
+                "bound": "fp64", "roofline": roofline, "fp64_roofline": fp64, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches,
                 "clocks": clk.summary()}
         print(json.dumps(line), flush=True)

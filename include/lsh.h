@@ -149,6 +149,14 @@ int lsh_get_eta_max(lsh_ctx* ctx, double* eta_max, double* eta_max_time);
  * bit2 granular layer at rest (h2 >= eps_h and q2 == 0: Coulomb stop). */
 int lsh_get_masks(lsh_ctx* ctx, uint8_t* host_mask);
 
+/* The reference's gauge value at `n` cells, gathered on the device:
+ * out[g] = h1 - H at cells[g] (eta1 without the granular layer and before
+ * the Hmin shift, as ShallowWater.cu:318-331 prints it); a cell index
+ * outside the grid gives NaN.  Synchronous; moves 8 bytes per gauge to the
+ * host (the reference copies its whole layer-1 array back per gauge row,
+ * ShallowWater.cu:320). */
+int lsh_get_gauge_eta(lsh_ctx* ctx, int n, const int* cells, double* out);
+
 /* Number of kernels this library launched since the context was created
  * (each graph replay counts its kernel nodes). */
 int lsh_get_launch_count(lsh_ctx* ctx, long long* launches);

@@ -109,10 +109,21 @@ int shallowWater(lsh_dato_cluster* dc, float xmin, float ymin, float Hmin, char*
         if (!fp) { lsh_destroy(ctx); return 3; }
     }
 
+    // gauge mode: the gauge cells' h1 - H gathered on the device, 8 bytes per
+    // gauge per row (ShallowWater.cu:318-331 prints (h1 - H - Hmin) H)
+    std::vector<int> gcells;
+    std::vector<double> gval;
+    if (fp) {
+        for (int g = 0; g < num_puntos_guardar; ++g) {
+            const int c = indiceVolumenesGuardado ? indiceVolumenesGuardado[g] : -1;
+            if (c >= 0 && (size_t)c < N) gcells.push_back(c);
+        }
+        gval.resize(gcells.size());
+    }
     auto snapshot = [&](double t) -> int {
-        int st = lsh_get_state(ctx, dst);
-        if (st) return st;
         if (nc) {
+            int st = lsh_get_state(ctx, dst);
+            if (st) return st;
             std::vector<float> f[6];
             for (auto& a : f) a.resize(N);
             for (size_t c = 0; c < N; ++c) {
@@ -126,10 +137,12 @@ int shallowWater(lsh_dato_cluster* dc, float xmin, float ymin, float Hmin, char*
             return lsh_nc_write(nc, (float)(t * T), f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(),
                                 f[5].data());
         }
+        if (int st = lsh_get_gauge_eta(ctx, (int)gcells.size(), gcells.data(), gval.data())) return st;
         std::fprintf(fp, "%e", t * T);
+        size_t k = 0;
         for (int g = 0; g < num_puntos_guardar; ++g) {
             const int c = indiceVolumenesGuardado ? indiceVolumenesGuardado[g] : -1;
-            if (c >= 0 && (size_t)c < N) std::fprintf(fp, " %.8e", (h.v[0][c] - h.v[6][c] - Hmin) * H);  // :325
+            if (c >= 0 && (size_t)c < N) std::fprintf(fp, " %.8e", (gval[k++] - Hmin) * H);  // :325
             else std::fprintf(fp, " -999");
         }
         std::fprintf(fp, "\n");

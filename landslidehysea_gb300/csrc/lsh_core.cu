@@ -69,6 +69,15 @@ __global__ void k_fp64_probe(double* out, int iters, double a, double b) {
     if (s == 12345.678) out[0] = s;  // keeps the chains live; never true in practice
 }
 
+// h1 - H at the listed cells (lsh_get_gauge_eta); NaN for a cell off the grid.
+__global__ void k_gauge_eta(const double* __restrict__ h1, const double* __restrict__ H, const int* cells, int n,
+                            long long N, double* out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int c = cells[g];
+    out[g] = (c >= 0 && c < N) ? h1[c] - H[c] : __longlong_as_double(0x7ff8000000000000LL);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ context
@@ -93,6 +102,10 @@ struct lsh_ctx {
     Geo geo{};
     TimeRec* tm = nullptr;
     TimeRec* tm_host = nullptr;     // pinned mirror for reads
+    int* gauge_cells = nullptr;     // lsh_get_gauge_eta: device copy of the last cell list
+    double* gauge_out = nullptr;    // and its gathered values
+    int gauge_cap = 0;
+    std::vector<int> gauge_host;    // the cell list gauge_cells holds
     cudaGraphExec_t g_chunk = nullptr, g_one = nullptr;
     long long launches = 0;
     int kernels_per_step = 0;
@@ -373,6 +386,7 @@ int lsh_destroy(lsh_ctx* ctx) {
     if (ctx->g_chunk) cudaGraphExecDestroy(ctx->g_chunk);
     if (ctx->g_one) cudaGraphExecDestroy(ctx->g_one);
     if (ctx->slab) cudaFree(ctx->slab);
+    if (ctx->gauge_cells) cudaFree(ctx->gauge_cells);
     if (ctx->tm_host) cudaFreeHost(ctx->tm_host);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     (void)cudaGetLastError();
@@ -469,6 +483,35 @@ int lsh_get_eta_max(lsh_ctx* ctx, double* eta_max, double* eta_time) {
     if (eta_max) LSH_CUDA(cudaMemcpyAsync(eta_max, ctx->eta_max, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     if (eta_time) LSH_CUDA(cudaMemcpyAsync(eta_time, ctx->eta_time, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     LSH_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LSH_OK;
+}
+
+int lsh_get_gauge_eta(lsh_ctx* ctx, int n, const int* cells, double* out) {
+    if (!ctx || n < 0 || (n > 0 && (!cells || !out))) return LSH_ERR_INVALID;
+    if (n == 0) return LSH_OK;
+    if (n > ctx->gauge_cap) {
+        // one buffer: n cell indices, then n values (256-byte aligned)
+        if (ctx->gauge_cells) { cudaFree(ctx->gauge_cells); ctx->gauge_cells = nullptr; ctx->gauge_cap = 0; }
+        const size_t idx_bytes = (size_t(n) * sizeof(int) + 255) & ~size_t(255);
+        void* buf = nullptr;
+        LSH_CUDA(cudaMalloc(&buf, idx_bytes + size_t(n) * sizeof(double)));
+        ctx->gauge_cells = static_cast<int*>(buf);
+        ctx->gauge_out = reinterpret_cast<double*>(static_cast<char*>(buf) + idx_bytes);
+        ctx->gauge_cap = n;
+        ctx->gauge_host.clear();
+    }
+    cudaStream_t s = ctx->stream;
+    if (ctx->gauge_host.size() != size_t(n) || !std::equal(cells, cells + n, ctx->gauge_host.begin())) {
+        ctx->gauge_host.assign(cells, cells + n);
+        LSH_CUDA(cudaMemcpyAsync(ctx->gauge_cells, ctx->gauge_host.data(), size_t(n) * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
+    }
+    k_gauge_eta<<<(n + 127) / 128, 128, 0, s>>>(ctx->X[0], ctx->X[6], ctx->gauge_cells, n, (long long)ctx->N,
+                                                ctx->gauge_out);
+    ctx->launches += 1;
+    LSH_CUDA(cudaGetLastError());
+    LSH_CUDA(cudaMemcpyAsync(out, ctx->gauge_out, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    LSH_CUDA(cudaStreamSynchronize(s));
     return LSH_OK;
 }
 

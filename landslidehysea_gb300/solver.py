@@ -48,6 +48,7 @@ SIGNATURES = {
     "lsh_get_time": (ctypes.c_int, [P, DP, DP, ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_get_eta_max": (ctypes.c_int, [P, P, P]),
     "lsh_get_masks": (ctypes.c_int, [P, P]),
+    "lsh_get_gauge_eta": (ctypes.c_int, [P, ctypes.c_int, P, P]),
     "lsh_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_profile_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsh_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, DP]),
@@ -220,6 +221,15 @@ class Solver:
         m = np.empty((self.ny, self.nx), dtype=np.uint8)
         _check(self.lib.lsh_get_masks(self._ctx, m.ctypes.data), "lsh_get_masks")
         return m
+
+    def gauge_eta(self, cells):
+        """h1 - H at the given cell indices (row-major j*nx + i), gathered on
+        the device; NaN for an index outside the grid."""
+        c = np.ascontiguousarray(cells, dtype=np.int32).reshape(-1)
+        out = np.empty(c.size)
+        _check(self.lib.lsh_get_gauge_eta(self._ctx, int(c.size), c.ctypes.data if c.size else None,
+                                          out.ctypes.data if c.size else None), "lsh_get_gauge_eta")
+        return out
 
     def launch_count(self):
         n = ctypes.c_longlong()

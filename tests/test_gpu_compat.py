@@ -90,3 +90,30 @@ def test_shallow_water_entry_point(gpu_lib, oracle, tmp_path, monkeypatch, gauge
             for gi, c in enumerate(pr.gauges):
                 want = (a[0].ravel()[c] - a[6].ravel()[c] - hmin) * H
                 assert vals[1 + gi] == pytest.approx(want, rel=1e-7, abs=1e-12)
+
+
+def test_gauge_gather_equals_the_state(gpu_lib):
+    """lsh_get_gauge_eta gathers h1 - H at the gauge cells on the device: the
+    same bits as the downloaded state, NaN off the grid, and a changed cell
+    list is taken up."""
+    from landslidehysea_gb300 import scenarios
+    from landslidehysea_gb300.solver import Solver
+    sc = scenarios.fjord(n=48, dcell_deg=0.008, seed=2)
+    n = sc.nx * sc.ny
+    cells = np.array([0, 5, n // 2, n - 1, -3, n + 7], dtype=np.int32)
+    with Solver(sc.params) as s:
+        s.set_state(sc.state)
+        for k, steps in enumerate((0, 7, 3)):
+            s.step(steps)
+            s.synchronize()
+            if k == 2:
+                cells = cells[::-1].copy()
+            got = s.gauge_eta(cells)
+            st = s.get_state()
+            ref = (st["h1"] - st["H"]).reshape(-1)
+            for c, g in zip(cells, got):
+                if 0 <= c < n:
+                    assert g == ref[c], (k, c)
+                else:
+                    assert np.isnan(g), (k, c)
+        assert s.gauge_eta(np.zeros(0, dtype=np.int32)).size == 0
