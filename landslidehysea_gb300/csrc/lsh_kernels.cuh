@@ -76,31 +76,135 @@ constexpr int kEdgeTile = LSH_EDGE_THREADS;
 #endif
 constexpr int kEdgeHBX = LSH_EDGE_H_BX, kEdgeHBY = kEdgeTile / LSH_EDGE_H_BX;
 constexpr int kEdgeVBX = LSH_EDGE_V_BX, kEdgeVBY = kEdgeTile / LSH_EDGE_V_BX;
+#ifndef LSH_CELL_BX
+#define LSH_CELL_BX 16
+#endif
+constexpr int kCellBX = LSH_CELL_BX, kCellBY = kCellBlock / LSH_CELL_BX;
+
+// ---------------------------------------------------------------- pass overlap
+// The passes of a step run as consecutive kernels.  Each kernel's blocks end
+// unevenly (wet tiles carry all the FP64 work), so a whole-grid boundary
+// leaves SMs idle while the last wet tiles finish.  With `Dep` set, a pass is
+// launched as a programmatic dependent of the one before it: its blocks may
+// be scheduled once every block of that pass has started, and each of them
+// waits only for the producer's row tiles that wrote the cell rows it reads.
+// Every block of a pass adds 1 to its row tile's counter when its writes are
+// done (fence, then atomic add); a consumer's thread 0 spins on the counters
+// it needs with acquire loads, then the block synchronises.  The producer's
+// blocks have all started before a consumer block can be scheduled, so a
+// waiting block never keeps a producer block off the GPU.  Which rows a pass
+// reads and writes:
+//   horizontal edges, parity p, block row by: edge rows p + 2t,
+//     t in [4 by, 4 by + 3] (kEdgeHBY = 4 lines), cells rows y - 1 and y;
+//   vertical edges, block row by: cell rows [8 by, 8 by + 7];
+//   cell kernels, block row by: cell rows [16 by, 16 by + 15] (the
+//     reconstruction also reads the rows above and below).
+// The counters are zeroed by the clock kernel at the end of the step.
+enum DepKind : int { kDepH0 = 0, kDepH1 = 1, kDepV = 2, kDepCell = 3 };
+struct Dep {
+    const unsigned* wait = nullptr;  // producer pass's counters per block row (null: no wait)
+    unsigned* done = nullptr;        // this pass's counters per block row (null: none)
+    unsigned target = 0;             // producer blocks per block row (its gridDim.x)
+    int kind = 0;                    // producer tiling (DepKind)
+    int ntiles = 0;                  // producer block rows (its gridDim.y)
+};
+
+// Producer block rows that wrote cell rows [r0, r1].
+__device__ __forceinline__ void dep_tiles(const Dep& d, int r0, int r1, int& t0, int& t1) {
+    if (d.kind == kDepV) { t0 = r0 / kEdgeVBY; t1 = r1 / kEdgeVBY; }
+    else if (d.kind == kDepCell) { t0 = r0 / kCellBY; t1 = r1 / kCellBY; }
+    else {
+        // horizontal edge row y = p + 2 t writes cell rows y - 1 and y: the
+        // edge rows touching [r0, r1] are [r0, r1 + 1]
+        const int p = d.kind;
+        const int lo = max(r0 - p + 1, 0) / 2, hi = (r1 + 1 - p) / 2;
+        t0 = lo / kEdgeHBY;
+        t1 = max(hi, 0) / kEdgeHBY;
+    }
+    t0 = max(t0, 0);
+    t1 = min(t1, d.ntiles - 1);
+}
+
+// Start of a dependent pass's block: let the next pass be scheduled, then
+// wait (thread 0, bounded) for the producer rows [r0, r1].  A wait that runs
+// past ~2 s, or finds another block's wait already timed out, sets
+// LSH_ERR_TIMEOUT in the time record and gives up (the step is then reported
+// as failed and the clock kernel stops further steps).  Uniform per block.
+__device__ __forceinline__ void dep_begin(const Dep& d, TimeRec* tm, int r0, int r1) {
+    if (d.done) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (!d.wait) return;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        int t0, t1;
+        dep_tiles(d, r0, r1, t0, t1);
+        const int tbit = 1 << LSH_ERR_TIMEOUT;
+        volatile int* err = &tm->err;
+        unsigned long long start = 0;
+        for (int t = t0; t <= t1; ++t) {
+            unsigned ns = 32;
+            for (;;) {
+                unsigned v;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(d.wait + t) : "memory");
+                if (v >= d.target) break;
+                if (*err & tbit) { t = t1; break; }
+                unsigned long long now;
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                if (start == 0) start = now;
+                else if (now - start > 2000000000ull) { atomicOr(&tm->err, tbit); t = t1; break; }
+                __nanosleep(ns);
+                if (ns < 1024) ns *= 2;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// End of a pass's block: its writes are done; count it in its block row.
+__device__ __forceinline__ void dep_end(const Dep& d) {
+    if (!d.done) return;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        atomicAdd(d.done + blockIdx.y, 1u);
+    }
+}
 
 // Horizontal edges of parity `par`: x along threadIdx.x, edge rows par, par+2, ... along threadIdx.y / blocks.y.
+// With `d` set the grid covers every line at once (gridDim.y * kEdgeHBY >= lines).
 template <bool FIRST, int ORDER>
-__global__ void LSH_EDGE_BOUNDS k_edges_h(KArgs a, int par) {
+__global__ void LSH_EDGE_BOUNDS k_edges_h(KArgs a, int par, Dep d = Dep{}) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
+    if (d.done || d.wait) {
+        const int y0 = par + 2 * (blockIdx.y * kEdgeHBY);
+        dep_begin(d, a.tm, max(y0 - 1, 0), min(y0 + 2 * (kEdgeHBY - 1), ny - 1));
+    }
     const int x = blockIdx.x * kEdgeHBX + threadIdx.x;
-    if (x >= nx) return;
-    const double dt = a.tm->dt;
-    const int nlines = (ny - par) / 2 + 1;
-    for (int t = blockIdx.y * kEdgeHBY + threadIdx.y; t < nlines; t += gridDim.y * kEdgeHBY)
-        lsh::do_edge<0, FIRST, ORDER>(a, x, par + 2 * t, dt);
+    if (x < nx) {
+        const double dt = a.tm->dt;
+        const int nlines = (ny - par) / 2 + 1;
+        for (int t = blockIdx.y * kEdgeHBY + threadIdx.y; t < nlines; t += gridDim.y * kEdgeHBY)
+            lsh::do_edge<0, FIRST, ORDER>(a, x, par + 2 * t, dt);
+    }
+    dep_end(d);
 }
 
 // Vertical edges of parity `par`: edge columns par, par+2, ... along threadIdx.x, rows along threadIdx.y / blocks.y.
 template <int ORDER>
-__global__ void LSH_EDGE_BOUNDS k_edges_v(KArgs a, int par) {
+__global__ void LSH_EDGE_BOUNDS k_edges_v(KArgs a, int par, Dep d = Dep{}) {
     if (a.tm->done) return;
     const int nx = a.c.nx, ny = a.c.ny;
+    if (d.done || d.wait) {
+        const int y0 = blockIdx.y * kEdgeVBY;
+        dep_begin(d, a.tm, y0, min(y0 + kEdgeVBY - 1, ny - 1));
+    }
     const int t = blockIdx.x * kEdgeVBX + threadIdx.x;
     const int x = par + 2 * t;
-    if (x > nx) return;
-    const double dt = a.tm->dt;
-    for (int y = blockIdx.y * kEdgeVBY + threadIdx.y; y < ny; y += gridDim.y * kEdgeVBY)
-        lsh::do_edge<1, false, ORDER>(a, x, y, dt);
+    if (x <= nx) {
+        const double dt = a.tm->dt;
+        for (int y = blockIdx.y * kEdgeVBY + threadIdx.y; y < ny; y += gridDim.y * kEdgeVBY)
+            lsh::do_edge<1, false, ORDER>(a, x, y, dt);
+    }
+    dep_end(d);
 }
 
 // Launch shapes of the two edge passes: one edge per thread.  (Blocks that
@@ -121,10 +225,6 @@ inline dim3 edge_grid_v(int nx, int ny, int par) {
 // Cell kernels: blocks of kCellBlock threads shaped LSH_CELL_BX x
 // (kCellBlock / LSH_CELL_BX) over (x, y); LSH_CELL_BX = kCellBlock is one
 // row segment per block.
-#ifndef LSH_CELL_BX
-#define LSH_CELL_BX 16
-#endif
-constexpr int kCellBX = LSH_CELL_BX, kCellBY = kCellBlock / LSH_CELL_BX;
 inline dim3 cell_block() { return dim3(kCellBX, kCellBY); }
 inline dim3 cell_grid(int nx, int ny) { return dim3((nx + kCellBX - 1) / kCellBX, (ny + kCellBY - 1) / kCellBY); }
 // The cell of this thread, or -1 outside the grid.
@@ -141,29 +241,40 @@ __device__ __forceinline__ int cell_of_thread(int nx, int ny) {
 // memory, the depths first and the other variables only for tiles with a
 // wet cell, measured 2.00 ms per 2048^2 step against 1.97 for this one: the
 // stencil's neighbour loads already hit in L1.)
-__global__ void LSH_RECON_BOUNDS k_recon(KArgs a) {
+__global__ void LSH_RECON_BOUNDS k_recon(KArgs a, Dep d = Dep{}) {
     if (a.tm->done) return;
+    if (d.done || d.wait) {
+        const int y0 = blockIdx.y * kCellBY;
+        dep_begin(d, a.tm, max(y0 - 1, 0), min(y0 + kCellBY, a.c.ny - 1));
+    }
     const int id = cell_of_thread(a.c.nx, a.c.ny);
-    if (id < 0) return;
-    lsh::recon_cell(a, id);
+    if (id >= 0) lsh::recon_cell(a, id);
+    dep_end(d);
 }
 
 // MODE 0: order 1, in place; per-cell dt min.  MODE 1: order 2 stage 1
 // (W -> Wout), per-cell dt min.  MODE 2: order 2 stage 2, Wout = (Xavg + E(W)) / 2.
 template <int MODE>
-__global__ void LSH_CELL_BOUNDS k_volume(KArgs a) {
+__global__ void LSH_CELL_BOUNDS k_volume(KArgs a, Dep d = Dep{}) {
     if (a.tm->done) return;
+    if (d.done || d.wait) {
+        const int y0 = blockIdx.y * kCellBY;
+        dep_begin(d, a.tm, y0, min(y0 + kCellBY - 1, a.c.ny - 1));
+    }
     const int id = cell_of_thread(a.c.nx, a.c.ny);
     const double dt = a.tm->dt;
     unsigned long long bits = kRateInitBits;
     if (id >= 0) bits = lsh::volume_cell<MODE>(a, id, dt);
     if (MODE != 2) lsh::block_max_bits<kCellBlock>(bits, &a.tm->rmax_bits);
+    dep_end(d);
 }
 
 
 // Advance the device clock: t += dt, dt = min per-cell dt (ShallowWater.cu:436-442).
-__global__ void k_advance(TimeRec* tm, double two_cfl) {
-    if (tm->done) return;
+// With `ctr`, its threads also zero the n_ctr pass-overlap counters of the step.
+__global__ void k_advance(TimeRec* tm, double two_cfl, unsigned* ctr = nullptr, int n_ctr = 0) {
+    for (int i = threadIdx.x; i < n_ctr; i += blockDim.x) ctr[i] = 0u;
+    if (threadIdx.x != 0 || tm->done) return;
     tm->t += tm->dt;
     tm->steps += 1;
     const double nd = lsh::dt_of(tm->rmax_bits, two_cfl);

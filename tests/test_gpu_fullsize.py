@@ -56,3 +56,33 @@ def test_fjord2048_mass_conserved_with_walls(gpu_lib):
         m1 = mass(s.get_state())
     for a, b in zip(m0, m1):
         assert abs(b - a) <= 1e-12 * a, (a, b)
+
+
+@pytest.mark.parametrize("order", [2, 1])
+def test_fjord2048_overlapped_passes_equal_ordered_launches(gpu_lib, order):
+    """lsh_step replays the step with its passes overlapped (programmatic
+    dependent launches that wait on per-row counters); lsh_profile_step
+    launches the same kernels one after the other with full ordering.  Over
+    40 steps of the full 2048^2 grid -- thousands of blocks per pass, many
+    resident at once -- the two give the same bits."""
+    from landslidehysea_gb300.solver import Solver
+    sc = _fjord()
+    p = copy.copy(sc.params)
+    p.order = order
+    n = 40
+    with Solver(p) as s:
+        s.set_state(sc.state)
+        s.step(n)
+        s.synchronize()
+        a = s.get_state()
+        ta = s.time()
+    with Solver(p) as s:
+        s.set_state(sc.state)
+        for _ in range(n):
+            s.profile_step()
+        s.synchronize()
+        b = s.get_state()
+        tb = s.time()
+    assert ta == tb
+    for v in VARS[:6]:
+        assert np.array_equal(a[v], b[v]), v
