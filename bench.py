@@ -117,7 +117,8 @@ def parse():
     ap.add_argument("--n", type=int, default=2048, help="grid size (n x n); the headline is 2048")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint", "adjoint-batch"), default="fjord",
+    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint", "adjoint-batch", "adjoint-fd"),
+                    default="fjord",
                     help="fjord: the 2048^2 headline; ensemble: the batched 256-scenario ensemble vs serial; "
                          "adjoint: gradient of the 16-gauge misfit on the 1024^2 fjord vs its forward")
     ap.add_argument("--adj-n", type=int, default=1024, help="adjoint workload grid size")
@@ -125,6 +126,11 @@ def parse():
     ap.add_argument("--adj-budget-gb", type=float, default=None, help="checkpoint budget (default 180 GB or free)")
     ap.add_argument("--adj-thin", type=float, default=0.1,
                     help="thin-layer projection of the adjoint, metres (0: the exact adjoint)")
+    ap.add_argument("--fd-steps", type=int, default=500, help="adjoint-fd workload steps")
+    ap.add_argument("--vmax", type=float, default=0.0,
+                    help="adjoint and adjoint-fd workloads: speed caps vmax1 = vmax2 in m/s (0: off, as configured)")
+    ap.add_argument("--fd-rels", default="1e-2,1e-3,1e-4,1e-5,1e-6",
+                    help="adjoint-fd relative difference steps (the last is the reference)")
     ap.add_argument("--count", type=int, default=256, help="ensemble scenarios")
     ap.add_argument("--cal-count", type=int, default=64, help="batched-adjoint scenarios")
     ap.add_argument("--cal-steps", type=int, default=300, help="batched-adjoint steps (the full calibration: 3000)")
@@ -609,6 +615,8 @@ def run_adjoint(args):
     from landslidehysea_gb300.solver import Adjoint, Solver
     sc = scenarios.fjord(n=args.adj_n)
     p = sc.params
+    if args.vmax > 0:
+        p.vmax1 = p.vmax2 = args.vmax
     ij = [(int(i), int(j)) for i, j in sc.gauges if i >= 0 and j >= 0]
     gauges = np.array([j * p.nx + i for i, j in ij], dtype=np.int32)
     nsteps = args.adj_steps
@@ -653,6 +661,113 @@ def run_adjoint(args):
             "forward_s": t_fwd, "adjoint_forward_s": t1 - t0, "adjoint_gradient_s": t2 - t1, "misfit": J,
             "grad_params": gp, "grad_h2_l2": float(np.linalg.norm(g["h2"])), "stats": st,
             "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def twin_target(p, state, gauges, nsteps, seed=2024):
+    """The adjoint workload's calibration target: the gauge series of a twin
+    run whose (angle1, mf0, mfs, r) are scaled by seeded +-5%."""
+    import copy
+    import numpy as np
+    from landslidehysea_gb300.solver import Adjoint
+    rng = np.random.default_rng(seed)
+    twin = copy.copy(p)
+    f = 1.0 + 0.05 * rng.choice([-1.0, 1.0], 4)
+    twin.angle1, twin.mf0, twin.mfs, twin.r = p.angle1 * f[0], p.mf0 * f[1], p.mfs * f[2], p.r * f[3]
+    with Adjoint(twin, gauges) as T:
+        T.set_budget(0.0 + 6 * 8 * (p.nx * p.ny + 32) + 1.0)
+        _, target = T.forward(state, nsteps)
+    return target, f
+
+
+def run_adjoint_fd(args):
+    """Finite-difference check of the adjoint workload's parameter gradient:
+    the 16-gauge misfit J of an N-step run of the n^2 second-order fjord
+    against its twin's gauge series (as --workload adjoint), differentiated
+    with respect to (angle1, mf0, mfs, r) by lsh_adjoint_gradient -- the
+    exact discrete adjoint (thin-layer projection 0) and the projected one
+    (--adj-thin) -- and by FP64 central differences of J itself,
+    (J(p + d e_k) - J(p - d e_k)) / 2d, at relative steps d / |p_k| of
+    --fd-rels (default 1e-2 ... 1e-6).  Prints the gradients, the
+    differences and their relative gaps; `value` is the projected gradient's
+    largest relative gap to the difference at the last step.  `roughness`
+    holds J and the simulated time after the N steps at angle1 (1 + k 1e-7),
+    k = -3..3: a discrete branch switch (the CFL step's arg-max cell, a speed
+    cap) shows there as a jump that no finite difference can resolve."""
+    import copy
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from landslidehysea_gb300 import build as B
+    B.build()
+    from landslidehysea_gb300 import scenarios
+    from landslidehysea_gb300.solver import Adjoint
+    sc = scenarios.fjord(n=args.adj_n)
+    p = sc.params
+    if args.vmax > 0:
+        p.vmax1 = p.vmax2 = args.vmax
+    gauges = scenarios.gauge_cells(sc)
+    n = args.fd_steps
+    target, f = twin_target(p, sc.state, gauges, n)
+    names = ("angle1", "mf0", "mfs", "r")
+    slot = 6 * 8 * (p.nx * p.ny + 32)
+
+    def misfit(q, with_time=False):
+        with Adjoint(q, gauges, device=local) as A:
+            A.set_budget(slot + 1.0)
+            J, _ = A.forward(sc.state, n, target)
+            t_end = float(A.times()[-1])
+        return (J, t_end) if with_time else J
+
+    t0 = time.perf_counter()
+    grads = {}
+    for label, thin in (("exact", 0.0), ("projected", args.adj_thin)):
+        with Adjoint(p, gauges, device=local) as A:
+            if thin:
+                A.set_thin_layer(thin)
+            J0, _ = A.forward(sc.state, n, target)
+            _, gp = A.gradient()
+        grads[label] = {k: gp[k] for k in names}
+    rels = [float(x) for x in args.fd_rels.split(",")]
+    fd = {}
+    for k in names:
+        base = getattr(p, k)
+        fd[k] = {}
+        for rel in rels:
+            d = rel * abs(base)
+            qp, qm = copy.copy(p), copy.copy(p)
+            setattr(qp, k, base + d)
+            setattr(qm, k, base - d)
+            fd[k][f"{rel:g}"] = (misfit(qp) - misfit(qm)) / (2.0 * d)
+    rough = []
+    for k in range(-3, 4):
+        q = copy.copy(p)
+        q.angle1 = p.angle1 * (1.0 + k * 1e-7)
+        J, t_end = misfit(q, with_time=True)
+        rough.append({"k": k, "J": J, "t_end": t_end})
+    el = time.perf_counter() - t0
+
+    def gap(g, ref):
+        return abs(g - ref) / abs(ref) if ref != 0.0 else None
+
+    report = {}
+    for k in names:
+        ref = fd[k][f"{rels[-1]:g}"]
+        report[k] = {"exact": grads["exact"][k], "projected": grads["projected"][k], "fd": fd[k],
+                     "gap_exact": gap(grads["exact"][k], ref), "gap_projected": gap(grads["projected"][k], ref),
+                     "fd_spread": max(gap(v, ref) or 0.0 for v in fd[k].values())}
+    gaps = [report[k]["gap_projected"] for k in names if report[k]["gap_projected"] is not None]
+    line = {"metric": "adjoint parameter gradient vs FP64 central differences (largest relative gap, projected)",
+            "value": max(gaps) if gaps else None, "unit": "relative", "n_gpus": 1, "steps": n, "warmup": 0,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"fjord{args.adj_n}x{args.adj_n}_order2_spherical_adjoint_fd", "steps": n,
+                       "gauges": int(gauges.size), "twin_perturbation": [float(x) for x in f],
+                       "thin_layer_m": args.adj_thin, "fd_relative_steps": rels, "vmax_mps": args.vmax},
+            "misfit": J0, "parameters": report, "roughness": rough, "seconds": el}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -737,6 +852,8 @@ def main():
         return run_adjoint(args)
     if args.impl == "ours" and args.workload == "adjoint-batch":
         return run_adjoint_batch(args)
+    if args.impl == "ours" and args.workload == "adjoint-fd":
+        return run_adjoint_fd(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

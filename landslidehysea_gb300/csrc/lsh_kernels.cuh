@@ -40,13 +40,19 @@ using lsh::kRateInitBits;
 //   before the empty-edge test: 128x3 2.46, 128x4 (128) 2.33, 128x5 (96) 2.26, 128x6 2.27;
 //   after it: 128x5 2.09, 128x6 (85) 2.03, 128x7 (73) 2.01, 64x12 (85) 2.03,
 //   64x14 (73) 2.00, 64x16 (64) 1.98-1.99, 64x20 (48) 2.00, 64x24 (40) 2.13, 256x2 2.40.
-// The spills of 64 registers (a few hundred bytes) stay in L1.  1: the
-// compiler's choice.
+// With the passes overlapped (programmatic dependent launches, below) the
+// SMs hold blocks of two or three passes at once, and more resident warps
+// pay again (steps 5-148, ms per step; edge threads x blocks, then cell
+// blocks of 256 per SM): 64x12 1.814, 64x16 1.666, 64x20 1.608, 64x24 1.690,
+// 64x28 1.721, 128x8 1.640, 128x10 1.611, 128x12 1.639; with 64x20: cells
+// at the compiler's choice (62-64 registers) 1.608, 5 blocks 1.587,
+// 6 blocks (40 registers) 1.582; 64x24 with 6 cell blocks 1.666.
+// The spills stay in L1.  1: the compiler's choice.
 #ifndef LSH_EDGE_MINB
-#define LSH_EDGE_MINB 16
+#define LSH_EDGE_MINB 20
 #endif
 #ifndef LSH_CELL_MINB
-#define LSH_CELL_MINB 1
+#define LSH_CELL_MINB 6
 #endif
 // Threads per edge-pass block (a tile of LSH_EDGE_H_BX x threads / BX).
 #ifndef LSH_EDGE_THREADS

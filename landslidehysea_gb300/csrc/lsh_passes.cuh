@@ -104,6 +104,34 @@ LSH_HD void face_rest(const KArgs& a, int id, int side, bool pos_normal, lsh::Fa
     f.H = H;
 }
 
+// The accumulator update of one edge: subtract the first KL flux terms of
+// each cell (KL = 3: layer 1 only, the layer-2 terms being zeros) and add the
+// wave term.  The first pass of a stage writes instead of accumulating:
+// every cell meets exactly one hor-even edge.
+template <bool FIRST, int KL>
+LSH_HD void scatter_edge(const KArgs& a, int id0, int id1, bool interior, const double d0[6], const double d1[6],
+                         double wave) {
+    if (FIRST) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.acc[k][id0] = (k < KL) ? 0.0 - d0[k] : 0.0;
+        a.acc[6][id0] = 0.0 + wave;
+        if (interior) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) a.acc[k][id1] = (k < KL) ? 0.0 - d1[k] : 0.0;
+            a.acc[6][id1] = 0.0 + wave;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < KL; ++k) a.acc[k][id0] -= d0[k];
+        a.acc[6][id0] += wave;
+        if (interior) {
+#pragma unroll
+            for (int k = 0; k < KL; ++k) a.acc[k][id1] -= d1[k];
+            a.acc[6][id1] += wave;
+        }
+    }
+}
+
 // One edge: gather both sides, evaluate, scatter to the accumulators.
 // dir 0: horizontal edge row y between rows y-1 and y, column x.
 // dir 1: vertical edge column x between columns x-1 and x, row y.
@@ -191,7 +219,8 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
     }
     lsh::EdgeOut o;
     using lsh::is_zero;
-    if (is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2))
+    const bool single = is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2);
+    if (single)
         lsh::edge_flux<false>(e, dt, a.c, o);
     else
         lsh::edge_flux<true>(e, dt, a.c, o);
@@ -215,26 +244,14 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
             d1[k + 2] = neg_if(o.p[k + 1], !pos_normal);
         }
     }
-    if (FIRST) {
-        // every cell meets exactly one hor-even edge: write, do not accumulate
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a.acc[k][id0] = 0.0 - d0[k];
-        a.acc[6][id0] = 0.0 + o.wave;
-        if (e.interior) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.acc[k][id1] = 0.0 - d1[k];
-            a.acc[6][id1] = 0.0 + o.wave;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a.acc[k][id0] -= d0[k];
-        a.acc[6][id0] += o.wave;
-        if (e.interior) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.acc[k][id1] -= d1[k];
-            a.acc[6][id1] += o.wave;
-        }
-    }
+    // A single-layer edge's layer-2 terms are zeros, and an accumulator never
+    // holds -0 (the first pass writes 0 - d, which is +0 for d = +-0, and
+    // x - y is -0 only for x = -0): subtracting them leaves the accumulator's
+    // bits as they are.  A warp whose edges are all single-layer skips that
+    // arithmetic and its loads, and the first pass stores the +0 it would
+    // compute.
+    if (warp_all(single)) scatter_edge<FIRST, 3>(a, id0, id1, e.interior, d0, d1, o.wave);
+    else scatter_edge<FIRST, 6>(a, id0, id1, e.interior, d0, d1, o.wave);
 }
 
 // minmod: the operand of smaller magnitude when both are nonzero with one
