@@ -57,18 +57,18 @@ COUNTER_SOURCES = ("landslidehysea_gb300/csrc/lsh_core.cu", "landslidehysea_gb30
                    "landslidehysea_gb300/csrc/lsh_passes.cuh", "landslidehysea_gb300/csrc/lsh_scheme.cuh",
                    "landslidehysea_gb300/csrc/lsh_fpmath.h", "landslidehysea_gb300/csrc/lsh_setup.h",
                    "landslidehysea_gb300/build.py", "landslidehysea_gb300/scenarios.py")
-COUNTERS_SOURCE_HASH = "f66c69cba4c7f9bc"
-# FP64-pipe thread instructions per cell-update of one step (7.060e8 per step
+COUNTERS_SOURCE_HASH = "34750d247dfe5f92"
+# FP64-pipe thread instructions per cell-update of one step (6.941e8 per step
 # / 4,194,304 cells).  The FP64 pipe takes one such instruction per lane as
 # the measured peak's DFMA does, so the peak instruction rate is the measured
 # FP64 FLOP/s / 2.
-FJORD2048_FP64_INSTR_PER_CELL_STEP = 168.33
+FJORD2048_FP64_INSTR_PER_CELL_STEP = 165.49
 # DRAM bytes (read + write) per launch of each step kernel; edge_h0 is the
 # first (accumulator-writing) horizontal pass.  A second-order step launches
 # recon and the four edge passes twice, each volume kernel once.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
-    "recon": 141.21e6, "edge_h0": 349.19e6, "edge_h1": 197.94e6, "edge_v0": 198.42e6, "edge_v1": 193.08e6,
-    "volume1": 627.86e6, "volume2": 679.87e6,
+    "recon": 141.05e6, "edge_h0": 373.6e6, "edge_h1": 198.1e6, "edge_v0": 193.85e6, "edge_v1": 190.1e6,
+    "volume1": 673.7e6, "volume2": 714.9e6,
 }
 # Algorithmic HBM bytes per cell-step (FP64 state with perfect reuse): first
 # order 13 x 8 = 104 B (read 6 state + H, write 6 state); TVD-RK2 104 B for
@@ -114,10 +114,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=48)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--ref-build", choices=("cpu", "cuda"), default="cpu",
+                    help="--impl reference: the FP64 CPU restatement (cpu, the reference arm) or the reference's own "
+                         "CUDA kernels compiled for this GPU (cuda: FP32, first order, Cartesian shelf of --n)")
     ap.add_argument("--n", type=int, default=2048, help="grid size (n x n); the headline is 2048")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("fjord", "ensemble", "adjoint", "adjoint-batch", "adjoint-fd"),
+    ap.add_argument("--workload", choices=("fjord", "shelf", "ensemble", "adjoint", "adjoint-batch", "adjoint-fd"),
                     default="fjord",
                     help="fjord: the 2048^2 headline; ensemble: the batched 256-scenario ensemble vs serial; "
                          "adjoint: gradient of the 16-gauge misfit on the 1024^2 fjord vs its forward")
@@ -175,17 +178,24 @@ def init_dist(world, local, backend):
     return dist
 
 
-def workload(n):
+def workload(n, kind="fjord"):
+    """fjord: the headline second-order spherical fjord; shelf: the plain
+    method's first-order Cartesian shelf (25 m cells, walls), at n x n."""
     from landslidehysea_gb300 import scenarios
-    sc = scenarios.fjord(n=n)
-    return sc
+    return scenarios.shelf(n=n) if kind == "shelf" else scenarios.fjord(n=n)
 
 
 def config_dict(sc, n, extra=None):
-    d = {"workload": f"fjord{n}x{n}_order2_spherical", "grid": [n, n], "cells": n * n, "order": 2,
-         "coords": "spherical", "cell_deg": 0.0002, "lat_c": 60.0, "slide_m3": 2e7, "seed": 0,
-         "wet_fraction": round(sc.meta["wet_fraction"], 4), "cfl": sc.params.cfl,
-         "l2": "inputs larger than L2 (state+accumulators+slopes ~1 GB)", "parallelism": "replicas"}
+    if sc.params.order == 1:
+        d = {"workload": f"shelf{n}x{n}_order1_cartesian", "grid": [n, n], "cells": n * n, "order": 1,
+             "coords": "cartesian", "dx_m": sc.params.dx, "seed": 0, "cfl": sc.params.cfl,
+             "l2": "inputs larger than L2" if n * n * 8 * 21 > 129e6 else "inputs smaller than L2",
+             "parallelism": "replicas"}
+    else:
+        d = {"workload": f"fjord{n}x{n}_order2_spherical", "grid": [n, n], "cells": n * n, "order": 2,
+             "coords": "spherical", "cell_deg": 0.0002, "lat_c": 60.0, "slide_m3": 2e7, "seed": 0,
+             "wet_fraction": round(sc.meta["wet_fraction"], 4), "cfl": sc.params.cfl,
+             "l2": "inputs larger than L2 (state+accumulators+slopes ~1 GB)", "parallelism": "replicas"}
     if extra:
         d.update(extra)
     return d
@@ -316,10 +326,63 @@ def cpu_baseline(sc, n):
             "shelf200_order1_serial_250_steps": {"value": v1, "cores": 1, "seconds": round(el1, 2)}}
 
 
+def run_reference_cuda(args):
+    """The reference's own CUDA build on this GPU: its unmodified kernel
+    sources compiled for sm_103a (oracle/build_ref.sh, through a shim for the
+    removed texture API) and driven through one rank's shallowWater() step
+    sequence (oracle/ref_cuda_driver.cpp), FP32, on the first-order Cartesian
+    shelf of --n (its native scheme).  Timed by wall clock over --steps
+    after --warmup steps, as the reference times its loop (MPI_Wtime).
+    `check_one_step` compares one step from the initial state with the FP64
+    oracle: the depths (relative to their scale) and dt agree to FP32
+    rounding.  Over many steps the FP32 state departs from FP64 on these
+    inputs (a slide at its Coulomb threshold, 1e-5 m dry threshold under
+    100 m of water): the host build of the same sources does the same."""
+    import numpy as np
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    if not pyoracle.ref_cuda_available():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference CUDA build (oracle/_ref) is absent: "
+                                                              "its cubin is compiled where the reference sources are"}))
+        return 0
+    sc = workload(args.n, "shelf")
+    steps, warm = max(1, args.steps), max(1, args.warmup)
+    try:
+        one, trace1, _, _ = pyoracle.ref_cuda_run(sc.params, sc.state, 0, 1, device=local)
+        arrs, trace, t, ms = pyoracle.ref_cuda_run(sc.params, sc.state, warm, steps, device=local)
+    except RuntimeError as e:
+        print(json.dumps({"impl": "reference", "unavailable": str(e)}))
+        return 0
+    value = sc.nx * sc.ny * steps / (ms * 1e-3)
+    pyoracle.set_threads(os.cpu_count() or 1)
+    o = pyoracle.state_arrays(sc.state)
+    dt0 = pyoracle.initial_dt(sc.params, o)
+    _, dt1, _ = pyoracle.run(sc.params, o, 1, dt=dt0)
+    depth = {}
+    for i, v in ((0, "h1"), (3, "h2")):
+        scale = max(float(np.abs(o[i]).max()), float(np.abs(sc.state[v]).max()), 1e-30)
+        depth[v] = float(np.abs(one[i] - o[i]).max()) / scale
+    check = {"depth_rel_of_scale": depth, "dt0_rel": abs(float(trace1[0]) - dt0) / dt0,
+             "dt1_rel": abs(float(trace1[1]) - dt1) / dt1}
+    line = {"impl": "reference", "build": "reference CUDA kernels (FP32) compiled for sm_103a",
+            "metric": f"FP32 cell-updates/s at {args.n}^2, first order (reference CUDA build)", "value": value,
+            "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": ms / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(sc, args.n, {"runner": "oracle/ref_cuda_driver.cpp + oracle/_ref/ref_kernels.cubin"}),
+            "sim_time_s": t, "dt_last": float(trace[-1]), "check_one_step": check}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
+    if args.ref_build == "cuda":
+        return run_reference_cuda(args)
     sc = workload(args.n)
     steps, warm = max(1, args.steps), max(1, args.warmup)
     value, threads, el = time_oracle(sc, steps, warm)
@@ -349,7 +412,7 @@ def run_ours(args):
     from landslidehysea_gb300._abi import VARS
     from landslidehysea_gb300.solver import Solver, probe_fp64_peak
 
-    sc = workload(args.n)
+    sc = workload(args.n, args.workload)
     cells = sc.nx * sc.ny
     # a dedicated (non-legacy) stream shared by the library and the timing events
     stream = torch.cuda.Stream()
@@ -397,7 +460,7 @@ def run_ours(args):
         fp64_peak = probe_fp64_peak(local)
     except Exception:
         fp64_peak = None
-    current = counters_current() and args.n == 2048 and order == 2
+    current = counters_current() and args.n == 2048 and args.workload == "fjord"
     ms_step = ms / args.steps
     rate = value / world
     fp64 = None
@@ -411,7 +474,8 @@ def run_ours(args):
                 "what": "FP64-pipe thread instructions the step kernels execute per cell-update (ncu count on "
                         "this workload, valid for the hashed kernel sources only) x cell-updates/s, over the "
                         "measured FP64 instruction rate (lsh_probe_fp64_peak DFMA GFLOP/s / 2)",
-                "scheme_gflops": round(FJORD2048_FLOPS_PER_CELL_STEP * rate / 1e9, 1) if args.n == 2048 else None,
+                "scheme_gflops": round(FJORD2048_FLOPS_PER_CELL_STEP * rate / 1e9, 1)
+                if args.n == 2048 and args.workload == "fjord" else None,
                 "scheme_flops_per_cell_step": FJORD2048_FLOPS_PER_CELL_STEP,
                 "scheme_note": "the reference scheme's FP64 operations (oracle count, FMA = 2) at this rate; "
                                "the kernels skip exact-zero work on dry cells and single-layer edges, so this "
@@ -856,7 +920,7 @@ def main():
         return run_adjoint_fd(args)
     if args.impl == "reference":
         return run_reference(args)
-    return run_ours(args)
+    return run_ours(args)  # fjord (the headline) or shelf
 
 
 if __name__ == "__main__":

@@ -230,3 +230,41 @@ def ops_per_cell_step(params, arrs, steps=(1, 3)):
     ca, cb = count_ops(params, arrs, a), count_ops(params, arrs, b)
     n = params.nx * params.ny * (b - a)
     return {k: (cb[k] - ca[k]) / n for k in OP_KINDS}
+
+
+REF_CUDA_SO = os.path.join(HERE, "_ref", "liblsh_ref_cuda.so")
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernels.cubin")
+
+
+def ref_cuda_available():
+    """The reference's own CUDA build: its kernels compiled for sm_103a from
+    the reference sources (ref_kernels.cubin) and the driver that runs them
+    (liblsh_ref_cuda.so)."""
+    return os.path.exists(REF_CUDA_SO) and os.path.exists(REF_CUBIN)
+
+
+def ref_cuda_run(params, state, warmup, nsteps, device=0):
+    """Run the reference's CUDA kernels on the GPU (FP32, Coulomb law): one
+    rank's shallowWater() step sequence, `warmup` untimed steps then
+    `nsteps` timed ones.  Returns (float32 arrays list, dt trace of the timed
+    steps, t, wall ms of the timed steps)."""
+    from landslidehysea_gb300._abi import VARS
+    lib_ = ctypes.CDLL(REF_CUDA_SO)
+    f = ctypes.c_float
+    P = ctypes.c_void_p
+    lib_.lsh_ref_cuda_run.argtypes = ([ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, P] + [f] * 24 +
+                                      [ctypes.c_int, ctypes.c_int, P, P, P])
+    lib_.lsh_ref_cuda_error.restype = ctypes.c_char_p
+    arrs = [np.ascontiguousarray(state[v], dtype=np.float32).copy() for v in VARS]
+    trace = np.zeros(nsteps + 1, dtype=np.float32)
+    t = ctypes.c_float()
+    ms = ctypes.c_double()
+    p = params
+    st = lib_.lsh_ref_cuda_run(REF_CUBIN.encode(), int(device), p.nx, p.ny, _ptrs(arrs), p.borde_sup, p.borde_inf,
+                               p.borde_izq, p.borde_der, p.dx, p.dy, p.dx * p.dy, p.cfl, p.r, p.angle1, p.angle2,
+                               p.angle3, p.angle4, p.peso, p.beta, p.mfc, p.mf0, p.mfs, p.vmax1, p.vmax2, p.gravity,
+                               p.eps_h, p.L, p.H, int(warmup), int(nsteps), trace.ctypes.data, ctypes.byref(t),
+                               ctypes.byref(ms))
+    if st:
+        raise RuntimeError("reference CUDA build: " + lib_.lsh_ref_cuda_error().decode())
+    return arrs, trace, t.value, ms.value
