@@ -135,6 +135,10 @@ def parse():
     ap.add_argument("--fd-rels", default="1e-2,1e-3,1e-4,1e-5,1e-6",
                     help="adjoint-fd relative difference steps (the last is the reference)")
     ap.add_argument("--count", type=int, default=256, help="ensemble scenarios")
+    ap.add_argument("--ens-sizes", default="128,256,512,768",
+                    help="ensemble: grid sizes the scenarios are drawn from (one size: a uniform ensemble)")
+    ap.add_argument("--ens-kind", choices=("shelf", "fjord"), default="shelf",
+                    help="ensemble: the config-0 shelf generator (configs[3]) or the fjord generator")
     ap.add_argument("--cal-count", type=int, default=64, help="batched-adjoint scenarios")
     ap.add_argument("--cal-steps", type=int, default=300, help="batched-adjoint steps (the full calibration: 3000)")
     ap.add_argument("--cal-serial", type=int, default=1, help="also run the members one by one (1) or not (0)")
@@ -587,8 +591,15 @@ def run_ensemble(args):
     from landslidehysea_gb300 import scenarios
     from landslidehysea_gb300.solver import Batch, Solver
     ids = shard(args.count, rank, world)
-    scs = scenarios.ensemble(args.count, ids=ids)
-    all_cells = sum(s_.nx * s_.ny for s_ in scenarios.ensemble(args.count)) if world > 1 else \
+    sizes = tuple(int(x) for x in args.ens_sizes.split(","))
+
+    def members(ks):
+        if args.ens_kind == "fjord":
+            return [scenarios.fjord(n=sizes[k % len(sizes)], seed=k) for k in ks]
+        return scenarios.ensemble(args.count, sizes=sizes, ids=list(ks))
+
+    scs = members(ids)
+    all_cells = sum(s_.nx * s_.ny for s_ in members(range(args.count))) if world > 1 else \
         sum(s_.nx * s_.ny for s_ in scs)
 
     def barrier():
@@ -643,7 +654,8 @@ def run_ensemble(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
                 "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"ensemble{args.count}_shelf_order2", "scenarios": args.count,
+                "config": {"workload": f"ensemble{args.count}_{args.ens_kind}_order2", "scenarios": args.count,
+                           "sizes": list(sizes),
                            "grids_rank0": {str(k): v for k, v in sorted(sizes.items())}, "cells": all_cells,
                            "order": 2, "split": "round-robin over ranks" if world > 1 else None,
                            "l2": f"inputs larger than L2 (~{all_cells * 36 * 8 / 1e9 / world:.0f} GB per GPU)"},

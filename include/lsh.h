@@ -208,16 +208,17 @@ int lsh_probe_fp64_peak(int device, double* gflops);
 /* ---------------------------------------------------------------------------
  * Batched ensemble (no counterpart in the reference): n scenarios with their
  * own parameters and uneven grids (all of one `order`) advanced together.
- * Each pass of a step is one persistent launch whose CTAs pull (scenario,
- * tile) work items from a device counter; a run of steps is a CUDA graph.
- * Every scenario stays bit-identical to its single-grid run (lsh_create...). */
+ * A time step of the whole ensemble is ONE persistent launch: its CTAs pull
+ * work items -- (pass, scenario, 2-D tile of edges or cells) -- from a device
+ * queue in pass order, and an item waits only for its own scenario's rows of
+ * the pass before it (completion counters); a small kernel then advances
+ * every scenario's clock.  A run of steps is a CUDA graph.  Every scenario
+ * stays bit-identical to its single-grid run (lsh_create...). */
 typedef struct lsh_batch lsh_batch;
 typedef struct lsh_tune {
-    int32_t edge_tile;          /* edges per work item, in units of 128        */
-    int32_t edge_ctas_per_sm;   /* persistent CTAs per SM for the edge passes  */
-    int32_t cell_tile;          /* cells per work item, in units of 256        */
-    int32_t cell_ctas_per_sm;   /* persistent CTAs per SM for the cell passes  */
-    double ms_per_step;         /* measured by lsh_batch_autotune              */
+    int32_t ctas_per_sm;        /* persistent CTAs of 64 threads per SM (1-20)  */
+    int32_t items_per_fetch;    /* work items a CTA takes from the queue at once */
+    double ms_per_step;         /* measured by lsh_batch_autotune               */
 } lsh_tune;
 int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** out);
 int lsh_batch_destroy(lsh_batch* b);
@@ -227,7 +228,7 @@ int lsh_batch_step(lsh_batch* b, int nsteps);              /* asynchronous */
 int lsh_batch_synchronize(lsh_batch* b);
 int lsh_batch_get_state(lsh_batch* b, int s, double* const host_state[LSH_NVARS]);
 int lsh_batch_get_time(lsh_batch* b, int s, double* t, double* dt_next, long long* steps);
-/* autotuner: time the candidate tile lengths and CTA counts on live steps and
+/* autotuner: time the candidate CTA counts and fetch sizes on live steps and
  * keep the fastest (the trial steps advance the simulation) */
 int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best);
 int lsh_batch_set_tune(lsh_batch* b, const lsh_tune* tune);

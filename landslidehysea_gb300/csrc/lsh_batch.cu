@@ -4,16 +4,20 @@
 // Every scenario keeps its own parameters, geometry, state and device clock
 // (t, dt), in one slab.  A step runs the same passes as the single-grid path
 // (reconstruction, 4 colour edge passes, Euler stage; twice at second
-// order), but each pass is ONE persistent launch for all scenarios: a grid
-// sized to the SM count whose CTAs pull work items -- (scenario, tile of
-// edges or cells) -- from a device counter until the pass's item list is
-// exhausted.  Items of one pass are independent (edges of one colour touch
-// disjoint cells), so the order in which CTAs take them does not change a bit
-// of the result: every scenario is bit-identical to its single-grid run.
-// The last kernel of a step advances every scenario's clock and resets the
-// counters, so a run of steps is one CUDA graph launch.  Tile length and
-// CTAs per SM are picked by lsh_batch_autotune, which times candidate
-// configurations on the live batch.
+// order), with the same device code (lsh_passes.cuh), but the whole step of
+// every scenario is ONE persistent launch: CTAs of 64 threads pull work items
+// -- (pass, scenario, 2-D tile of the single-grid shapes) -- from a device
+// queue, in pass order.  An item waits only for the rows of its own scenario
+// that the pass before it writes (per-row completion counters, as the
+// single-grid path's overlapped launches do), so a pass of one scenario runs
+// while other scenarios, or other rows, are still in the pass before: no
+// whole-grid barrier between passes.  Items of one pass touch disjoint cells
+// of their scenario, so which CTA takes an item, and when, changes no bit:
+// every scenario is bit-identical to its single-grid run.  A small kernel
+// then advances every scenario's clock and resets the queue and counters, so
+// a run of steps is one CUDA graph launch.  The CTA count per SM and the
+// items taken per queue fetch are picked by lsh_batch_autotune, which times
+// candidates on the live batch.
 
 #include <cuda_runtime.h>
 
@@ -36,84 +40,216 @@ using lsh::kRateInitBits;
 namespace {
 
 constexpr int kBatchGraphSteps = 8;
-constexpr int kPasses = 16;  // counters: up to 13 kernels per step
+constexpr int kBThreads = 64;    // threads per persistent CTA
+constexpr int kBMaxCtas = 20;    // CTAs per SM the step kernel is compiled for (48 registers)
+constexpr int kMaxPasses = 12;
 
-struct Item {
-    int s;      // scenario
-    int line;   // edge row (horizontal) / cell row (vertical); unused for cells
-    int start;  // first x (horizontal), first edge-column index t (vertical) or first cell id
-    int pad;
+// Tilings of a scenario's passes, 64-thread tiles of the single-grid shapes:
+// horizontal edges of parity 0 / 1 (16 columns x 4 edge lines), vertical
+// edges of parity 0 / 1 (8 edge columns x 8 rows), cells (16 x 4).
+enum BKind : int { kBH0 = 0, kBH1 = 1, kBV0 = 2, kBV1 = 3, kBCell = 4, kBKinds = 5 };
+constexpr int kTileHX = 16, kTileHY = 4, kTileVX = 8, kTileVY = 8, kTileCX = 16, kTileCY = 4;
+// What a pass does.
+enum BOp : int { kOpH0 = 0, kOpH1 = 1, kOpV0 = 2, kOpV1 = 3, kOpRecon = 4, kOpVol0 = 5, kOpVol1 = 6, kOpVol2 = 7 };
+
+struct BPass {
+    int op;        // BOp
+    int kind;      // BKind of its tiles
+    int stage;     // arguments: args[s] (stage 1) or args[n + s] (stage 2)
+    int prod;      // the pass whose writes it reads (-1: the step's first pass)
+    int item_off;  // first item of the pass in the step's queue
+    int ctr_off;   // first counter of the pass
 };
 
-// ------------------------------------------------------------------ kernels
+// Everything the step kernel needs, passed by value.
+struct BPlan {
+    int n;                  // scenarios
+    int npass;
+    int total_items;
+    BPass pass[kMaxPasses];
+    const int* tile_pre;    // [kind][n + 1]: first tile of each scenario (prefix sums)
+    const int* row_pre;     // [kind][n + 1]: first tile row of each scenario
+    const int* tiles_x;     // [kind][n]: tiles per tile row
+    const KArgs* args;      // [n] stage 1, [n, 2n) stage 2 (second order)
+    unsigned* ctr;          // completion counters: per pass, per scenario tile row
+    unsigned* head;         // the step's queue head
+    int* abort_flag;        // set when a wait gives up; later waits give up at once
+};
 
-// One persistent pass.  KIND 0: horizontal edges (x along the tile),
-// 1: vertical edges (edge column index along the tile), 2: cells (recon),
-// 3: cells (volume stage, MODE), per = tiles of BLOCK * per units.
-// Register caps like the single-grid kernels': edge passes at 64 registers
-// (8 resident CTAs of 128 per SM: the FP64 and load latencies need the
-// warps), the reconstruction at 32 (8 CTAs of 256), the volume update for 4.
-template <int KIND, bool FIRST, int ORDER, int MODE, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (KIND <= 2) ? 8 : 4) k_batch_pass(const KArgs* __restrict__ args, const Item* __restrict__ items,
-                                                       int n_items, unsigned int* counter, int par, int per) {
-    __shared__ int s_item;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
-        __syncthreads();
-        const int it = s_item;
-        __syncthreads();
-        if (it >= n_items) break;
-        const Item w = items[it];
-        const KArgs& a = args[w.s];
-        if (a.tm->done) continue;  // uniform over the CTA
-        const double dt = a.tm->dt;
-        const int nx = a.c.nx, ny = a.c.ny;
-        if (KIND == 0) {
-            for (int k = 0; k < per; ++k) {
-                const int x = w.start + k * BLOCK + (int)threadIdx.x;
-                if (x < nx) lsh::do_edge<0, FIRST, ORDER>(a, x, w.line, dt);
-            }
-        } else if (KIND == 1) {
-            for (int k = 0; k < per; ++k) {
-                const int x = par + 2 * (w.start + k * BLOCK + (int)threadIdx.x);
-                if (x <= nx) lsh::do_edge<1, false, ORDER>(a, x, w.line, dt);
-            }
-        } else if (KIND == 2) {
-            for (int k = 0; k < per; ++k) {
-                const int id = w.start + k * BLOCK + (int)threadIdx.x;
-                if (id < nx * ny) lsh::recon_cell(a, id);
-            }
+// Cell rows an item of `op` reads (tile row ty of a scenario with ny rows).
+__device__ __forceinline__ void item_rows(int op, int ty, int ny, int& r0, int& r1) {
+    if (op == kOpH0 || op == kOpH1) {
+        const int y0 = op + 2 * kTileHY * ty;  // first edge row (parity op)
+        r0 = y0 - 1; r1 = y0 + 2 * (kTileHY - 1);
+    } else if (op == kOpV0 || op == kOpV1) {
+        r0 = kTileVY * ty; r1 = r0 + kTileVY - 1;
+    } else if (op == kOpRecon) {
+        r0 = kTileCY * ty - 1; r1 = kTileCY * ty + kTileCY;
+    } else {
+        r0 = kTileCY * ty; r1 = r0 + kTileCY - 1;
+    }
+    r0 = max(r0, 0);
+    r1 = min(r1, ny - 1);
+}
+
+// Tile rows of a pass of `kind` that write cell rows [r0, r1].
+__device__ __forceinline__ void producer_rows(int kind, int r0, int r1, int& t0, int& t1) {
+    if (kind == kBV0 || kind == kBV1) { t0 = r0 / kTileVY; t1 = r1 / kTileVY; }
+    else if (kind == kBCell) { t0 = r0 / kTileCY; t1 = r1 / kTileCY; }
+    else {
+        // horizontal edge row y = p + 2 t writes cell rows y - 1 and y
+        const int p = kind;
+        t0 = (max(r0 - p + 1, 0) / 2) / kTileHY;
+        t1 = (max(r1 + 1 - p, 0) / 2) / kTileHY;
+    }
+}
+
+// One item's work: the single-grid kernels' per-thread bodies on one tile.
+template <int ORDER, int OP>
+__device__ __forceinline__ void item_work(const KArgs& a, int tx, int ty, double dt) {
+    const int nx = a.c.nx, ny = a.c.ny, tid = threadIdx.x;
+    if (OP == kOpH0 || OP == kOpH1) {
+        const int par = OP;
+        const int x = tx * kTileHX + tid % kTileHX, line = ty * kTileHY + tid / kTileHX;
+        if (x < nx && line < (ny - par) / 2 + 1) lsh::do_edge<0, OP == kOpH0, ORDER>(a, x, par + 2 * line, dt);
+    } else if (OP == kOpV0 || OP == kOpV1) {
+        const int par = OP - kOpV0;
+        const int x = par + 2 * (tx * kTileVX + tid % kTileVX), y = ty * kTileVY + tid / kTileVX;
+        if (x <= nx && y < ny) lsh::do_edge<1, false, ORDER>(a, x, y, dt);
+    } else {
+        const int i = tx * kTileCX + tid % kTileCX, j = ty * kTileCY + tid / kTileCX;
+        const bool in = (i < nx && j < ny);
+        if (OP == kOpRecon) {
+            if (in) lsh::recon_cell(a, j * nx + i);
         } else {
+            constexpr int MODE = OP - kOpVol0;
             unsigned long long bits = kRateInitBits;
-            for (int k = 0; k < per; ++k) {
-                const int id = w.start + k * BLOCK + (int)threadIdx.x;
-                if (id < nx * ny) {
-                    const unsigned long long b = lsh::volume_cell<MODE>(a, id, dt);
-                    bits = (b > bits) ? b : bits;
-                }
-            }
-            if (MODE != 2) lsh::block_max_bits<BLOCK>(bits, &a.tm->rmax_bits);
+            if (in) bits = lsh::volume_cell<MODE>(a, j * nx + i, dt);
+            if (MODE != 2) lsh::block_max_bits<kBThreads>(bits, &a.tm->rmax_bits);
         }
     }
 }
 
-// Every scenario's clock (k_advance of the single-grid path), and the work
-// counters back to zero for the next step.
-__global__ void k_batch_advance(const KArgs* __restrict__ args, int n, unsigned int* counters) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0)
-        for (int k = 0; k < kPasses; ++k) counters[k] = 0u;
-    if (s >= n) return;
-    lsh::TimeRec* tm = args[s].tm;
-    if (tm->done) return;
-    tm->t += tm->dt;
-    tm->steps += 1;
-    const double nd = lsh::dt_of(tm->rmax_bits, 2.0 * args[s].c.cfl);
-    tm->dt = nd;
-    tm->rmax_bits = kRateInitBits;
-    if (tm->t >= tm->t_end) tm->done = 1;
-    if (tm->dt_min > 0.0 && nd < tm->dt_min) { tm->err |= 1 << LSH_ERR_STALL; tm->done = 1; }
-    if (tm->err) tm->done = 1;
+// The whole step of every scenario.  Items are dequeued in pass order, and an
+// item waits only for items of earlier passes, which running CTAs took
+// before it: the earliest unfinished item always has its inputs, so the
+// queue drains whatever the number of resident CTAs.  Waits are bounded
+// (~2 s of %globaltimer); one that runs out sets LSH_ERR_TIMEOUT on its
+// scenario and the batch's abort flag, and later waits give up at once.
+template <int ORDER>
+__global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, int fetch) {
+    __shared__ __align__(16) unsigned long long sargs[(sizeof(KArgs) + 7) / 8];
+    __shared__ int s_first, s_pass, s_scen, s_tile;
+    const KArgs& a = *reinterpret_cast<const KArgs*>(sargs);
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)fetch);
+        __syncthreads();
+        const int first = s_first;
+        if (first >= P.total_items) break;
+        const int last = min(first + fetch, P.total_items);
+        for (int it = first; it < last; ++it) {
+            if (tid == 0) {
+                int p = 0;
+                while (p + 1 < P.npass && it >= P.pass[p + 1].item_off) ++p;
+                const int* tp = P.tile_pre + P.pass[p].kind * (P.n + 1);
+                const int l = it - P.pass[p].item_off;
+                int lo = 0, hi = P.n - 1;  // the scenario: the last one whose first tile is <= l
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (tp[mid] <= l) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_pass = p; s_scen = lo; s_tile = l - tp[lo];
+            }
+            __syncthreads();
+            const int p = s_pass, s = s_scen, t = s_tile;
+            const BPass ps = P.pass[p];
+            {
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(P.args + ps.stage * P.n + s);
+                for (int k = tid; k < (int)((sizeof(KArgs) + 7) / 8); k += kBThreads) sargs[k] = src[k];
+            }
+            __syncthreads();
+            const int ntx = P.tiles_x[ps.kind * P.n + s];
+            const int ty = t / ntx, tx = t - ty * ntx;
+            const bool live = !a.tm->done;  // uniform: the clock changes between steps only
+            if (live && ps.prod >= 0 && tid == 0) {
+                const BPass pp = P.pass[ps.prod];
+                int r0, r1, t0, t1;
+                item_rows(ps.op, ty, a.c.ny, r0, r1);
+                producer_rows(pp.kind, r0, r1, t0, t1);
+                const int rbase = P.row_pre[pp.kind * (P.n + 1) + s];
+                const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
+                t0 = max(t0, 0);
+                t1 = min(t1, nrows - 1);
+                const unsigned target = (unsigned)P.tiles_x[pp.kind * P.n + s];
+                const unsigned* c = P.ctr + pp.ctr_off + rbase;
+                volatile int* abort_flag = P.abort_flag;
+                unsigned long long start = 0;
+                bool gave_up = false;
+                for (int r = t0; r <= t1 && !gave_up; ++r) {
+                    unsigned ns = 32;
+                    for (;;) {
+                        unsigned v;
+                        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(c + r) : "memory");
+                        if (v >= target) break;
+                        if (*abort_flag) { gave_up = true; break; }
+                        unsigned long long now;
+                        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                        if (start == 0) start = now;
+                        else if (now - start > 2000000000ull) { atomicExch(P.abort_flag, 1); gave_up = true; break; }
+                        __nanosleep(ns);
+                        if (ns < 1024) ns *= 2;
+                    }
+                }
+                if (gave_up) atomicOr(&a.tm->err, 1 << LSH_ERR_TIMEOUT);
+            }
+            __syncthreads();
+            if (live) {
+                const double dt = a.tm->dt;
+                switch (ps.op) {
+                    case kOpH0: item_work<ORDER, kOpH0>(a, tx, ty, dt); break;
+                    case kOpH1: item_work<ORDER, kOpH1>(a, tx, ty, dt); break;
+                    case kOpV0: item_work<ORDER, kOpV0>(a, tx, ty, dt); break;
+                    case kOpV1: item_work<ORDER, kOpV1>(a, tx, ty, dt); break;
+                    default:
+                        if constexpr (ORDER == 1) {
+                            item_work<ORDER, kOpVol0>(a, tx, ty, dt);
+                        } else {
+                            if (ps.op == kOpRecon) item_work<ORDER, kOpRecon>(a, tx, ty, dt);
+                            else if (ps.op == kOpVol1) item_work<ORDER, kOpVol1>(a, tx, ty, dt);
+                            else item_work<ORDER, kOpVol2>(a, tx, ty, dt);
+                        }
+                        break;
+                }
+            }
+            __syncthreads();  // the tile's writes are done, and sargs may be refilled
+            if (tid == 0) {
+                __threadfence();
+                atomicAdd(P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty, 1u);
+            }
+        }
+    }
+}
+
+// Every scenario's clock (k_advance of the single-grid path); the queue head
+// and the completion counters back to zero for the next step.
+__global__ void k_batch_advance(const KArgs* __restrict__ args, int n, unsigned* ctr, int n_ctr, unsigned* head) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    if (gid == 0) *head = 0u;
+    for (int i = gid; i < n_ctr; i += stride) ctr[i] = 0u;
+    for (int s = gid; s < n; s += stride) {
+        lsh::TimeRec* tm = args[s].tm;
+        if (tm->done) continue;
+        tm->t += tm->dt;
+        tm->steps += 1;
+        const double nd = lsh::dt_of(tm->rmax_bits, 2.0 * args[s].c.cfl);
+        tm->dt = nd;
+        tm->rmax_bits = kRateInitBits;
+        if (tm->t >= tm->t_end) tm->done = 1;
+        if (tm->dt_min > 0.0 && nd < tm->dt_min) { tm->err |= 1 << LSH_ERR_STALL; tm->done = 1; }
+        if (tm->err) tm->done = 1;
+    }
 }
 
 // Initial dt of one scenario (set_state): wave pass, rate max, dt.
@@ -178,14 +314,12 @@ struct lsh_batch {
     std::vector<size_t> base;       // first cell of each scenario in the slab arrays
     size_t total = 0;
     void* slab = nullptr;
-    KArgs* d_args = nullptr;        // [n]
+    KArgs* d_args = nullptr;        // [n] (stage 1), [n, 2n) (stage 2)
     std::vector<KArgs> h_args;
     lsh::TimeRec* d_tm = nullptr;   // [n]
-    unsigned int* d_counters = nullptr;
-    Item* d_items = nullptr;        // all item lists, back to back
-    size_t items_cap = 0;
-    int n_items[5] = {0, 0, 0, 0, 0};  // hor0, hor1, ver0, ver1, cells
-    size_t items_off[5] = {0, 0, 0, 0, 0};
+    void* d_plan_mem = nullptr;     // the plan's tables, counters, queue head and abort flag
+    BPlan plan{};
+    int n_ctr = 0;                  // completion counters of one step
     lsh_tune tune{};
     cudaGraphExec_t graph = nullptr;
     long long launches = 0;
@@ -193,71 +327,107 @@ struct lsh_batch {
 
 namespace {
 
-int kernels_per_step(const lsh_batch* b) { return (b->order == 1) ? 6 : 13; }
+constexpr int kernels_per_step = 2;  // the step kernel and the clock kernel
 
-// Work items for the current tile lengths.
-int build_items(lsh_batch* b) {
-    std::vector<Item> lists[5];
-    const int te = kEdgeBlock * b->tune.edge_tile, tc = kCellBlock * b->tune.cell_tile;
-    for (int s = 0; s < b->n; ++s) {
-        const int nx = b->params[s].nx, ny = b->params[s].ny;
-        for (int par = 0; par < 2; ++par) {
-            for (int y = par; y <= ny; y += 2)
-                for (int x0 = 0; x0 < nx; x0 += te) lists[par].push_back(Item{s, y, x0, 0});
-            const int ncols = (nx - par) / 2 + 1;
-            for (int y = 0; y < ny; ++y)
-                for (int t0 = 0; t0 < ncols; t0 += te) lists[2 + par].push_back(Item{s, y, t0, 0});
+// Tiles of scenario `p` in each tiling: (tiles per row, tile rows).
+void scenario_tiles(const lsh_params& p, int kind, int& tx, int& ty) {
+    const int nx = p.nx, ny = p.ny;
+    if (kind == kBH0 || kind == kBH1) {
+        tx = (nx + kTileHX - 1) / kTileHX;
+        ty = ((ny - kind) / 2 + 1 + kTileHY - 1) / kTileHY;
+    } else if (kind == kBV0 || kind == kBV1) {
+        tx = ((nx - (kind - kBV0)) / 2 + 1 + kTileVX - 1) / kTileVX;
+        ty = (ny + kTileVY - 1) / kTileVY;
+    } else {
+        tx = (nx + kTileCX - 1) / kTileCX;
+        ty = (ny + kTileCY - 1) / kTileCY;
+    }
+}
+
+// The step's passes, their items and counters, and the device tables.
+int build_plan(lsh_batch* b) {
+    const int n = b->n;
+    std::vector<int> tile_pre(size_t(kBKinds) * (n + 1)), row_pre(size_t(kBKinds) * (n + 1)), tiles_x(size_t(kBKinds) * n);
+    long long kind_tiles[kBKinds], kind_rows[kBKinds];
+    for (int k = 0; k < kBKinds; ++k) {
+        long long tsum = 0, rsum = 0;
+        for (int s = 0; s < n; ++s) {
+            int tx, ty;
+            scenario_tiles(b->params[s], k, tx, ty);
+            tile_pre[k * (n + 1) + s] = (int)tsum;
+            row_pre[k * (n + 1) + s] = (int)rsum;
+            tiles_x[k * n + s] = tx;
+            tsum += (long long)tx * ty;
+            rsum += ty;
         }
-        for (int c0 = 0; c0 < nx * ny; c0 += tc) lists[4].push_back(Item{s, 0, c0, 0});
+        tile_pre[k * (n + 1) + n] = (int)tsum;
+        row_pre[k * (n + 1) + n] = (int)rsum;
+        kind_tiles[k] = tsum;
+        kind_rows[k] = rsum;
     }
-    size_t total = 0;
-    for (int k = 0; k < 5; ++k) { b->items_off[k] = total; b->n_items[k] = (int)lists[k].size(); total += lists[k].size(); }
-    if (total > b->items_cap) {
-        if (b->d_items) cudaFree(b->d_items);
-        b->d_items = nullptr;
-        B_CUDA(cudaMalloc(&b->d_items, total * sizeof(Item)));
-        b->items_cap = total;
+    // the passes of a step, each reading what the one before it wrote
+    struct P { int op, kind, stage; };
+    std::vector<P> passes;
+    const int stages = (b->order == 2) ? 2 : 1;
+    for (int st = 0; st < stages; ++st) {
+        if (b->order == 2) passes.push_back({kOpRecon, kBCell, st});
+        passes.push_back({kOpH0, kBH0, st});
+        passes.push_back({kOpH1, kBH1, st});
+        passes.push_back({kOpV0, kBV0, st});
+        passes.push_back({kOpV1, kBV1, st});
+        passes.push_back({(b->order == 1) ? kOpVol0 : (st == 0 ? kOpVol1 : kOpVol2), kBCell, st});
     }
-    for (int k = 0; k < 5; ++k)
-        if (!lists[k].empty())
-            B_CUDA(cudaMemcpy(b->d_items + b->items_off[k], lists[k].data(), lists[k].size() * sizeof(Item),
-                              cudaMemcpyHostToDevice));
+    BPlan& P0 = b->plan;
+    P0 = BPlan{};
+    P0.n = n;
+    P0.npass = (int)passes.size();
+    long long items = 0, ctrs = 0;
+    for (int i = 0; i < P0.npass; ++i) {
+        BPass& q = P0.pass[i];
+        q.op = passes[i].op;
+        q.kind = passes[i].kind;
+        q.stage = passes[i].stage;
+        q.prod = i - 1;
+        q.item_off = (int)items;
+        q.ctr_off = (int)ctrs;
+        items += kind_tiles[q.kind];
+        ctrs += kind_rows[q.kind];
+    }
+    if (items > 0x7fffffffLL - 1024 || ctrs > 0x7fffffffLL) {
+        lsh::set_last_error("batch too large for one step's work queue");
+        return LSH_ERR_INVALID;
+    }
+    P0.total_items = (int)items;
+    b->n_ctr = (int)ctrs;
+    // one allocation: tables, counters, queue head, abort flag
+    const size_t tbytes = (tile_pre.size() + row_pre.size() + tiles_x.size()) * sizeof(int);
+    const size_t bytes = ((tbytes + 255) & ~size_t(255)) + size_t(ctrs) * sizeof(unsigned) + 256;
+    if (b->d_plan_mem) { cudaFree(b->d_plan_mem); b->d_plan_mem = nullptr; }
+    B_CUDA(cudaMalloc(&b->d_plan_mem, bytes));
+    int* ti = static_cast<int*>(b->d_plan_mem);
+    B_CUDA(cudaMemcpy(ti, tile_pre.data(), tile_pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+    B_CUDA(cudaMemcpy(ti + tile_pre.size(), row_pre.data(), row_pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+    B_CUDA(cudaMemcpy(ti + tile_pre.size() + row_pre.size(), tiles_x.data(), tiles_x.size() * sizeof(int),
+                      cudaMemcpyHostToDevice));
+    P0.tile_pre = ti;
+    P0.row_pre = ti + tile_pre.size();
+    P0.tiles_x = ti + tile_pre.size() + row_pre.size();
+    char* rest = static_cast<char*>(b->d_plan_mem) + ((tbytes + 255) & ~size_t(255));
+    P0.ctr = reinterpret_cast<unsigned*>(rest);
+    P0.head = reinterpret_cast<unsigned*>(rest + size_t(ctrs) * sizeof(unsigned));
+    P0.abort_flag = reinterpret_cast<int*>(P0.head + 1);
+    B_CUDA(cudaMemset(rest, 0, size_t(ctrs) * sizeof(unsigned) + 256));
+    P0.args = b->d_args;
     return LSH_OK;
 }
 
-template <int KIND, bool FIRST, int ORDER, int MODE, int BLOCK>
-void launch_pass(lsh_batch* b, const KArgs* args, int list, int counter, int par, int per, int ctas_per_sm,
-                 cudaStream_t s) {
-    const int grid = std::max(1, std::min(b->sms * ctas_per_sm, b->n_items[list]));
-    k_batch_pass<KIND, FIRST, ORDER, MODE, BLOCK><<<grid, BLOCK, 0, s>>>(
-        args, b->d_items + b->items_off[list], b->n_items[list], b->d_counters + counter, par, per);
-}
-
-template <int ORDER>
-void enqueue_stage(lsh_batch* b, const KArgs* args, int mode, int& counter, cudaStream_t s) {
-    const int pe = b->tune.edge_tile, ce = b->tune.edge_ctas_per_sm;
-    const int pc = b->tune.cell_tile, cc = b->tune.cell_ctas_per_sm;
-    if (ORDER == 2) launch_pass<2, false, 2, 0, kCellBlock>(b, args, 4, counter++, 0, pc, cc, s);
-    launch_pass<0, true, ORDER, 0, kEdgeBlock>(b, args, 0, counter++, 0, pe, ce, s);
-    launch_pass<0, false, ORDER, 0, kEdgeBlock>(b, args, 1, counter++, 1, pe, ce, s);
-    launch_pass<1, false, ORDER, 0, kEdgeBlock>(b, args, 2, counter++, 0, pe, ce, s);
-    launch_pass<1, false, ORDER, 0, kEdgeBlock>(b, args, 3, counter++, 1, pe, ce, s);
-    if (mode == 0) launch_pass<3, false, ORDER, 0, kCellBlock>(b, args, 4, counter++, 0, pc, cc, s);
-    else if (mode == 1) launch_pass<3, false, ORDER, 1, kCellBlock>(b, args, 4, counter++, 0, pc, cc, s);
-    else launch_pass<3, false, ORDER, 2, kCellBlock>(b, args, 4, counter++, 0, pc, cc, s);
-}
-
-// args[0..n) describe stage 1 (X -> Y at second order), args[n..2n) stage 2
-// (Y -> X with the average), see lsh_batch_create.
 void enqueue_batch_step(lsh_batch* b, cudaStream_t s) {
-    int counter = 0;
-    if (b->order == 1) {
-        enqueue_stage<1>(b, b->d_args, 0, counter, s);
-    } else {
-        enqueue_stage<2>(b, b->d_args, 1, counter, s);
-        enqueue_stage<2>(b, b->d_args + b->n, 2, counter, s);
-    }
-    k_batch_advance<<<(b->n + 127) / 128, 128, 0, s>>>(b->d_args, b->n, b->d_counters);
+    const int grid = std::max(1, b->sms * std::min(std::max(b->tune.ctas_per_sm, 1), kBMaxCtas));
+    const int fetch = std::max(1, b->tune.items_per_fetch);
+    if (b->order == 1) k_batch_step<1><<<grid, kBThreads, 0, s>>>(b->plan, fetch);
+    else k_batch_step<2><<<grid, kBThreads, 0, s>>>(b->plan, fetch);
+    const int adv = std::max(1, std::min((std::max(b->n_ctr, b->n) + 255) / 256, 2 * b->sms));
+    k_batch_advance<<<adv, 256, 0, s>>>(b->d_args, b->n, b->plan.ctr, b->n_ctr, b->plan.head);
 }
 
 int build_graph(lsh_batch* b) {
@@ -320,8 +490,6 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
     const size_t bytes = (size_t(arrays) * cells + geo) * sizeof(double) + flag_bytes;
     { cudaError_t e = cudaMalloc(&b->slab, bytes); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc batch slab")); }
     { cudaError_t e = cudaMalloc(&b->d_tm, sizeof(lsh::TimeRec) * n); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc")); }
-    { cudaError_t e = cudaMalloc(&b->d_counters, sizeof(unsigned int) * kPasses); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc")); }
-    cudaMemset(b->d_counters, 0, sizeof(unsigned int) * kPasses);
     const int nargs = (b->order == 2) ? 2 * n : n;
     { cudaError_t e = cudaMalloc(&b->d_args, sizeof(KArgs) * nargs); if (e != cudaSuccess) return bail(bfail(e, "cudaMalloc")); }
 
@@ -370,8 +538,8 @@ int lsh_batch_create(const lsh_params* params, int n, int device, lsh_batch** ou
     std::vector<lsh::TimeRec> tms(n);
     for (int s = 0; s < n; ++s) { tms[s] = lsh::TimeRec{}; tms[s].t_end = INFINITY; tms[s].dt_min = params[s].dt_min; tms[s].done = 1; }
     { cudaError_t e = cudaMemcpy(b->d_tm, tms.data(), sizeof(lsh::TimeRec) * n, cudaMemcpyHostToDevice); if (e != cudaSuccess) return bail(bfail(e, "time")); }
-    b->tune = lsh_tune{2, 3, 2, 4, 0.0};
-    if (int st = build_items(b)) return bail(st);
+    b->tune = lsh_tune{16, 1, 0.0};
+    if (int st = build_plan(b)) return bail(st);
     *out = b;
     return LSH_OK;
 }
@@ -380,9 +548,8 @@ int lsh_batch_destroy(lsh_batch* b) {
     if (!b) return LSH_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->d_items) cudaFree(b->d_items);
+    if (b->d_plan_mem) cudaFree(b->d_plan_mem);
     if (b->d_args) cudaFree(b->d_args);
-    if (b->d_counters) cudaFree(b->d_counters);
     if (b->d_tm) cudaFree(b->d_tm);
     if (b->slab) cudaFree(b->slab);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -428,7 +595,7 @@ int lsh_batch_step(lsh_batch* b, int nsteps) {
     for (int i = 0; i < full; ++i) B_CUDA(cudaGraphLaunch(b->graph, b->stream));
     for (int i = 0; i < rest; ++i) enqueue_batch_step(b, b->stream);
     B_CUDA(cudaGetLastError());
-    b->launches += (long long)nsteps * (kernels_per_step(b) + 1);
+    b->launches += (long long)nsteps * kernels_per_step;
     return LSH_OK;
 }
 
@@ -466,12 +633,13 @@ int lsh_batch_get_time(lsh_batch* b, int s, double* t, double* dt, long long* st
 }
 
 int lsh_batch_set_tune(lsh_batch* b, const lsh_tune* tune) {
-    if (!b || !tune || tune->edge_tile < 1 || tune->cell_tile < 1 || tune->edge_ctas_per_sm < 1 || tune->cell_ctas_per_sm < 1)
+    if (!b || !tune || tune->ctas_per_sm < 1 || tune->ctas_per_sm > kBMaxCtas || tune->items_per_fetch < 1 ||
+        tune->items_per_fetch > 64)
         return LSH_ERR_INVALID;
     B_CUDA(cudaStreamSynchronize(b->stream));
     b->tune = *tune;
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
-    return build_items(b);
+    return LSH_OK;
 }
 
 int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune) {
@@ -485,34 +653,26 @@ int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune) {
 // taken while tuning are real steps of the simulation.
 int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best_out) {
     if (!b || trial_steps < 1) return LSH_ERR_INVALID;
-    static const int edge_tiles[] = {1, 2, 4};
-    static const int edge_ctas[] = {2, 4, 6, 8};
-    static const int cell_tiles[] = {1, 2, 4};
-    static const int cell_ctas[] = {2, 4, 8};
+    static const int ctas[] = {8, 12, 16, 20};
+    static const int fetches[] = {1, 2, 4};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     lsh_tune best = b->tune;
     best.ms_per_step = INFINITY;
-    // edge configuration first (with the current cell configuration), then cells
-    for (int phase = 0; phase < 2; ++phase) {
-        const int nj = (phase == 0) ? (int)(sizeof(edge_ctas) / sizeof(int)) : (int)(sizeof(cell_ctas) / sizeof(int));
-        for (int i = 0; i < 3; ++i) {
-            for (int j = 0; j < nj; ++j) {
-                lsh_tune t = best;
-                if (phase == 0) { t.edge_tile = edge_tiles[i]; t.edge_ctas_per_sm = edge_ctas[j]; }
-                else { t.cell_tile = cell_tiles[i]; t.cell_ctas_per_sm = cell_ctas[j]; }
-                if (int s = lsh_batch_set_tune(b, &t)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }
-                if (int s = lsh_batch_step(b, 1)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }  // graph build + warm-up
-                cudaEventRecord(e0, b->stream);
-                if (int s = lsh_batch_step(b, trial_steps)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }
-                cudaEventRecord(e1, b->stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                t.ms_per_step = ms / trial_steps;
-                if (t.ms_per_step < best.ms_per_step) best = t;
-            }
+    for (int c : ctas) {
+        for (int f : fetches) {
+            lsh_tune t{c, f, 0.0};
+            if (int s = lsh_batch_set_tune(b, &t)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }
+            if (int s = lsh_batch_step(b, 1)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }  // warm-up
+            cudaEventRecord(e0, b->stream);
+            if (int s = lsh_batch_step(b, trial_steps)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            t.ms_per_step = ms / trial_steps;
+            if (t.ms_per_step < best.ms_per_step) best = t;
         }
     }
     cudaEventDestroy(e0);

@@ -249,8 +249,8 @@ class Solver:
 
 class Tune(ctypes.Structure):
     """Mirror of lsh_tune."""
-    _fields_ = [("edge_tile", ctypes.c_int32), ("edge_ctas_per_sm", ctypes.c_int32),
-                ("cell_tile", ctypes.c_int32), ("cell_ctas_per_sm", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
+    _fields_ = [("ctas_per_sm", ctypes.c_int32), ("items_per_fetch", ctypes.c_int32),
+                ("ms_per_step", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -32,7 +32,7 @@ def test_batch_matches_single_grid(gpu_lib, order):
         b.step(steps1)
         b.synchronize()
         mid = [b.get_state(k) for k in range(len(scs))]
-        b.set_tune(edge_tile=1, edge_ctas_per_sm=4, cell_tile=4, cell_ctas_per_sm=2)
+        b.set_tune(ctas_per_sm=4, items_per_fetch=2)
         b.step(steps2)
         b.synchronize()
         fin = [b.get_state(k) for k in range(len(scs))]

@@ -47,7 +47,7 @@ def test_ensemble_members_equal_the_oracle(gpu_lib, order):
         got = []
         for i, n in enumerate(steps):
             if i == 1:
-                b.set_tune(edge_tile=2, edge_ctas_per_sm=3, cell_tile=1, cell_ctas_per_sm=4)
+                b.set_tune(ctas_per_sm=3, items_per_fetch=4)
             b.step(n)
             b.synchronize()
             got.append(([b.get_state(k) for k in range(len(scs))], [b.time(k) for k in range(len(scs))]))
