@@ -139,9 +139,15 @@ __device__ __forceinline__ void item_work(const KArgs& a, int tx, int ty, double
 template <int ORDER>
 __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, int fetch) {
     __shared__ __align__(16) unsigned long long sargs[(sizeof(KArgs) + 7) / 8];
-    __shared__ int s_first, s_pass, s_scen, s_tile;
+    __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy;
+    // the last decoded (pass, scenario): its items [s_lo, s_hi) of the queue,
+    // and the arguments held in sargs (stage * n + scenario, -1: none).
+    // Consecutive items of the queue share them, so most items skip the
+    // scenario search and the argument copy.
+    __shared__ int s_lo, s_hi, s_args_key;
     const KArgs& a = *reinterpret_cast<const KArgs*>(sargs);
     const int tid = threadIdx.x;
+    if (tid == 0) { s_lo = 0; s_hi = 0; s_args_key = -1; }
     for (;;) {
         if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)fetch);
         __syncthreads();
@@ -150,27 +156,37 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
         const int last = min(first + fetch, P.total_items);
         for (int it = first; it < last; ++it) {
             if (tid == 0) {
-                int p = 0;
-                while (p + 1 < P.npass && it >= P.pass[p + 1].item_off) ++p;
-                const int* tp = P.tile_pre + P.pass[p].kind * (P.n + 1);
-                const int l = it - P.pass[p].item_off;
-                int lo = 0, hi = P.n - 1;  // the scenario: the last one whose first tile is <= l
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (tp[mid] <= l) lo = mid;
-                    else hi = mid - 1;
+                if (it < s_lo || it >= s_hi) {
+                    int p = 0;
+                    while (p + 1 < P.npass && it >= P.pass[p + 1].item_off) ++p;
+                    const int kind = P.pass[p].kind;
+                    const int* tp = P.tile_pre + kind * (P.n + 1);
+                    const int l = it - P.pass[p].item_off;
+                    int lo = 0, hi = P.n - 1;  // the scenario: the last one whose first tile is <= l
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (tp[mid] <= l) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    s_pass = p;
+                    s_scen = lo;
+                    s_lo = P.pass[p].item_off + tp[lo];
+                    s_hi = P.pass[p].item_off + tp[lo + 1];
+                    s_ntx = P.tiles_x[kind * P.n + lo];
                 }
-                s_pass = p; s_scen = lo; s_tile = l - tp[lo];
+                s_tile = it - s_lo;
+                const int key = P.pass[s_pass].stage * P.n + s_scen;
+                s_copy = (key != s_args_key);
+                s_args_key = key;
             }
             __syncthreads();
-            const int p = s_pass, s = s_scen, t = s_tile;
+            const int p = s_pass, s = s_scen, t = s_tile, ntx = s_ntx;
             const BPass ps = P.pass[p];
-            {
+            if (s_copy) {
                 const unsigned long long* src = reinterpret_cast<const unsigned long long*>(P.args + ps.stage * P.n + s);
                 for (int k = tid; k < (int)((sizeof(KArgs) + 7) / 8); k += kBThreads) sargs[k] = src[k];
+                __syncthreads();
             }
-            __syncthreads();
-            const int ntx = P.tiles_x[ps.kind * P.n + s];
             const int ty = t / ntx, tx = t - ty * ntx;
             const bool live = !a.tm->done;  // uniform: the clock changes between steps only
             if (live && ps.prod >= 0 && tid == 0) {
