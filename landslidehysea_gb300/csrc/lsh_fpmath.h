@@ -9,11 +9,15 @@
 //       scaling by 2^k built from the exponent bits (two steps below 2^-1021
 //       so subnormal results round once).  Exactly 1 for x < 2^-54 and
 //       exactly 0 for x > 746 (what a correctly rounded exp returns there).
-//   cbrt_pos(x) = x^(1/3), x >= 0.  x = m 2^(3q + rem) with m in [1, 2);
-//       z ~ (m 2^rem)^(-1/3) from a quadratic first guess (4.4% error),
-//       4 Newton steps on f(z) = z^-3 - a (z <- z (4 - a z^3) / 3, no
-//       division; the error squares each step), then a^(1/3) = a z^2
-//       (within a few ulp, no division).
+//   cbrt_pos(x) = x^(1/3), x >= 0.  x = a 2^(3q) with a in [1, 8) (integer
+//       ops); z ~ a^(-1/3) by Newton's method on f(z) = z^-3 - a, written
+//       without division as z <- z + (z / 3)(1 - a z^3): a quadratic first
+//       guess (4.4% error) and three steps in FP32 on a's leading 24 bits
+//       (to about 1e-7: FP32 rounding), then two FP64 steps (the error
+//       squares each step); a^(1/3) = a z^2, and 2^q is added to the
+//       exponent bits.  Within a few ulp; about 12 FP64 operations, the rest
+//       on the FP32 and integer pipes.  FP32 basic operations and fmaf are
+//       IEEE on host and device alike, so both give the same bits.
 //   log_pos(x) = ln x, x > 0.  x = m 2^e with m in [sqrt(1/2), sqrt(2)),
 //       ln m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^23.
 // Accuracy: a few ulp (tests/test_fpmath.py checks them against the C
@@ -57,6 +61,34 @@ LSH_HD double fmad(double a, double b, double c) {
     return fma(a, b, c);
 #else
     return std::fma(a, b, c);
+#endif
+}
+
+LSH_HD float fmadf(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return fmaf(a, b, c);
+#else
+    return std::fmaf(a, b, c);
+#endif
+}
+
+LSH_HD uint32_t fbits_of(float x) {
+#if defined(__CUDA_ARCH__)
+    return (uint32_t)__float_as_uint(x);
+#else
+    uint32_t u;
+    std::memcpy(&u, &x, sizeof(u));
+    return u;
+#endif
+}
+
+LSH_HD float ffrom_bits(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float x;
+    std::memcpy(&x, &u, sizeof(x));
+    return x;
 #endif
 }
 
@@ -181,18 +213,31 @@ LSH_HD double cbrt_pos(double x) {
     if (kx < (int64_t)bits_of(0x1p-1000)) { x *= 0x1p300; scale = -100; }  // keep the exponent normal
     const uint64_t u = bits_of(x);
     const int e = (int)((u >> 52) & 0x7ff) - 1023;
-    const double m = from_bits((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);  // [1, 2)
     int q = e / 3, rem = e - 3 * q;
     if (rem < 0) { rem += 3; q -= 1; }
-    const double a = m * pow2i(rem);  // [1, 8)
-    double z = fmad(fmad(0.0115, a, -0.1656), a, 1.1098);
-    const double third = 1.0 / 3.0;
-    // relative error 0.044 -> 4e-3 -> 3e-5 -> 2e-9 -> 1e-17: four steps
-    for (int i = 0; i < 4; ++i) {
-        const double z3 = z * z * z;
-        z = z * ((4.0 - a * z3) * third);
+    // a = m 2^rem in [1, 8): x's mantissa with the exponent field set to rem
+    const uint64_t ua = (u & 0x000fffffffffffffULL) | ((uint64_t)(rem + 1023) << 52);
+    const double a = from_bits(ua);
+    // FP32: a's leading 24 bits (truncated), a quadratic guess, three steps
+    const float af = ffrom_bits(((uint32_t)(rem + 127) << 23) | (uint32_t)((ua >> 29) & 0x7fffffu));
+    float zf = fmadf(fmadf(0.0115f, af, -0.1656f), af, 1.1098f);
+    const float thirdf = 1.0f / 3.0f;
+    for (int i = 0; i < 3; ++i) {
+        const float t = (af * zf) * zf;
+        zf = fmadf(zf * thirdf, fmadf(-t, zf, 1.0f), zf);
     }
-    return ((a * z) * z) * pow2i(q + scale);
+    // widen exactly (zf in [1/2, 1], normal): sign 0, exponent rebased, mantissa shifted
+    const uint32_t zb = fbits_of(zf);
+    double z = from_bits(((uint64_t)(((zb >> 23) & 0xffu) - 127 + 1023) << 52) | ((uint64_t)(zb & 0x7fffffu) << 29));
+    const double third = 1.0 / 3.0;
+    for (int i = 0; i < 2; ++i) {
+        const double t = (a * z) * z;
+        z = fmad(z * third, fmad(-t, z, 1.0), z);
+    }
+    // a z^2 is in [1, 2]; times 2^(q + scale) by the exponent bits (the result
+    // of a positive normal or subnormal x is normal)
+    const double r = (a * z) * z;
+    return from_bits(bits_of(r) + ((uint64_t)(int64_t)(q + scale) << 52));
 }
 
 LSH_HD double log_pos(double x) {

@@ -132,6 +132,26 @@ LSH_HD void scatter_edge(const KArgs& a, int id0, int id1, bool interior, const 
     }
 }
 
+// The positivity limiter's inputs of one edge, loaded from the state and the
+// accumulators where the limiter reads them: cell areas by row, cell depths
+// h1, h2, and the depths' partial accumulators (zero in the first pass); a
+// boundary edge's outer side mirrors the cell's area with zero depths.
+template <bool FIRST>
+struct LazyPos {
+    const KArgs& a;
+    int id0, id1, row0, row1;
+    LSH_HD double area(int side) const { return a.geo.area[(side && id1 >= 0) ? row1 : row0]; }
+    LSH_HD double inv_area(int side) const { return a.geo.inv_area[(side && id1 >= 0) ? row1 : row0]; }
+    LSH_HD double hc(int side, int layer) const {
+        if (side && id1 < 0) return 0.0;
+        return a.W[layer ? 3 : 0][side ? id1 : id0];
+    }
+    LSH_HD double acch(int side, int layer) const {
+        if (FIRST || (side && id1 < 0)) return 0.0;
+        return a.acc[layer ? 3 : 0][side ? id1 : id0];
+    }
+};
+
 // One edge: gather both sides, evaluate, scatter to the accumulators.
 // dir 0: horizontal edge row y between rows y-1 and y, column x.
 // dir 1: vertical edge column x between columns x-1 and x, row y.
@@ -193,37 +213,24 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
         return;
     }
     face_rest<DIR, ORDER>(a, id0, side0, pos_normal, e.A);
-    e.area0 = a.geo.area[row0];
-    e.inv_area0 = a.geo.inv_area[row0];
-    e.hc0[0] = a.W[0][id0];
-    e.hc0[1] = a.W[3][id0];
-    if (FIRST) { e.acc0h[0] = 0.0; e.acc0h[1] = 0.0; }
-    else { e.acc0h[0] = a.acc[0][id0]; e.acc0h[1] = a.acc[3][id0]; }
     if (e.interior) {
         face_rest<DIR, ORDER>(a, id1, side1, pos_normal, e.B);
-        e.area1 = a.geo.area[row1];
-        e.inv_area1 = a.geo.inv_area[row1];
-        e.hc1[0] = a.W[0][id1];
-        e.hc1[1] = a.W[3][id1];
-        if (FIRST) { e.acc1h[0] = 0.0; e.acc1h[1] = 0.0; }
-        else { e.acc1h[0] = a.acc[0][id1]; e.acc1h[1] = a.acc[3][id1]; }
     } else {
         // ghost: the cell's face with the normal discharges times the boundary factor
         e.B = e.A;
         e.B.qn1 = e.A.qn1 * bor;
         e.B.qn2 = e.A.qn2 * bor;
-        e.area1 = e.area0;
-        e.inv_area1 = e.inv_area0;
-        e.hc1[0] = e.hc1[1] = 0.0;
-        e.acc1h[0] = e.acc1h[1] = 0.0;
     }
+    // the limiter's inputs are loaded where it reads them (LazyPos), not kept
+    // live through the flux computation
+    const LazyPos<FIRST> pos{a, id0, id1, row0, row1};
     lsh::EdgeOut o;
     using lsh::is_zero;
     const bool single = is_zero(e.A.h2) && is_zero(e.B.h2) && is_zero(e.A.qn2) && is_zero(e.B.qn2);
     if (single)
-        lsh::edge_flux<false>(e, dt, a.c, o);
+        lsh::edge_flux<false>(e, dt, a.c, o, pos);
     else
-        lsh::edge_flux<true>(e, dt, a.c, o);
+        lsh::edge_flux<true>(e, dt, a.c, o, pos);
     // back to x/y: DIR 1: (qx, qy) = sg (fn, ft); DIR 0: qx = -sg ft, qy = sg fn
     double d0[6], d1[6];
 #pragma unroll

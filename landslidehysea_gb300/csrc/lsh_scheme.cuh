@@ -210,12 +210,25 @@ struct EdgeIn {
 // momentum) to subtract from cell 0 (m) and cell 1 (p), and the wave term.
 struct EdgeOut { double m[6], p[6]; double wave; };
 
+// The positivity limiter's inputs, read from an EdgeIn that holds them.
+struct EdgeInPos {
+    const EdgeIn& e;
+    LSH_HD double area(int side) const { return side ? e.area1 : e.area0; }
+    LSH_HD double inv_area(int side) const { return side ? e.inv_area1 : e.inv_area0; }
+    LSH_HD double hc(int side, int layer) const { return side ? e.hc1[layer] : e.hc0[layer]; }
+    LSH_HD double acch(int side, int layer) const { return side ? e.acc1h[layer] : e.acc0h[layer]; }
+};
+
 // procesarArista (Arista_kernel.cu:324-645), the depths already known to be
 // wet (the caller skips dry edges, :397).  L2 == false: both faces have no
 // granular layer (h2 = qn2 = 0); every layer-1 value is then the same as in
 // the general path and every layer-2 output is zero, so that work is skipped.
-template <bool L2>
-LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
+// `pos` supplies the positivity limiter's inputs (cell areas, cell depths and
+// the partial accumulators of the cells' depths; EdgeInPos reads them from
+// `e`): a caller may load them only where the limiter needs them, so they do
+// not stay live through the flux computation.
+template <bool L2, class Pos>
+LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o, const Pos& pos) {
     const double eps = c.eps_h;
     double Aq1 = e.A.qn1, Aq2 = L2 ? e.A.qn2 : 0.0, Bq1 = e.B.qn1, Bq2 = L2 ? e.B.qn2 : 0.0;
     const double Ah1 = e.A.h1, Bh1 = e.B.h1;
@@ -349,14 +362,14 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
 #pragma unroll
     for (int k = 0; k < KL; ++k) { P[k] = e.len * P[k]; M[k] = e.len * M[k]; }
 
-    const double b0 = dt * e.inv_area0;
-    const double hp00 = fmad(b0, e.acc0h[0], e.hc0[0]);
-    const double hp01 = L2 ? fmad(b0, e.acc0h[1], e.hc0[1]) : 0.0;
+    const double b0 = dt * pos.inv_area(0);
+    const double hp00 = fmad(b0, pos.acch(0, 0), pos.hc(0, 0));
+    const double hp01 = L2 ? fmad(b0, pos.acch(0, 1), pos.hc(0, 1)) : 0.0;
     double hp10 = 0.0, hp11 = 0.0;
     if (e.interior) {
-        const double b1 = dt * e.inv_area1;
-        hp10 = fmad(b1, e.acc1h[0], e.hc1[0]);
-        if (L2) hp11 = fmad(b1, e.acc1h[1], e.hc1[1]);
+        const double b1 = dt * pos.inv_area(1);
+        hp10 = fmad(b1, pos.acch(1, 0), pos.hc(1, 0));
+        if (L2) hp11 = fmad(b1, pos.acch(1, 1), pos.hc(1, 1));
     }
     const double factor = 1.0 * c.beta;
 #pragma unroll
@@ -366,7 +379,7 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
         // hp area / (beta M + eps): tested as dt (beta M + eps) > hp area (the
         // denominator is positive), so the divisions run only on limited edges
         const bool oa = gt0(M[k]), ob = e.interior && gt0(P[k]);
-        const double ha = (layer ? hp01 : hp00) * e.area0, hb = (layer ? hp11 : hp10) * e.area1;
+        const double ha = (layer ? hp01 : hp00) * pos.area(0), hb = (layer ? hp11 : hp10) * pos.area(1);
         const double da = oa ? fmad(factor, M[k], kEps) : 1.0, db = ob ? fmad(factor, P[k], kEps) : 1.0;
         const bool lim = (oa && lt(ha, dt * da)) || (ob && lt(hb, dt * db));
         if (lim) {
@@ -387,6 +400,11 @@ LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) { o.m[k] = M[k]; o.p[k] = P[k]; }
+}
+
+template <bool L2>
+LSH_HD void edge_flux(const EdgeIn& e, double dt, const Consts& c, EdgeOut& o) {
+    edge_flux<L2>(e, dt, c, o, EdgeInPos{e});
 }
 
 // procesarAristaDeltaTInicial: wave-speed bound for the initial dt.
