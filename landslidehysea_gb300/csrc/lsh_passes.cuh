@@ -406,18 +406,42 @@ LSH_HD unsigned long long volume_cell(const KArgs& a, int id, double dt) {
         for (int k = 0; k < 6; ++k) w[k] = wo[k];
         rate = 0.0;
     } else {
+        // The cell has no granular layer and receives none: wo[3..5] zero and
+        // acc[3..5] +0 (bit patterns).  With finite slopes its layer-2
+        // pressure term is g (+-0) (finite) = +-0, leaving acc[4], acc[5] at
+        // +0, and volume_update<true> gives the general path's bits.  A warp
+        // whose cells all qualify takes that path (if-converted per-lane
+        // selects would still issue the FP64 work).
+        using lsh::is_zero;
+        bool one = is_zero(wo[3]) && is_zero(wo[4]) && is_zero(wo[5]) && lshm::bits_of(acc[3]) == 0 &&
+                   lshm::bits_of(acc[4]) == 0 && lshm::bits_of(acc[5]) == 0;
+        double s0x = 0.0, s3x = 0.0, s0y = 0.0, s3y = 0.0;
         if (a.c.order == 2) {
-            // cell-midpoint integral of g h d(eta) over the reconstructed cell
-            const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
-            const double e1x = 2.0 * a.sx[0][id], e2x = 2.0 * a.sx[3][id];
-            const double e1y = 2.0 * a.sy[0][id], e2y = 2.0 * a.sy[3][id];
-            const double wx = a.geo.wx[j], wy = a.geo.wy[j];
-            acc[1] -= a.c.peso * ((gh1 * e1x) * wx);
-            acc[4] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2x, a.c.r * e1x)) * wx);
-            acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
-            acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
+            s0x = a.sx[0][id]; s3x = a.sx[3][id]; s0y = a.sy[0][id]; s3y = a.sy[3][id];
+            one = one && !lsh::is_bad(s0x) && !lsh::is_bad(s3x) && !lsh::is_bad(s0y) && !lsh::is_bad(s3y);
         }
-        lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
+        if (warp_all(one)) {
+            if (a.c.order == 2) {
+                const double gh1 = a.c.g * wo[0];
+                const double wx = a.geo.wx[j], wy = a.geo.wy[j];
+                acc[1] -= a.c.peso * ((gh1 * (2.0 * s0x)) * wx);
+                acc[2] -= a.c.peso * ((gh1 * (2.0 * s0y)) * wy);
+            }
+            lsh::volume_update<true>(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
+        } else {
+            if (a.c.order == 2) {
+                // cell-midpoint integral of g h d(eta) over the reconstructed cell
+                const double gh1 = a.c.g * wo[0], gh2 = a.c.g * wo[3];
+                const double e1x = 2.0 * s0x, e2x = 2.0 * s3x;
+                const double e1y = 2.0 * s0y, e2y = 2.0 * s3y;
+                const double wx = a.geo.wx[j], wy = a.geo.wy[j];
+                acc[1] -= a.c.peso * ((gh1 * e1x) * wx);
+                acc[4] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2x, a.c.r * e1x)) * wx);
+                acc[2] -= a.c.peso * ((gh1 * e1y) * wy);
+                acc[5] -= a.c.peso * ((gh2 * lsh::fmad(a.c.omr, e2y, a.c.r * e1y)) * wy);
+            }
+            lsh::volume_update(wo, acc, w, rate, a.geo.inv_area[j], a.geo.tanR[j], dt, a.c);
+        }
     }
     // A still cell whose output is the very bits already stored where it goes
     // skips the stores: order 1 updates in place (w == wo); stage 2 writes back

@@ -555,16 +555,23 @@ LSH_HD void coulomb(double w[6], double dt, const Consts& c) {
 // `rate` gets acc_w / area (0 below EPSILON): the step's dt is
 // 2 CFL / max(rate), the min over cells of 2 CFL area / acc_w
 // (Volumen_kernel.cu:256) with one division per step.
+// ONE: the caller has checked that the cell's granular state wo[3..5] is
+// zero and its layer-2 accumulators are +0 (an accumulator never holds -0).
+// Then every layer-2 value below is the +0 the general path computes
+// (b * (+0) + (+-0) = +0; Coulomb's +0 * 0 = +0), so that arithmetic is
+// skipped and the single-layer branch taken.
+template <bool ONE = false>
 LSH_HD void volume_update(const double wo[6], const double acc[7], double w[6], double& rate,
                                               double inv_area, double tanR, double dt, const Consts& c) {
     rate = lt_pos(acc[6], kEps) ? 0.0 : acc[6] * inv_area;
     const double b = dt * inv_area;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) w[k] = fmad(b, acc[k], wo[k]);
+    for (int k = 0; k < (ONE ? 3 : 6); ++k) w[k] = fmad(b, acc[k], wo[k]);
+    if (ONE) { w[3] = 0.0; w[4] = 0.0; w[5] = 0.0; }
     const double fo1 = vfac(wo[0], c.eps_h);
     if (!is_zero(tanR)) {
 #pragma unroll
-        for (int layer = 0; layer < 2; ++layer) {
+        for (int layer = 0; layer < (ONE ? 1 : 2); ++layer) {
             const int k = 3 * layer;
             if (is_zero(wo[k]) && is_zero(wo[k + 1]) && is_zero(wo[k + 2])) continue;  // adds exactly 0
             const double ux = (layer ? vfac(wo[k], c.eps_h) : fo1) * wo[k + 1];
@@ -575,7 +582,10 @@ LSH_HD void volume_update(const double wo[6], const double acc[7], double w[6], 
     }
     // single layer: the granular layer is empty before and after the Euler
     // update (h2 = q2 = 0 in both), so its friction and Coulomb terms are zeros
-    if (is_zero(wo[3]) && is_zero(wo[4]) && is_zero(wo[5]) && is_zero(w[3]) && is_zero(w[4]) && is_zero(w[5])) {
+    if (ONE) {
+        filtro<false>(w, dt, c);
+        dis_implicita<false>(wo, w, dt, c, fo1);
+    } else if (is_zero(wo[3]) && is_zero(wo[4]) && is_zero(wo[5]) && is_zero(w[3]) && is_zero(w[4]) && is_zero(w[5])) {
         filtro<false>(w, dt, c);
         dis_implicita<false>(wo, w, dt, c, fo1);
         w[4] = w[4] * 0.0;  // coulomb() with h2 = 0
