@@ -313,25 +313,62 @@ LSH_HD void recon_cell_from(const KArgs& a, int id, int i, int j, const Acc& w) 
         if (k == 3) return w(3, di, dj) - w(6, di, dj);
         return w(k, di, dj);
     };
-    double sx[7], sy[7];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
+    const bool inx = (i > 0 && i < nx - 1), iny = (j > 0 && j < ny - 1);
+    auto slope_x = [&](int k) {
         const double pc = rv(k, 0, 0);
-        sx[k] = (i > 0 && i < nx - 1) ? 0.5 * minmod(pc - rv(k, -1, 0), rv(k, 1, 0) - pc) : 0.0;
-        sy[k] = (j > 0 && j < ny - 1) ? 0.5 * minmod(pc - rv(k, 0, -1), rv(k, 0, 1) - pc) : 0.0;
+        return inx ? 0.5 * minmod(pc - rv(k, -1, 0), rv(k, 1, 0) - pc) : 0.0;
+    };
+    auto slope_y = [&](int k) {
+        const double pc = rv(k, 0, 0);
+        return iny ? 0.5 * minmod(pc - rv(k, 0, -1), rv(k, 0, 1) - pc) : 0.0;
+    };
+    // No granular layer anywhere in the stencil (h2 = q2 = 0 at the cell and
+    // the neighbours it reads): eta2 = 0 - H, whose differences are exactly
+    // the negated differences of H, so its slope is the negated H slope, or
+    // +0 where minmod gives 0; the q2 slopes are minmod's 0, so +0; and the
+    // fallback's h2 tests, 0 +- 0 against 0.5 * 0, never fire.  A warp whose
+    // cells all qualify skips that FP64 work and gets the same bits.
+    bool one = true;
+    {
+        using lsh::is_zero;
+        auto nolayer = [&](int di, int dj) {
+            return is_zero(w(3, di, dj)) && is_zero(w(4, di, dj)) && is_zero(w(5, di, dj));
+        };
+        one = nolayer(0, 0);
+        if (one && i > 0) one = nolayer(-1, 0);
+        if (one && i < nx - 1) one = nolayer(1, 0);
+        if (one && j > 0) one = nolayer(0, -1);
+        if (one && j < ny - 1) one = nolayer(0, 1);
+    }
+    double sx[7], sy[7];
+    const bool fast = warp_all(one);
+    if (fast) {
+        sx[0] = slope_x(0); sy[0] = slope_y(0);
+        sx[1] = slope_x(1); sy[1] = slope_y(1);
+        sx[2] = slope_x(2); sy[2] = slope_y(2);
+        sx[6] = slope_x(6); sy[6] = slope_y(6);
+        sx[3] = lsh::is_zero(sx[6]) ? 0.0 : lshm::neg_if(sx[6], true);
+        sy[3] = lsh::is_zero(sy[6]) ? 0.0 : lshm::neg_if(sy[6], true);
+        sx[4] = sx[5] = sy[4] = sy[5] = 0.0;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) { sx[k] = slope_x(k); sy[k] = slope_y(k); }
     }
     const double h1 = w(0, 0, 0), h2 = w(3, 0, 0);
-    const double dh1x = sx[0] - sx[3], dh2x = sx[3] + sx[6];
-    const double dh1y = sy[0] - sy[3], dh2y = sy[3] + sy[6];
+    const double dh1x = sx[0] - sx[3], dh1y = sy[0] - sy[3];
     // first order where a reconstructed depth would fall below kReconThin of
     // the cell's: a thin face with a finite discharge has an unbounded
     // velocity, whose wave speed would collapse dt
     // (the compares on the integer pipe)
-    const double g1 = kReconThin * h1, g2 = kReconThin * h2;
+    const double g1 = kReconThin * h1;
     using lshm::okey;
-    const int64_t k1 = okey(g1), k2 = okey(g2);
-    const bool bad = okey(h1 + dh1x) < k1 || okey(h1 - dh1x) < k1 || okey(h2 + dh2x) < k2 || okey(h2 - dh2x) < k2 ||
-                     okey(h1 + dh1y) < k1 || okey(h1 - dh1y) < k1 || okey(h2 + dh2y) < k2 || okey(h2 - dh2y) < k2;
+    const int64_t k1 = okey(g1);
+    bool bad = okey(h1 + dh1x) < k1 || okey(h1 - dh1x) < k1 || okey(h1 + dh1y) < k1 || okey(h1 - dh1y) < k1;
+    if (!fast) {
+        const double dh2x = sx[3] + sx[6], dh2y = sy[3] + sy[6];
+        const int64_t k2 = okey(kReconThin * h2);
+        bad = bad || okey(h2 + dh2x) < k2 || okey(h2 - dh2x) < k2 || okey(h2 + dh2y) < k2 || okey(h2 - dh2y) < k2;
+    }
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
         a.sxw[k][id] = bad ? 0.0 : sx[k];
