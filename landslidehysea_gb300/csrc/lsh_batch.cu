@@ -241,8 +241,9 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
             }
             __syncthreads();  // the tile's writes are done, and sargs may be refilled
             if (tid == 0) {
-                __threadfence();
-                atomicAdd(P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty, 1u);
+                // release: the barrier above orders the tile's writes before it
+                unsigned* c = P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty;
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(c) : "memory");
             }
         }
     }

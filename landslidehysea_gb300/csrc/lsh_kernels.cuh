@@ -95,7 +95,7 @@ constexpr int kCellBX = LSH_CELL_BX, kCellBY = kCellBlock / LSH_CELL_BX;
 // be scheduled once every block of that pass has started, and each of them
 // waits only for the producer's row tiles that wrote the cell rows it reads.
 // Every block of a pass adds 1 to its row tile's counter when its writes are
-// done (fence, then atomic add); a consumer's thread 0 spins on the counters
+// done (a release add after the block's barrier); a consumer's thread 0 spins on the counters
 // it needs with acquire loads, then the block synchronises.  The producer's
 // blocks have all started before a consumer block can be scheduled, so a
 // waiting block never keeps a producer block off the GPU.  Which rows a pass
@@ -165,13 +165,13 @@ __device__ __forceinline__ void dep_begin(const Dep& d, TimeRec* tm, int r0, int
 }
 
 // End of a pass's block: its writes are done; count it in its block row.
+// The barrier orders every thread's writes before thread 0's add, whose
+// release semantics (cumulative, GPU scope) publish them with it.
 __device__ __forceinline__ void dep_end(const Dep& d) {
     if (!d.done) return;
     __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        __threadfence();
-        atomicAdd(d.done + blockIdx.y, 1u);
-    }
+    if (threadIdx.x == 0 && threadIdx.y == 0)
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(d.done + blockIdx.y) : "memory");
 }
 
 // Horizontal edges of parity `par`: x along threadIdx.x, edge rows par, par+2, ... along threadIdx.y / blocks.y.
