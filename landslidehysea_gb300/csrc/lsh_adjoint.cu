@@ -176,10 +176,16 @@ __global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
 
 // The recomputation's reconstruction: slopes (bit-identical to k_recon's)
 // and the branch tape the reconstruction adjoint replays.
-__global__ void __launch_bounds__(kCellBlock, 8) k_recon_tape(KArgs a, unsigned* tape) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.c.nx * a.c.ny) return;
-    tape[id] = lsh::recon_cell_tape(a, id);
+// The reconstruction with its branch tape, in the step's cell tiles (so it
+// can take part in the overlapped passes through `d`).
+__global__ void __launch_bounds__(kCellBlock, 8) k_recon_tape(KArgs a, unsigned* tape, Dep d = Dep{}) {
+    if (d.done || d.wait) {
+        const int y0 = blockIdx.y * kCellBY;
+        dep_begin(d, a.tm, max(y0 - 1, 0), min(y0 + kCellBY, a.c.ny - 1));
+    }
+    const int id = cell_of_thread(a.c.nx, a.c.ny);
+    if (id >= 0) tape[id] = lsh::recon_cell_tape(a, id);
+    dep_end(d);
 }
 
 // Max and arg-max (lowest cell on ties) of acc_w / area (0 below EPSILON).
@@ -348,6 +354,8 @@ struct lsh_adjoint {
     double* eta_dummy = nullptr;
     unsigned* tape1 = nullptr, *tape2 = nullptr;
     unsigned char* szero1 = nullptr, *szero2 = nullptr;  // slope-zero flags of s1x/s1y and s2x/s2y
+    unsigned* dep_ctr = nullptr;    // pass-overlap counters of one step (13 segments of dep_stride)
+    int dep_stride = 0;             // 0: the passes run fully ordered
     double* geo_buf = nullptr;
     Geo geo{};
     lsh::TimeRec* tm = nullptr;
@@ -433,6 +441,17 @@ void fwd_passes(const lsh_adjoint* A, const KArgs& a, double* snaps[3][2], doubl
 void fwd_step(const lsh_adjoint* A, cudaStream_t s) {
     const dim3 nbc = cell_grid(A->p.nx, A->p.ny);
     double* const* X = A->X;
+    if (A->dep_ctr) {
+        // the product's overlapped step (lsh_kernels.cuh)
+        double* Y7[7];
+        for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+        Y7[6] = A->X[6];
+        const KArgs a1 = (A->order == 1) ? fwd_args(A, X, X, nullptr, A->acc1, nullptr, nullptr)
+                                         : fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+        const KArgs a2 = (A->order == 1) ? a1 : fwd_args(A, Y7, X, X, A->acc2, A->s2x, A->s2y);
+        enqueue_step_overlap(A->p.nx, A->p.ny, A->order, a1, a2, A->dep_ctr, A->dep_stride, A->tm, 2.0 * A->c.cfl, s);
+        return;
+    }
     if (A->order == 1) {
         const KArgs a = fwd_args(A, X, X, nullptr, A->acc1, nullptr, nullptr);
         fwd_passes<1>(A, a, nullptr, A->acc1, s);
@@ -564,7 +583,36 @@ int Ops::reverse_step(int n) {
     k_set_dt<<<1, 1, 0, s>>>(A->tm, A->d_dts + n);
     double* const* X = A->X;
     const double dt = A->h_dts[n];
-    if (A->order == 1) {
+    if (A->dep_ctr) {
+        // overlapped passes; the edge passes take the accumulator snapshots
+        // themselves, at the cells the reverse sweep reads them
+        unsigned* c = A->dep_ctr;
+        const int st = A->dep_stride, nx = A->p.nx, ny = A->p.ny;
+        if (A->order == 1) {
+            const KArgs a = fwd_args(A, X, nullptr, nullptr, A->acc1, nullptr, nullptr);
+            enqueue_stage_overlap<1, -1>(nx, ny, a, s, Dep{}, c, st, true, A->snap1);
+        } else {
+            double* Y7[7];
+            for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+            Y7[6] = A->X[6];
+            const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+            Dep r1;
+            r1.done = c;
+            launch_pass(false, nbc, cell_block(), s, k_recon_tape, a1, A->tape1, r1);
+            Dep pr;
+            pr.wait = c; pr.target = nbc.x; pr.kind = kDepCell; pr.ntiles = (int)nbc.y;
+            const Dep v1 = enqueue_stage_overlap<2, 1>(nx, ny, a1, s, pr, c + st, st, false, A->snap1);
+            const KArgs a2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
+            Dep r2 = v1;
+            r2.done = c + 6 * st;
+            launch_pass(true, nbc, cell_block(), s, k_recon_tape, a2, A->tape2, r2);
+            Dep pr2;
+            pr2.wait = c + 6 * st; pr2.target = nbc.x; pr2.kind = kDepCell; pr2.ntiles = (int)nbc.y;
+            enqueue_stage_overlap<2, -1>(nx, ny, a2, s, pr2, c + 7 * st, st, true, A->snap2);
+        }
+        // ordered after the passes (a stream operation waits for them all)
+        cudaMemsetAsync(c, 0, size_t(13) * st * sizeof(unsigned), s);
+    } else if (A->order == 1) {
         const KArgs a = fwd_args(A, X, nullptr, nullptr, A->acc1, nullptr, nullptr);
         fwd_passes<1>(A, a, A->snap1, A->acc1, s);
     } else {
@@ -572,11 +620,11 @@ int Ops::reverse_step(int n) {
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
         Y7[6] = A->X[6];
         const KArgs a1 = fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
-        k_recon_tape<<<nb, kCellBlock, 0, s>>>(a1, A->tape1);
+        k_recon_tape<<<nbc, cell_block(), 0, s>>>(a1, A->tape1);
         fwd_passes<2>(A, a1, A->snap1, A->acc1, s);
         k_volume<1><<<nbc, cell_block(), 0, s>>>(a1);
         const KArgs a2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
-        k_recon_tape<<<nb, kCellBlock, 0, s>>>(a2, A->tape2);
+        k_recon_tape<<<nbc, cell_block(), 0, s>>>(a2, A->tape2);
         fwd_passes<2>(A, a2, A->snap2, A->acc2, s);
     }
     // the stage-1 rate's arg-max and the adjoint of the rate
@@ -876,8 +924,9 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     // working arrays: X 7, Y 6, s1/s2 28, acc 14, snaps 12, Xb/Xbn/Yb 18, sxb/syb/accb 21, eta dummy 1, hN 2
     const int narr = 7 + 6 + 28 + 14 + 12 + 18 + 21 + 1 + 2;
     const size_t geo_n = 7 * size_t(params->ny + 1);
+    A->dep_stride = dep_stride_for(params->nx, params->ny);
     const size_t bytes = (size_t(narr) * A->npad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) +
-                         2 * A->npad * sizeof(unsigned) + 2 * A->npad;
+                         2 * A->npad * sizeof(unsigned) + 2 * A->npad + size_t(13) * A->dep_stride * sizeof(unsigned);
     { cudaError_t e = cudaMalloc(&A->slab, bytes); if (e != cudaSuccess) return bail(afail(e, "cudaMalloc adjoint work arrays")); }
     {
         // zero the work arrays and wait: the geometry and gauge copies below go
@@ -905,6 +954,7 @@ int lsh_adjoint_create(const lsh_params* params, int device, int n_gauges, const
     A->tape2 = A->tape1 + A->npad;
     A->szero1 = reinterpret_cast<unsigned char*>(A->tape2 + A->npad);  // zeroed with the slab
     A->szero2 = A->szero1 + A->npad;
+    if (A->dep_stride) A->dep_ctr = reinterpret_cast<unsigned*>(A->szero2 + A->npad);  // zeroed with the slab
     {
         std::vector<double> g(geo_n, 0.0);
         const size_t st = size_t(params->ny + 1);

@@ -166,92 +166,22 @@ void enqueue_passes(const lsh_ctx* ctx, const KArgs& a, cudaStream_t s) {
     k_edges_v<ORDER><<<grid_v(ctx, 1), edge_block_v(), 0, s>>>(a, 1);
 }
 
-// Launch `kernel` on `s`; `dependent`: as a programmatic dependent of the
-// kernel before it on the stream (it may start once that kernel's blocks
-// have all started; its blocks order themselves through the pass counters).
-template <class... P, class... A>
-void launch_pass(bool dependent, dim3 grid, dim3 block, cudaStream_t s, void (*kernel)(P...), A&&... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = dependent ? at : nullptr;
-    cfg.numAttrs = dependent ? 1 : 0;
-    (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
-}
-
-// The passes of one stage with overlap: `prev` is the producer of the first
-// edge pass (the reconstruction at order 2, nothing at order 1: then h0 is
-// the step's first kernel); counters seg[0..4] for h0, h1, v0, v1, volume.
-template <int ORDER, int MODE>
-Dep enqueue_stage_overlap(const lsh_ctx* ctx, const KArgs& a, cudaStream_t s, Dep prev, unsigned* seg,
-                          bool last) {
-    const int nx = ctx->p.nx, ny = ctx->p.ny;
-    const dim3 gh0 = edge_grid_h(nx, ny, 0), gh1 = edge_grid_h(nx, ny, 1);
-    const dim3 gv0 = edge_grid_v(nx, ny, 0), gv1 = edge_grid_v(nx, ny, 1), gc = cell_grid(nx, ny);
-    const int st = ctx->dep_stride;
-    Dep d0 = prev;
-    d0.done = seg;
-    launch_pass(prev.wait != nullptr, gh0, edge_block_h(), s, k_edges_h<true, ORDER>, a, 0, d0);
-    Dep d1;
-    d1.wait = seg; d1.done = seg + st; d1.target = gh0.x; d1.kind = kDepH0; d1.ntiles = (int)gh0.y;
-    launch_pass(true, gh1, edge_block_h(), s, k_edges_h<false, ORDER>, a, 1, d1);
-    Dep d2;
-    d2.wait = seg + st; d2.done = seg + 2 * st; d2.target = gh1.x; d2.kind = kDepH1; d2.ntiles = (int)gh1.y;
-    launch_pass(true, gv0, edge_block_v(), s, k_edges_v<ORDER>, a, 0, d2);
-    Dep d3;
-    d3.wait = seg + 2 * st; d3.done = seg + 3 * st; d3.target = gv0.x; d3.kind = kDepV; d3.ntiles = (int)gv0.y;
-    launch_pass(true, gv1, edge_block_v(), s, k_edges_v<ORDER>, a, 1, d3);
-    Dep d4;
-    d4.wait = seg + 3 * st; d4.done = last ? nullptr : seg + 4 * st; d4.target = gv1.x; d4.kind = kDepV;
-    d4.ntiles = (int)gv1.y;
-    launch_pass(true, gc, cell_block(), s, k_volume<MODE>, a, d4);
-    // the producer description for a pass that reads this stage's volume output
-    Dep next;
-    next.wait = seg + 4 * st; next.target = gc.x; next.kind = kDepCell; next.ntiles = (int)gc.y;
-    return next;
-}
-
 // Enqueue one time step; returns the number of kernels launched.
 int enqueue_step(const lsh_ctx* ctx, cudaStream_t s) {
     const dim3 nbc = cell_grid(ctx->p.nx, ctx->p.ny);
-    const int nk = (ctx->p.order == 1) ? 6 : 13;
     if (ctx->dep_ctr) {
-        unsigned* c = ctx->dep_ctr;
-        const int st = ctx->dep_stride;
+        KArgs a1 = base_args(ctx), a2 = base_args(ctx);
+        for (int k = 0; k < 7; ++k) a1.W[k] = ctx->X[k];
         if (ctx->p.order == 1) {
-            KArgs a = base_args(ctx);
-            for (int k = 0; k < 7; ++k) a.W[k] = ctx->X[k];
-            for (int k = 0; k < 6; ++k) a.Wout[k] = ctx->X[k];
-            enqueue_stage_overlap<1, 0>(ctx, a, s, Dep{}, c, true);
+            for (int k = 0; k < 6; ++k) a1.Wout[k] = ctx->X[k];
         } else {
-            KArgs a1 = base_args(ctx);
-            for (int k = 0; k < 7; ++k) a1.W[k] = ctx->X[k];
             for (int k = 0; k < 6; ++k) a1.Wout[k] = ctx->Y[k];
-            Dep r1;
-            r1.done = c;
-            launch_pass(false, nbc, cell_block(), s, k_recon, a1, r1);
-            Dep pr;
-            pr.wait = c; pr.target = nbc.x; pr.kind = kDepCell; pr.ntiles = (int)nbc.y;
-            Dep v1 = enqueue_stage_overlap<2, 1>(ctx, a1, s, pr, c + st, false);
-            KArgs a2 = base_args(ctx);
             for (int k = 0; k < 6; ++k) a2.W[k] = ctx->Y[k];
             a2.W[6] = ctx->X[6];
             for (int k = 0; k < 6; ++k) { a2.Wout[k] = ctx->X[k]; a2.Xavg[k] = ctx->X[k]; }
-            Dep r2 = v1;
-            r2.done = c + 6 * st;
-            launch_pass(true, nbc, cell_block(), s, k_recon, a2, r2);
-            Dep pr2;
-            pr2.wait = c + 6 * st; pr2.target = nbc.x; pr2.kind = kDepCell; pr2.ntiles = (int)nbc.y;
-            enqueue_stage_overlap<2, 2>(ctx, a2, s, pr2, c + 7 * st, true);
         }
-        // a plain launch: waits for the whole step, then zeroes the counters
-        k_advance<<<1, 256, 0, s>>>(ctx->tm, 2.0 * ctx->p.cfl, c, nk * st);
-        return nk;
+        return enqueue_step_overlap(ctx->p.nx, ctx->p.ny, ctx->p.order, a1, a2, ctx->dep_ctr, ctx->dep_stride, ctx->tm,
+                                    2.0 * ctx->p.cfl, s);
     }
     if (ctx->p.order == 1) {
         KArgs a = base_args(ctx);
@@ -422,12 +352,7 @@ int lsh_create(const lsh_params* p, int device, lsh_ctx** out) {
     // pass-overlap counters: one per block row of each pass of a step (the
     // block rows of the edge and cell kernels), when the grids cover every
     // row in one launch
-    const int dep_rows = std::max({(int)edge_grid_h(p->nx, p->ny, 0).y, (int)edge_grid_v(p->nx, p->ny, 0).y,
-                                   (int)cell_grid(p->nx, p->ny).y});
-    const int nlines_max = p->ny / 2 + 1;
-    const bool overlap = (long long)((nlines_max + kEdgeHBY - 1) / kEdgeHBY) <= 65535 &&
-                         (long long)((p->ny + kEdgeVBY - 1) / kEdgeVBY) <= 65535;
-    const int dep_stride = overlap ? ((dep_rows + 63) & ~63) : 0;
+    const int dep_stride = dep_stride_for(p->nx, p->ny);
     const int kps = (p->order == 1) ? 6 : 13;
     const size_t dep_bytes = size_t(dep_stride) * kps * sizeof(unsigned);
     const size_t bytes = (size_t(n_arrays) * n_pad + ((geo_n + 31) & ~size_t(31))) * sizeof(double) + 256 +

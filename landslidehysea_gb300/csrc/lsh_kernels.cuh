@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <utility>
 
 #include "../../include/lsh.h"
 #include "lsh_passes.cuh"
@@ -343,6 +344,108 @@ __global__ void __launch_bounds__(kCellBlock) k_init_eta(KArgs a) {
     if (id < 0) return;
     a.eta_max[id] = a.W[0][id] + a.W[3][id] - a.W[6][id];
     a.eta_time[id] = 0.0;
+}
+
+// ---------------------------------------------------------------- overlapped launches
+
+// Counters per pass of a step when the passes can overlap: one per block row
+// of the edge and cell kernels, rounded up; 0 when a grid would need more
+// block rows than a launch holds (the passes then run fully ordered).
+inline int dep_stride_for(int nx, int ny) {
+    const int rows = std::max({(int)edge_grid_h(nx, ny, 0).y, (int)edge_grid_v(nx, ny, 0).y, (int)cell_grid(nx, ny).y});
+    const bool fits = (long long)((ny / 2 + 1 + kEdgeHBY - 1) / kEdgeHBY) <= 65535 &&
+                      (long long)((ny + kEdgeVBY - 1) / kEdgeVBY) <= 65535;
+    return fits ? ((rows + 63) & ~63) : 0;
+}
+
+// Launch `kernel` on `s`; `dependent`: as a programmatic dependent of the
+// kernel before it on the stream (it may start once that kernel's blocks
+// have all started; its blocks order themselves through the pass counters).
+template <class... P, class... A>
+inline void launch_pass(bool dependent, dim3 grid, dim3 block, cudaStream_t s, void (*kernel)(P...), A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = dependent ? at : nullptr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
+// The passes of one stage with overlap on an nx x ny grid: `prev` is the
+// producer of the first edge pass (the reconstruction at order 2, nothing
+// at order 1: then h0 is the step's first kernel); counters seg[0..4 st)
+// for h0, h1, v0, v1 and the volume update (`last`: the volume's counters
+// are not needed).  MODE < 0: no volume update (the stage ends after its
+// edge passes).  Returns the producer description for a pass that reads
+// this stage's volume output.
+// snaps (may be null): for the adjoint's recomputation, the three passes
+// after the first copy the partial sums they read to snaps[0], [1], [2].
+template <int ORDER, int MODE>
+inline Dep enqueue_stage_overlap(int nx, int ny, const KArgs& a, cudaStream_t s, Dep prev, unsigned* seg, int st,
+                                 bool last, double* const (*snaps)[2] = nullptr) {
+    KArgs as[3] = {a, a, a};
+    if (snaps)
+        for (int i = 0; i < 3; ++i) { as[i].snap[0] = snaps[i][0]; as[i].snap[1] = snaps[i][1]; }
+    const dim3 gh0 = edge_grid_h(nx, ny, 0), gh1 = edge_grid_h(nx, ny, 1);
+    const dim3 gv0 = edge_grid_v(nx, ny, 0), gv1 = edge_grid_v(nx, ny, 1), gc = cell_grid(nx, ny);
+    Dep d0 = prev;
+    d0.done = seg;
+    launch_pass(prev.wait != nullptr, gh0, edge_block_h(), s, k_edges_h<true, ORDER>, a, 0, d0);
+    Dep d1;
+    d1.wait = seg; d1.done = seg + st; d1.target = gh0.x; d1.kind = kDepH0; d1.ntiles = (int)gh0.y;
+    launch_pass(true, gh1, edge_block_h(), s, k_edges_h<false, ORDER>, as[0], 1, d1);
+    Dep d2;
+    d2.wait = seg + st; d2.done = seg + 2 * st; d2.target = gh1.x; d2.kind = kDepH1; d2.ntiles = (int)gh1.y;
+    launch_pass(true, gv0, edge_block_v(), s, k_edges_v<ORDER>, as[1], 0, d2);
+    Dep d3;
+    d3.wait = seg + 2 * st; d3.done = (MODE < 0 && last) ? nullptr : seg + 3 * st; d3.target = gv0.x;
+    d3.kind = kDepV; d3.ntiles = (int)gv0.y;
+    launch_pass(true, gv1, edge_block_v(), s, k_edges_v<ORDER>, as[2], 1, d3);
+    Dep next;
+    if (MODE < 0) {
+        next.wait = seg + 3 * st; next.target = gv1.x; next.kind = kDepV; next.ntiles = (int)gv1.y;
+        return next;
+    }
+    Dep d4;
+    d4.wait = seg + 3 * st; d4.done = last ? nullptr : seg + 4 * st; d4.target = gv1.x; d4.kind = kDepV;
+    d4.ntiles = (int)gv1.y;
+    launch_pass(true, gc, cell_block(), s, k_volume<(MODE < 0 ? 0 : MODE)>, a, d4);
+    next.wait = seg + 4 * st; next.target = gc.x; next.kind = kDepCell; next.ntiles = (int)gc.y;
+    return next;
+}
+
+// One whole time step with overlapped passes, counters c[0 .. 13 st):
+// order 1 from a1 (in place); order 2 stage 1 from a1 (X -> Y), stage 2 from
+// a2 (Y -> X with the average).  The clock kernel closes the step as a
+// plain launch and zeroes the counters.  Returns the kernels launched.
+inline int enqueue_step_overlap(int nx, int ny, int order, const KArgs& a1, const KArgs& a2, unsigned* c, int st,
+                                TimeRec* tm, double two_cfl, cudaStream_t s) {
+    const int nk = (order == 1) ? 6 : 13;
+    if (order == 1) {
+        enqueue_stage_overlap<1, 0>(nx, ny, a1, s, Dep{}, c, st, true);
+    } else {
+        const dim3 nbc = cell_grid(nx, ny);
+        Dep r1;
+        r1.done = c;
+        launch_pass(false, nbc, cell_block(), s, k_recon, a1, r1);
+        Dep pr;
+        pr.wait = c; pr.target = nbc.x; pr.kind = kDepCell; pr.ntiles = (int)nbc.y;
+        const Dep v1 = enqueue_stage_overlap<2, 1>(nx, ny, a1, s, pr, c + st, st, false);
+        Dep r2 = v1;
+        r2.done = c + 6 * st;
+        launch_pass(true, nbc, cell_block(), s, k_recon, a2, r2);
+        Dep pr2;
+        pr2.wait = c + 6 * st; pr2.target = nbc.x; pr2.kind = kDepCell; pr2.ntiles = (int)nbc.y;
+        enqueue_stage_overlap<2, 2>(nx, ny, a2, s, pr2, c + 7 * st, st, true);
+    }
+    // a plain launch: waits for the whole step, then zeroes the counters
+    k_advance<<<1, 256, 0, s>>>(tm, two_cfl, c, nk * st);
+    return nk;
 }
 
 }  // namespace

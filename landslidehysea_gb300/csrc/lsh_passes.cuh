@@ -59,6 +59,11 @@ struct KArgs {
     double* eta_time;
     TimeRec* tm;
     unsigned char* szero;  // per cell: 1 when the stored slopes are all zero (may be null)
+    // the adjoint's recomputation (null otherwise): an edge pass after the
+    // first copies acc[0], acc[3] of its non-dry edges' cells, as the pass
+    // before left them, to snap[0], snap[1] -- the partial sums its limiter
+    // reads, which the reverse sweep needs at exactly those cells
+    double* snap[2];
 };
 
 // Depths of a face (first order: the cell's; second order: reconstructed).
@@ -211,6 +216,14 @@ LSH_HD void do_edge(const KArgs& a, int x, int y, double dt) {
             }
         }
         return;
+    }
+    if (!FIRST && a.snap[0]) {
+        a.snap[0][id0] = a.acc[0][id0];
+        a.snap[1][id0] = a.acc[3][id0];
+        if (e.interior) {
+            a.snap[0][id1] = a.acc[0][id1];
+            a.snap[1][id1] = a.acc[3][id1];
+        }
     }
     face_rest<DIR, ORDER>(a, id0, side0, pos_normal, e.A);
     if (e.interior) {
