@@ -35,6 +35,7 @@
 #include "../../include/lsh.h"
 #include "lsh_adjoint.cuh"
 #include "lsh_kernels.cuh"
+#include "lsh_queue.cuh"
 #include "lsh_revolve.h"
 #include "lsh_setup.h"
 
@@ -213,8 +214,8 @@ __global__ void __launch_bounds__(kCellBlock) k_adj_argmax(const double* acc6, G
 
 // dt' = 2 CFL / R: the adjoint of the largest rate R is -dt'bar dt' / R (the
 // volume adjoint turns it into acc_w's, times 1 / area, at the arg-max cell).
-__global__ void k_adj_ratebar(const unsigned long long* rmax, const long long* cell, const double* red,
-                              const double* dt_next, RateSel* out) {
+__device__ __forceinline__ void ratebar_body(const unsigned long long* rmax, const long long* cell, const double* red,
+                                             const double* dt_next, RateSel* out) {
     const double R = lshm::from_bits(*rmax);
     const long long c = *cell;
     const double dtb = red[0];
@@ -227,11 +228,14 @@ __global__ void k_adj_ratebar(const unsigned long long* rmax, const long long* c
     out->bar = -dtb * (*dt_next / R);
 }
 
+__global__ void k_adj_ratebar(const unsigned long long* rmax, const long long* cell, const double* red,
+                              const double* dt_next, RateSel* out) {
+    ratebar_body(rmax, cell, red, dt_next, out);
+}
+
 // The misfit's adjoint at the state after a step: 2 w (eta - target) at each gauge.
-__global__ void k_adj_gauges(double* hb1, double* hb2, const int* gauges, int ng, const double* eta, const double* tgt,
-                             double w) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ng) return;
+__device__ __forceinline__ void gauge_add(double* hb1, double* hb2, const int* gauges, int ng, const double* eta,
+                                          const double* tgt, double w, int g) {
     const int id = gauges[g];
     // several gauges may share a cell: one thread adds them all, in order
     if (g > 0) {
@@ -245,16 +249,29 @@ __global__ void k_adj_gauges(double* hb1, double* hb2, const int* gauges, int ng
     hb2[id] += s;
 }
 
+__global__ void k_adj_gauges(double* hb1, double* hb2, const int* gauges, int ng, const double* eta, const double* tgt,
+                             double w) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ng) gauge_add(hb1, hb2, gauges, ng, eta, tgt, w, g);
+}
+
 // Thin-layer projection: the adjoint of a layer thinner than h_adj (in the
 // state the adjoint belongs to) is zeroed; the tangent-linear model zeroes
 // the same tangents, so the pair stays transposes of each other.
-__global__ void __launch_bounds__(kCellBlock) k_adj_project(double* b0, double* b1, double* b2,
-                                                            double* b3, double* b4, double* b5, const double* h1,
-                                                            const double* h2, long long N, double h_adj) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void project_cells(double* b0, double* b1, double* b2, double* b3, double* b4, double* b5,
+                                              const double* h1, const double* h2, long long N, double h_adj,
+                                              long long start, long long stride) {
+    for (long long i = start; i < N; i += stride) {
         if (h1[i] < h_adj) { b0[i] = 0.0; b1[i] = 0.0; b2[i] = 0.0; }
         if (h2[i] < h_adj) { b3[i] = 0.0; b4[i] = 0.0; b5[i] = 0.0; }
     }
+}
+
+__global__ void __launch_bounds__(kCellBlock) k_adj_project(double* b0, double* b1, double* b2,
+                                                            double* b3, double* b4, double* b5, const double* h1,
+                                                            const double* h2, long long N, double h_adj) {
+    project_cells(b0, b1, b2, b3, b4, b5, h1, h2, N, h_adj, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                  (long long)gridDim.x * blockDim.x);
 }
 
 __global__ void k_adj_init(AdjArgs a, const RateSel* rs, double* part) {
@@ -272,7 +289,7 @@ __global__ void k_adj_init(AdjArgs a, const RateSel* rs, double* part) {
 // Sum the step's partials in a fixed order: red[0] = the dt adjoint of the
 // step's input dt; red[1..8] += the constant adjoints.  Warp k sums
 // component k (lane-strided, then a shuffle tree): deterministic.
-__global__ void __launch_bounds__(32 * kRed) k_adj_reduce(const double* part, int nparts, double* red) {
+__device__ __forceinline__ void reduce_body(const double* part, int nparts, double* red) {
     const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double s = 0.0;
     for (int i = lane; i < nparts; i += 32) s += part[(size_t)i * kRed + k];
@@ -284,28 +301,43 @@ __global__ void __launch_bounds__(32 * kRed) k_adj_reduce(const double* part, in
     }
 }
 
+__global__ void __launch_bounds__(32 * kRed) k_adj_reduce(const double* part, int nparts, double* red) {
+    reduce_body(part, nparts, red);
+}
+
 // First level of the partial sums: block b adds rows [b chunk, (b+1) chunk)
 // into row b of out (warp k: component k, lane-strided then a shuffle tree),
 // a fixed order, so the total stays bit-reproducible.
-__global__ void __launch_bounds__(32 * kRed) k_adj_reduce_rows(const double* part, long long nparts, long long chunk,
-                                                               double* out) {
+constexpr int kReduceRows = 128;  // first-level rows of a step's partial sums
+
+__device__ __forceinline__ void reduce_rows_body(const double* part, long long nparts, long long chunk, double* out,
+                                                 unsigned b) {
     const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long r0 = (long long)blockIdx.x * chunk;
+    const long long r0 = (long long)b * chunk;
     const long long r1 = (r0 + chunk < nparts) ? r0 + chunk : nparts;
     double s = 0.0;
     for (long long i = r0 + lane; i < r1; i += 32) s += part[(size_t)i * kRed + k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) out[(size_t)blockIdx.x * kRed + k] = s;
+    if (lane == 0) out[(size_t)b * kRed + k] = s;
 }
 
-__global__ void k_set_dt(lsh::TimeRec* tm, const double* dt) {
+__global__ void __launch_bounds__(32 * kRed) k_adj_reduce_rows(const double* part, long long nparts, long long chunk,
+                                                               double* out) {
+    reduce_rows_body(part, nparts, chunk, out, blockIdx.x);
+}
+
+// A replayed step's time record: the recorded dt.  A timed-out wait's bit
+// stays (the host reads it after the run, and later waits give up at once).
+__device__ __forceinline__ void set_dt_body(lsh::TimeRec* tm, const double* dt) {
     tm->dt = *dt;
     tm->rmax_bits = kRateInitBits;
     tm->done = 0;
-    tm->err = 0;
+    tm->err &= 1 << LSH_ERR_TIMEOUT;
     tm->t_end = INFINITY;
 }
+
+__global__ void k_set_dt(lsh::TimeRec* tm, const double* dt) { set_dt_body(tm, dt); }
 
 __global__ void k_record(const lsh::TimeRec* tm, double* dt_out) { *dt_out = tm->dt; }
 
@@ -340,6 +372,7 @@ struct lsh_adjoint {
     int device = 0;
     int sms = 152;
     cudaStream_t stream = nullptr;
+    bool own_stream = true;    // false: a batch's stream, destroyed with the batch
     size_t N = 0, npad = 0;
     int order = 1;
     // one slab for the working arrays
@@ -649,10 +682,9 @@ int Ops::reverse_step(int n) {
         rev_stage<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s);
     }
     {
-        constexpr int kRows = 128;
-        const long long chunk = (nparts + kRows - 1) / kRows;
-        k_adj_reduce_rows<<<kRows, 32 * kRed, 0, s>>>(A->part, nparts, chunk, A->part2);
-        k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part2, kRows, A->red);
+        const long long chunk = (nparts + kReduceRows - 1) / kReduceRows;
+        k_adj_reduce_rows<<<kReduceRows, 32 * kRed, 0, s>>>(A->part, nparts, chunk, A->part2);
+        k_adj_reduce<<<1, 32 * kRed, 0, s>>>(A->part2, kReduceRows, A->red);
     }
     for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
     if (n >= 1) misfit_and_project(A, n, A->X[0], A->X[3], s);
@@ -853,43 +885,748 @@ void grad_params_of(const lsh_adjoint* A, double gp[4]) {
     lsh::param_grads(A->p.angle1, A->p.mf0, A->p.mfs, A->p.r, A->p.gravity, A->p.eps_h, A->p.L, A->p.H, cb, gp);
 }
 
-// The schedule's operations applied to every member in turn: one schedule,
-// one slot count, every member's state at the same step.
-struct BatchOps : lsh::RevolveOps {
-    std::vector<Ops> ops;
-    int advance(int from, int to) override {
-        for (int n = from; n < to; ++n)
-            for (auto& o : ops)
-                if (int st = o.advance(n, n + 1)) return st;
-        return 0;
-    }
-    int store(int k) override {
-        for (auto& o : ops)
-            if (int st = o.store(k)) return st;
-        return 0;
-    }
-    int restore(int k, int step) override {
-        for (auto& o : ops)
-            if (int st = o.restore(k, step)) return st;
-        return 0;
-    }
-    int reverse_step(int n) override {
-        for (auto& o : ops)
-            if (int st = o.reverse_step(n)) return st;
-        return 0;
-    }
+// ------------------------------------------------------------------ batched adjoint
+//
+// lsh_adjoint_batch_* walks one checkpoint schedule for all members, and
+// each operation of the schedule is one set of launches for all members of
+// an order (a group), with no per-member kernel sequence:
+//   forward step   one persistent queue launch (lsh_queue.cuh: every
+//                  member's tiles of every pass), the clock kernel, and a
+//                  record kernel (dt, gauges);
+//   reversed step  the recomputation as one queue launch (reconstruction
+//                  with its branch tape, the edge passes taking their
+//                  snapshots), then the whole adjoint step as ONE persistent
+//                  launch of k_adjb_reverse, then the partial sums and the
+//                  misfit, each one launch over all members.
+// k_adjb_reverse pulls (pass, member, tile) items in pass order: the
+// adjoint's zeroing, the stage-1 rate's max and arg-max (each waiting for all
+// of the member's items of the pass before), the rate's adjoint (one item
+// per member), then each stage's volume, four colour and reconstruction
+// adjoints, last stage first.  Its tiles are the single adjoint kernels'
+// 128-thread blocks and each writes its partial-sum row where that kernel's
+// block does, so every member's gradient is bit-identical to a run of its
+// own.  An item waits only for the rows of its member that it reads or
+// overwrites in the pass it depends on, with bounded waits as in the queue.
+
+struct ReconTape {
+    static constexpr bool kOn = true;
+    __device__ static unsigned run(const KArgs& a, int id) { return lsh::recon_cell_tape(a, id); }
 };
+
+constexpr int kRThreads = kAdjCellBlock;  // the adjoint kernels' block size
+constexpr int kRMaxPasses = 16;
+// CTAs per SM of the reverse queue (its register budget: 40 at 12) and the
+// items a CTA takes per queue fetch.  Unlike the one-kernel-per-pass path,
+// the queue wants many resident CTAs: each item's waits, argument copy and
+// barriers leave its CTA idle, and the others fill that time.  The
+// 64-member calibration's reverse sweep (100 steps), s, by CTAs per SM /
+// fetch: 2/2 8.79, 3/2 7.02, 4/1 6.44, 4/2 6.23, 4/4 6.14, 5/4 5.69,
+// 6/4 5.33, 7/4 5.15, 8/4 4.96, 10/4 4.75, 12/4 4.63, 12/8 4.67, 14/4 4.60,
+// 16/2 4.56, 16/4 4.74, 16/8 4.95.
+#ifndef LSH_ADJB_MINB
+#define LSH_ADJB_MINB 12
+#endif
+#ifndef LSH_ADJB_FETCH
+#define LSH_ADJB_FETCH 4
+#endif
+constexpr int kRVars = 10;                // AdjArgs variants of a step (per Xb / Xbn parity)
+
+// Tilings: horizontal edges of parity 0 / 1 (16 columns x 8 edge lines),
+// vertical edges of parity 0 / 1 (8 edge columns x 16 rows), cells (16 x 8),
+// one item per member.
+enum RKind : int { kRH0 = 0, kRH1 = 1, kRV0 = 2, kRV1 = 3, kRCell = 4, kRMember = 5, kRKinds = 6 };
+enum ROp : int {
+    kRZero = 0, kRRateMax, kRArgMax, kRRateBar, kRVol0, kRVol1, kRVol2, kREV1, kREV0, kREH1, kREH0, kRRecon
+};
+
+struct RPass {
+    int op, kind, var;
+    int prod;   // the pass whose rows it waits for (-1: none)
+    int fprod;  // the pass all of whose items of the member it waits for (-1: none)
+    int rate;   // 1: reads the stage-1 rate selection
+    int parts;  // 1: writes one partial-sum row per item
+    int item_off, ctr_off;
+};
+
+// Per member: what the rate items, the partial sums and the waits use.
+struct RMember {
+    unsigned long long* rmax;
+    long long* argmax;
+    RateSel* rsel;
+    const double* red;   // red[0]: the adjoint of the next step's dt
+    const double* dts;   // the recorded dt of every step
+    double* part;        // partial-sum rows
+    lsh::TimeRec* tm;
+};
+
+struct RPlan {
+    int n, npass, total_items;
+    RPass pass[kRMaxPasses];
+    const int* tile_pre;  // [kind][n + 1]
+    const int* row_pre;   // [kind][n + 1]
+    const int* tiles_x;   // [kind][n]
+    const int* part_off;  // [pass][n]: the member's first partial row of the pass
+    const AdjArgs* args;  // [parity][kRVars][n]
+    const RMember* mem;   // [n]
+    unsigned* ctr;
+    unsigned* head;
+    int* abort_flag;
+};
+
+// Forward record of a step: dt and the gauges.
+struct FMember {
+    const lsh::TimeRec* tm;
+    double* dts;
+    const double* h1;
+    const double* h2;
+    const double* H;
+    const int* gauges;
+    int ng;
+    double* eta;
+};
+
+// The misfit's adjoint and the thin-layer projection after a reversed step.
+struct RMis {
+    double* b[6];          // the adjoint at the step's state
+    const double* h1;      // that state's depths
+    const double* h2;
+    const int* gauges;
+    int ng;                // 0: no misfit term
+    const double* eta;     // [nsteps][ng]
+    const double* tgt;
+    double w, h_adj;
+    long long N;
+};
+
+struct RRed {
+    const double* part;
+    long long nparts;
+    double* part2;
+    double* red;
+};
+
+void adj_tiles(int nx, int ny, int kind, int& tx, int& ty) {
+    if (kind == kRMember) { tx = ty = 1; return; }
+    const dim3 g = (kind == kRCell) ? adj_cell_grid(nx, ny) : adj_edge_grid(nx, ny, kind >= kRV0 ? 1 : 0, kind & 1);
+    tx = (int)g.x;
+    ty = (int)g.y;
+}
+
+// Cell rows an item reads or overwrites.  The stage-1 volume adjoint (kRVol1)
+// overwrites the slope adjoints that the stage-2 reconstruction adjoint reads
+// one row around each cell, so it covers one row more on each side.
+__device__ __forceinline__ void r_item_rows(int op, int kind, int ty, int ny, int& r0, int& r1) {
+    if (kind == kRH0 || kind == kRH1) { const int y0 = kind + 16 * ty; r0 = y0 - 1; r1 = y0 + 14; }
+    else if (kind == kRV0 || kind == kRV1) { r0 = 16 * ty; r1 = r0 + 15; }
+    else if (op == kRRecon || op == kRVol1) { r0 = 8 * ty - 1; r1 = 8 * ty + 8; }
+    else { r0 = 8 * ty; r1 = r0 + 7; }
+    r0 = max(r0, 0);
+    r1 = min(r1, ny - 1);
+}
+
+// Tile rows of a pass of `kind` that touch cell rows [r0, r1].
+__device__ __forceinline__ void r_producer_rows(int kind, int r0, int r1, int& t0, int& t1) {
+    if (kind == kRV0 || kind == kRV1) { t0 = r0 / 16; t1 = r1 / 16; }
+    else if (kind == kRCell) { t0 = r0 / 8; t1 = r1 / 8; }
+    else if (kind == kRMember) { t0 = 0; t1 = 0; }
+    else {
+        // horizontal edge row y = p + 2 t touches cell rows y - 1 and y
+        const int p = kind;
+        t0 = (max(r0 - p + 1, 0) / 2) / 8;
+        t1 = (max(r1 + 1 - p, 0) / 2) / 8;
+    }
+}
+
+template <int DIR, bool FIRST, int ORDER, int PAR>
+__device__ __forceinline__ void r_edges(const AdjArgs& a, int tx, int ty, double* part) {
+    const int nx = a.c.nx, ny = a.c.ny, tid = threadIdx.x;
+    double dtb = 0.0;
+    ConstBar cb;
+    lsh::cb_zero(cb);
+    if (DIR == 0) {
+        const int u = tx * 16 + (tid & 15), w = ty * 8 + (tid >> 4);
+        if (u < nx && w < (ny - PAR) / 2 + 1) lsh::edge_adj_body<0, FIRST, ORDER>(a, u, PAR + 2 * w, dtb, cb);
+    } else {
+        const int u = tx * 8 + (tid & 7), w = ty * 16 + (tid >> 3);
+        if (u < (nx - PAR) / 2 + 1 && w < ny) lsh::edge_adj_body<1, false, ORDER>(a, PAR + 2 * u, w, dtb, cb);
+    }
+    double v[kRed];
+    pack9(dtb, cb, v);
+    block_sum9<kRThreads>(v, part);
+}
+
+template <int MODE>
+__device__ __forceinline__ void r_volume(const AdjArgs& a, int tx, int ty, double* part) {
+    const int tid = threadIdx.x, i = tx * 16 + (tid & 15), j = ty * 8 + (tid >> 4);
+    double dtb = 0.0;
+    ConstBar cb;
+    lsh::cb_zero(cb);
+    if (i < a.c.nx && j < a.c.ny) lsh::volume_adj_body<MODE>(a, j * a.c.nx + i, dtb, cb);
+    double v[kRed];
+    pack9(dtb, cb, v);
+    block_sum9<kRThreads>(v, part);
+}
+
+// Max (ARG false) or arg-max (ARG true) of the stage-1 rate over a cell tile.
+template <bool ARG>
+__device__ __forceinline__ void r_rate(const AdjArgs& a, const RMember& M, int tx, int ty) {
+    const int tid = threadIdx.x, i = tx * 16 + (tid & 15), j = ty * 8 + (tid >> 4);
+    const bool in = (i < a.c.nx && j < a.c.ny);
+    const long long id = (long long)j * a.c.nx + i;
+    unsigned long long b = 0;
+    if (in) {
+        const double w = a.acc[6][id];
+        const double rate = (w < lsh::kEps) ? 0.0 : w * a.geo.inv_area[j];
+        b = lshm::bits_of(rate);
+    }
+    if (!ARG) {
+        lsh::block_max_bits<kRThreads>(b, M.rmax);
+    } else {
+        const unsigned long long m = *M.rmax;
+        if (in && m != 0 && b == m) atomicMin((unsigned long long*)M.argmax, (unsigned long long)id);
+    }
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(kRThreads, LSH_ADJB_MINB) k_adjb_reverse(RPlan P, int parity, int step) {
+    __shared__ __align__(16) unsigned long long sargs[(sizeof(AdjArgs) + 7) / 8];
+    __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy, s_lo, s_hi, s_key;
+    AdjArgs& a = *reinterpret_cast<AdjArgs*>(sargs);
+    const int tid = threadIdx.x;
+    if (tid == 0) { s_lo = 0; s_hi = 0; s_key = -1; }
+    for (;;) {
+        if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)LSH_ADJB_FETCH);
+        __syncthreads();
+        const int first = s_first;
+        if (first >= P.total_items) break;
+        const int last = min(first + LSH_ADJB_FETCH, P.total_items);
+        for (int it = first; it < last; ++it) {
+            if (tid == 0) {
+                if (it < s_lo || it >= s_hi) {
+                    int p = 0;
+                    while (p + 1 < P.npass && it >= P.pass[p + 1].item_off) ++p;
+                    const int kind = P.pass[p].kind;
+                    const int* tp = P.tile_pre + kind * (P.n + 1);
+                    const int l = it - P.pass[p].item_off;
+                    int lo = 0, hi = P.n - 1;  // the member: the last one whose first tile is <= l
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (tp[mid] <= l) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    s_pass = p;
+                    s_scen = lo;
+                    s_lo = P.pass[p].item_off + tp[lo];
+                    s_hi = P.pass[p].item_off + tp[lo + 1];
+                    s_ntx = P.tiles_x[kind * P.n + lo];
+                }
+                s_tile = it - s_lo;
+                const int key = (parity * kRVars + P.pass[s_pass].var) * P.n + s_scen;
+                s_copy = (key != s_key);
+                s_key = key;
+            }
+            __syncthreads();
+            const int p = s_pass, s = s_scen, t = s_tile, ntx = s_ntx;
+            const RPass ps = P.pass[p];
+            if (s_copy) {
+                const unsigned long long* src =
+                    reinterpret_cast<const unsigned long long*>(P.args + (parity * kRVars + ps.var) * P.n + s);
+                for (int k = tid; k < (int)((sizeof(AdjArgs) + 7) / 8); k += kRThreads) sargs[k] = src[k];
+                __syncthreads();
+            }
+            const int ty = t / ntx, tx = t - ty * ntx;
+            const RMember& M = P.mem[s];
+            if (tid == 0) {
+                bool gave_up = false;
+                unsigned long long start = 0;
+                if (ps.prod >= 0) {
+                    const RPass pp = P.pass[ps.prod];
+                    int r0, r1, t0, t1;
+                    r_item_rows(ps.op, ps.kind, ty, a.c.ny, r0, r1);
+                    r_producer_rows(pp.kind, r0, r1, t0, t1);
+                    const int rbase = P.row_pre[pp.kind * (P.n + 1) + s];
+                    const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
+                    t0 = max(t0, 0);
+                    t1 = min(t1, nrows - 1);
+                    gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, t0, t1, (unsigned)P.tiles_x[pp.kind * P.n + s],
+                                               P.abort_flag, start);
+                }
+                if (!gave_up && ps.fprod >= 0) {
+                    const RPass pp = P.pass[ps.fprod];
+                    const int rbase = P.row_pre[pp.kind * (P.n + 1) + s];
+                    const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
+                    gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, 0, nrows - 1, (unsigned)P.tiles_x[pp.kind * P.n + s],
+                                               P.abort_flag, start);
+                }
+                if (gave_up) atomicOr(&M.tm->err, 1 << LSH_ERR_TIMEOUT);
+                // the step's dt and, for the stage-1 passes, the rate selection
+                a.dt = M.dts[step];
+                if (ps.rate) { a.rate_cell = M.rsel->cell; a.rate_bar = M.rsel->bar; }
+                else { a.rate_cell = -1; a.rate_bar = 0.0; }
+            }
+            __syncthreads();
+            double* part = ps.parts ? M.part + ((size_t)P.part_off[p * P.n + s] + t) * kRed : nullptr;
+            switch (ps.op) {
+                case kRZero: {
+                    const int i = tx * 16 + (tid & 15), j = ty * 8 + (tid >> 4);
+                    if (i < a.c.nx && j < a.c.ny) {
+                        const int id = j * a.c.nx + i;
+                        for (int k = 0; k < 6; ++k) a.Wbar[k][id] = 0.0;
+                        if (a.Xbar[0])
+                            for (int k = 0; k < 6; ++k) a.Xbar[k][id] = 0.0;
+                    }
+                    break;
+                }
+                case kRRateMax: r_rate<false>(a, M, tx, ty); break;
+                case kRArgMax: r_rate<true>(a, M, tx, ty); break;
+                case kRRateBar:
+                    if (tid == 0) ratebar_body(M.rmax, M.argmax, M.red, M.dts + step + 1, M.rsel);
+                    break;
+                case kREV1: r_edges<1, false, ORDER, 1>(a, tx, ty, part); break;
+                case kREV0: r_edges<1, false, ORDER, 0>(a, tx, ty, part); break;
+                case kREH1: r_edges<0, false, ORDER, 1>(a, tx, ty, part); break;
+                case kREH0: r_edges<0, true, ORDER, 0>(a, tx, ty, part); break;
+                default:
+                    if constexpr (ORDER == 1) {
+                        r_volume<0>(a, tx, ty, part);
+                    } else {
+                        if (ps.op == kRVol2) r_volume<2>(a, tx, ty, part);
+                        else if (ps.op == kRVol1) r_volume<1>(a, tx, ty, part);
+                        else {
+                            const int i = tx * 16 + (tid & 15), j = ty * 8 + (tid >> 4);
+                            if (i < a.c.nx && j < a.c.ny) lsh::recon_adj_cell(a, j * a.c.nx + i);
+                        }
+                    }
+                    break;
+            }
+            __syncthreads();  // the tile's writes are done, and sargs may be refilled
+            if (tid == 0) queue_done(P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty);
+        }
+    }
+}
+
+// Every member's time record for step `step` (k_set_dt), and the arg-max
+// scratch reset.
+__global__ void k_adjb_pre(const RMember* t, int n, int step) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const RMember M = t[s];
+    set_dt_body(M.tm, M.dts + step);
+    *M.rmax = 0ull;
+    *M.argmax = 0x7fffffffffffffffLL;
+}
+
+// After a forward step: its dt and gauge records (k_record, k_gauge_eta); one block per member.
+__global__ void k_adjb_record(const FMember* t, int step) {
+    const FMember f = t[blockIdx.x];
+    if (threadIdx.x == 0) f.dts[step + 1] = f.tm->dt;
+    for (int g = threadIdx.x; g < f.ng; g += blockDim.x) {
+        const int id = f.gauges[g];
+        f.eta[(size_t)step * f.ng + g] = (f.h1[id] + f.h2[id]) - f.H[id];
+    }
+}
+
+// The queues' counters and heads back to zero.
+__global__ void k_adjb_reset(unsigned* c1, int n1, unsigned* h1, unsigned* c2, int n2, unsigned* h2) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    if (gid == 0) { *h1 = 0u; *h2 = 0u; }
+    for (int i = gid; i < n1; i += stride) c1[i] = 0u;
+    for (int i = gid; i < n2; i += stride) c2[i] = 0u;
+}
+
+__global__ void __launch_bounds__(32 * kRed) k_adjb_reduce_rows(const RRed* t) {
+    const RRed r = t[blockIdx.y];
+    reduce_rows_body(r.part, r.nparts, (r.nparts + kReduceRows - 1) / kReduceRows, r.part2, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(32 * kRed) k_adjb_reduce(const RRed* t) {
+    const RRed r = t[blockIdx.x];
+    reduce_body(r.part2, kReduceRows, r.red);
+}
+
+__global__ void k_adjb_gauges(const RMis* t, int m) {
+    const RMis& r = t[blockIdx.y];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= r.ng) return;
+    gauge_add(r.b[0], r.b[3], r.gauges, r.ng, r.eta + (size_t)(m - 1) * r.ng, r.tgt + (size_t)(m - 1) * r.ng, r.w, g);
+}
+
+__global__ void __launch_bounds__(kCellBlock) k_adjb_project(const RMis* t) {
+    const RMis& r = t[blockIdx.y];
+    if (!(r.h_adj > 0.0)) return;
+    project_cells(r.b[0], r.b[1], r.b[2], r.b[3], r.b[4], r.b[5], r.h1, r.h2, r.N, r.h_adj,
+                  (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// The members of one order, with their queues and tables.
+struct AdjGroup {
+    int order = 1;
+    std::vector<lsh_adjoint*> m;
+    KArgs* d_kargs = nullptr;  // [2][n] the forward step, then [8][n] the recomputation
+    void* qmem_fwd = nullptr;
+    void* qmem_rec = nullptr;
+    void* rmem = nullptr;      // the reverse plan's tables and counters
+    void* tables = nullptr;    // AdjArgs [2][kRVars][n], RMember [n], FMember [n], RMis [2][n], RRed [n]
+    BPlan fwd{}, rec{};
+    int nctr_fwd = 0, nctr_rec = 0;
+    RPlan rev{};
+    int nctr_rev = 0;
+    AdjArgs* d_aargs = nullptr;
+    RMember* d_mem = nullptr;
+    FMember* d_fmem = nullptr;
+    RMis* d_mis = nullptr;
+    RRed* d_red = nullptr;
+    int max_ng = 0;
+    unsigned proj_blocks = 1;
+    int parity = 0;            // Xb / Xbn as the AdjArgs of parity 0 hold them, or swapped (1)
+};
+
+void free_group(AdjGroup& g) {
+    cudaFree(g.d_kargs); cudaFree(g.qmem_fwd); cudaFree(g.qmem_rec); cudaFree(g.rmem); cudaFree(g.tables);
+    g = AdjGroup{};
+}
+
+// The reverse plan (order 2: 16 passes, order 1: 9).
+int build_rplan(AdjGroup& g) {
+    const int n = (int)g.m.size();
+    struct Spec { int op, kind, var, prod, fprod, rate, parts; };
+    std::vector<Spec> sp;
+    if (g.order == 2) {
+        sp = {{kRZero, kRCell, 5, -1, -1, 0, 0},   {kRRateMax, kRCell, 0, -1, -1, 0, 0},
+              {kRArgMax, kRCell, 0, -1, 1, 0, 0},  {kRRateBar, kRMember, 0, -1, 2, 0, 0},
+              {kRVol2, kRCell, 5, 0, -1, 0, 1},    {kREV1, kRV1, 6, 4, -1, 0, 1},
+              {kREV0, kRV0, 7, 5, -1, 0, 1},       {kREH1, kRH1, 8, 6, -1, 0, 1},
+              {kREH0, kRH0, 9, 7, -1, 0, 1},       {kRRecon, kRCell, 5, 8, -1, 0, 0},
+              {kRVol1, kRCell, 0, 9, 3, 1, 1},     {kREV1, kRV1, 1, 10, -1, 1, 1},
+              {kREV0, kRV0, 2, 11, -1, 1, 1},      {kREH1, kRH1, 3, 12, -1, 1, 1},
+              {kREH0, kRH0, 4, 13, -1, 1, 1},      {kRRecon, kRCell, 0, 14, -1, 0, 0}};
+    } else {
+        sp = {{kRZero, kRCell, 0, -1, -1, 0, 0},  {kRRateMax, kRCell, 0, -1, -1, 0, 0},
+              {kRArgMax, kRCell, 0, -1, 1, 0, 0}, {kRRateBar, kRMember, 0, -1, 2, 0, 0},
+              {kRVol0, kRCell, 0, 0, 3, 1, 1},    {kREV1, kRV1, 1, 4, -1, 1, 1},
+              {kREV0, kRV0, 2, 5, -1, 1, 1},      {kREH1, kRH1, 3, 6, -1, 1, 1},
+              {kREH0, kRH0, 4, 7, -1, 1, 1}};
+    }
+    std::vector<int> tile_pre(size_t(kRKinds) * (n + 1)), row_pre(size_t(kRKinds) * (n + 1)), tiles_x(size_t(kRKinds) * n);
+    long long kind_tiles[kRKinds], kind_rows[kRKinds];
+    for (int k = 0; k < kRKinds; ++k) {
+        long long tsum = 0, rsum = 0;
+        for (int s = 0; s < n; ++s) {
+            int tx, ty;
+            adj_tiles(g.m[s]->p.nx, g.m[s]->p.ny, k, tx, ty);
+            tile_pre[k * (n + 1) + s] = (int)tsum;
+            row_pre[k * (n + 1) + s] = (int)rsum;
+            tiles_x[k * n + s] = tx;
+            tsum += (long long)tx * ty;
+            rsum += ty;
+        }
+        tile_pre[k * (n + 1) + n] = (int)tsum;
+        row_pre[k * (n + 1) + n] = (int)rsum;
+        kind_tiles[k] = tsum;
+        kind_rows[k] = rsum;
+    }
+    RPlan& P = g.rev;
+    P = RPlan{};
+    P.n = n;
+    P.npass = (int)sp.size();
+    std::vector<int> part_off(sp.size() * n, 0);
+    std::vector<long long> part_run(n, 0);
+    long long items = 0, ctrs = 0;
+    for (int i = 0; i < P.npass; ++i) {
+        RPass& q = P.pass[i];
+        q.op = sp[i].op; q.kind = sp[i].kind; q.var = sp[i].var; q.prod = sp[i].prod; q.fprod = sp[i].fprod;
+        q.rate = sp[i].rate; q.parts = sp[i].parts;
+        q.item_off = (int)items;
+        q.ctr_off = (int)ctrs;
+        items += kind_tiles[q.kind];
+        ctrs += kind_rows[q.kind];
+        for (int s = 0; s < n; ++s) {
+            part_off[(size_t)i * n + s] = (int)part_run[s];
+            if (q.parts) part_run[s] += tile_pre[q.kind * (n + 1) + s + 1] - tile_pre[q.kind * (n + 1) + s];
+        }
+    }
+    for (int s = 0; s < n; ++s)
+        if (part_run[s] > g.m[s]->part_rows) { lsh::set_last_error("batched adjoint: partial-sum rows"); return LSH_ERR_INVALID; }
+    if (items > 0x7fffffffLL - 1024 || ctrs > 0x7fffffffLL) {
+        lsh::set_last_error("batched adjoint too large for one step's work queue");
+        return LSH_ERR_INVALID;
+    }
+    P.total_items = (int)items;
+    g.nctr_rev = (int)ctrs;
+    const size_t nints = tile_pre.size() + row_pre.size() + tiles_x.size() + part_off.size();
+    const size_t ibytes = (nints * sizeof(int) + 255) & ~size_t(255);
+    A_CUDA(cudaMalloc(&g.rmem, ibytes + size_t(ctrs) * sizeof(unsigned) + 256));
+    int* ti = static_cast<int*>(g.rmem);
+    std::vector<int> all;
+    all.reserve(nints);
+    all.insert(all.end(), tile_pre.begin(), tile_pre.end());
+    all.insert(all.end(), row_pre.begin(), row_pre.end());
+    all.insert(all.end(), tiles_x.begin(), tiles_x.end());
+    all.insert(all.end(), part_off.begin(), part_off.end());
+    A_CUDA(cudaMemcpy(ti, all.data(), nints * sizeof(int), cudaMemcpyHostToDevice));
+    P.tile_pre = ti;
+    P.row_pre = ti + tile_pre.size();
+    P.tiles_x = P.row_pre + row_pre.size();
+    P.part_off = P.tiles_x + tiles_x.size();
+    char* rest = static_cast<char*>(g.rmem) + ibytes;
+    P.ctr = reinterpret_cast<unsigned*>(rest);
+    P.head = P.ctr + ctrs;
+    P.abort_flag = reinterpret_cast<int*>(P.head + 1);
+    A_CUDA(cudaMemset(rest, 0, size_t(ctrs) * sizeof(unsigned) + 256));
+    P.args = g.d_aargs;
+    P.mem = g.d_mem;
+    // the partial-sum tables of the reduction
+    std::vector<RRed> red(n);
+    for (int s = 0; s < n; ++s) red[s] = RRed{g.m[s]->part, part_run[s], g.m[s]->part2, g.m[s]->red};
+    A_CUDA(cudaMemcpy(g.d_red, red.data(), sizeof(RRed) * n, cudaMemcpyHostToDevice));
+    return LSH_OK;
+}
+
+// The group's queues and tables (pointers that live as long as the members).
+int build_group(AdjGroup& g) {
+    const int n = (int)g.m.size();
+    std::vector<int> nx(n), ny(n);
+    std::vector<KArgs> ka(size_t(10) * n);
+    for (int s = 0; s < n; ++s) {
+        lsh_adjoint* A = g.m[s];
+        nx[s] = A->p.nx;
+        ny[s] = A->p.ny;
+        double* const* X = A->X;
+        double* Y7[7];
+        for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+        Y7[6] = A->X[6];
+        // the forward step: stage 1 (X -> Y, or X -> X), stage 2 (Y -> X, averaged with X)
+        const KArgs a1 = (g.order == 1) ? fwd_args(A, X, X, nullptr, A->acc1, nullptr, nullptr)
+                                        : fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+        ka[s] = a1;
+        ka[n + s] = (g.order == 1) ? a1 : fwd_args(A, Y7, X, X, A->acc2, A->s2x, A->s2y);
+        // the recomputation: per stage the plain arguments (with the branch
+        // tape), then the three snapshot-taking edge passes
+        KArgs r1 = (g.order == 1) ? fwd_args(A, X, nullptr, nullptr, A->acc1, nullptr, nullptr)
+                                  : fwd_args(A, X, A->Y, nullptr, A->acc1, A->s1x, A->s1y);
+        r1.tape = A->tape1;
+        KArgs r2 = r1;
+        if (g.order == 2) {
+            r2 = fwd_args(A, Y7, nullptr, nullptr, A->acc2, A->s2x, A->s2y);
+            r2.tape = A->tape2;
+        }
+        for (int st = 0; st < 2; ++st) {
+            const KArgs& base = st ? r2 : r1;
+            double* const (*snaps)[2] = st ? A->snap2 : A->snap1;
+            ka[size_t(2 + 4 * st) * n + s] = base;
+            for (int k = 0; k < 3; ++k) {
+                KArgs v = base;
+                v.snap[0] = snaps[k][0];
+                v.snap[1] = snaps[k][1];
+                ka[size_t(2 + 4 * st + 1 + k) * n + s] = v;
+            }
+        }
+        g.max_ng = std::max(g.max_ng, A->ng);
+        g.proj_blocks = std::max(g.proj_blocks, (unsigned)A->grid);
+    }
+    A_CUDA(cudaMalloc(&g.d_kargs, sizeof(KArgs) * ka.size()));
+    A_CUDA(cudaMemcpy(g.d_kargs, ka.data(), sizeof(KArgs) * ka.size(), cudaMemcpyHostToDevice));
+    // tables
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+    const size_t o_a = carve(sizeof(AdjArgs) * 2 * kRVars * n), o_m = carve(sizeof(RMember) * n),
+                 o_f = carve(sizeof(FMember) * n), o_mis = carve(sizeof(RMis) * 2 * n), o_r = carve(sizeof(RRed) * n);
+    A_CUDA(cudaMalloc(&g.tables, off));
+    char* tb = static_cast<char*>(g.tables);
+    g.d_aargs = reinterpret_cast<AdjArgs*>(tb + o_a);
+    g.d_mem = reinterpret_cast<RMember*>(tb + o_m);
+    g.d_fmem = reinterpret_cast<FMember*>(tb + o_f);
+    g.d_mis = reinterpret_cast<RMis*>(tb + o_mis);
+    g.d_red = reinterpret_cast<RRed*>(tb + o_r);
+    // the forward step's queue
+    std::vector<QPassSpec> fp, rp;
+    const int stages = (g.order == 2) ? 2 : 1;
+    for (int st = 0; st < stages; ++st) {
+        if (g.order == 2) fp.push_back({kOpRecon, kBCell, st});
+        fp.push_back({kOpH0, kBH0, st});
+        fp.push_back({kOpH1, kBH1, st});
+        fp.push_back({kOpV0, kBV0, st});
+        fp.push_back({kOpV1, kBV1, st});
+        fp.push_back({(g.order == 1) ? kOpVol0 : (st == 0 ? kOpVol1 : kOpVol2), kBCell, st});
+    }
+    if (int st = build_queue_plan(nx, ny, fp, g.d_kargs, &g.qmem_fwd, g.fwd, g.nctr_fwd)) return st;
+    // the recomputation's queue (variables 0..7 of its table)
+    for (int st = 0; st < stages; ++st) {
+        const int v = 4 * st;
+        if (g.order == 2) rp.push_back({kOpReconTape, kBCell, v});
+        rp.push_back({kOpH0, kBH0, v});
+        rp.push_back({kOpH1, kBH1, v + 1});
+        rp.push_back({kOpV0, kBV0, v + 2});
+        rp.push_back({kOpV1, kBV1, v + 3});
+        if (g.order == 2 && st == 0) rp.push_back({kOpVol1, kBCell, v});
+    }
+    if (int st = build_queue_plan(nx, ny, rp, g.d_kargs + 2 * n, &g.qmem_rec, g.rec, g.nctr_rec)) return st;
+    return build_rplan(g);
+}
+
+// The per-run tables: the records' pointers (after fwd_alloc) and, at the
+// start of a reverse sweep, the adjoint arguments of both parities and the
+// misfit terms.
+int group_tables(AdjGroup& g, bool sweep) {
+    const int n = (int)g.m.size();
+    std::vector<RMember> mem(n);
+    std::vector<FMember> fm(n);
+    for (int s = 0; s < n; ++s) {
+        lsh_adjoint* A = g.m[s];
+        mem[s] = RMember{A->rmax, A->argmax, A->rsel, A->red, A->d_dts, A->part, A->tm};
+        fm[s] = FMember{A->tm, A->d_dts, A->X[0], A->X[3], A->X[6], A->d_gauges, A->ng, A->d_eta};
+    }
+    A_CUDA(cudaMemcpy(g.d_mem, mem.data(), sizeof(RMember) * n, cudaMemcpyHostToDevice));
+    A_CUDA(cudaMemcpy(g.d_fmem, fm.data(), sizeof(FMember) * n, cudaMemcpyHostToDevice));
+    if (!sweep) return LSH_OK;
+    std::vector<AdjArgs> aa(size_t(2) * kRVars * n);
+    std::vector<RMis> mis(size_t(2) * n);
+    for (int par = 0; par < 2; ++par) {
+        for (int s = 0; s < n; ++s) {
+            lsh_adjoint* A = g.m[s];
+            double* Xb[6], *Xbn[6];
+            for (int k = 0; k < 6; ++k) {
+                Xb[k] = par ? A->Xbn[k] : A->Xb[k];
+                Xbn[k] = par ? A->Xb[k] : A->Xbn[k];
+            }
+            double* Y7[7];
+            for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
+            Y7[6] = A->X[6];
+            AdjArgs st[2];
+            // stage 1 (order 1: the step) and stage 2
+            if (g.order == 1) {
+                st[0] = adj_args(A, A->X, nullptr, nullptr, A->acc1, Xbn, Xb, nullptr, nullptr, 0.0);
+                st[1] = st[0];
+            } else {
+                st[0] = adj_args(A, A->X, A->s1x, A->s1y, A->acc1, Xbn, A->Yb, nullptr, A->tape1, 0.0);
+                st[1] = adj_args(A, Y7, A->s2x, A->s2y, A->acc2, A->Yb, Xb, Xbn, A->tape2, 0.0);
+            }
+            for (int h = 0; h < 2; ++h) {
+                double* const (*snaps)[2] = h ? A->snap2 : A->snap1;
+                // variables: base, then the edge passes v1, v0, h1 (snapshots 2, 1, 0), h0 (none)
+                for (int v = 0; v < 5; ++v) {
+                    AdjArgs x = st[h];
+                    x.snap[0] = x.snap[1] = nullptr;
+                    if (v >= 1 && v <= 3) { x.snap[0] = snaps[3 - v][0]; x.snap[1] = snaps[3 - v][1]; }
+                    aa[(size_t(par) * kRVars + 5 * h + v) * n + s] = x;
+                }
+            }
+            RMis r{};
+            for (int k = 0; k < 6; ++k) r.b[k] = Xb[k];
+            r.h1 = A->X[0];
+            r.h2 = A->X[3];
+            r.gauges = A->d_gauges;
+            r.ng = (A->have_target && A->ng > 0 && A->misfit_weight != 0.0) ? A->ng : 0;
+            r.eta = A->d_eta;
+            r.tgt = A->d_tgt;
+            r.w = A->misfit_weight;
+            r.h_adj = A->h_adj;
+            r.N = (long long)A->N;
+            mis[size_t(par) * n + s] = r;
+        }
+    }
+    A_CUDA(cudaMemcpy(g.d_aargs, aa.data(), sizeof(AdjArgs) * aa.size(), cudaMemcpyHostToDevice));
+    A_CUDA(cudaMemcpy(g.d_mis, mis.data(), sizeof(RMis) * mis.size(), cudaMemcpyHostToDevice));
+    g.parity = 0;
+    return LSH_OK;
+}
+
+#ifndef LSH_ADJB_FWD_CTAS
+#define LSH_ADJB_FWD_CTAS 20  // forward queue CTAs per SM (at most kBMaxCtas)
+#endif
+#ifndef LSH_ADJB_FWD_FETCH
+#define LSH_ADJB_FWD_FETCH 2
+#endif
+constexpr int kAdjbFwdCtas = LSH_ADJB_FWD_CTAS;
+constexpr int kAdjbFwdFetch = LSH_ADJB_FWD_FETCH;
+
+// Forward step n -> n + 1 of every member (RECORD: with its dt and gauge records).
+void group_forward(AdjGroup& g, int sms, int n, bool record, cudaStream_t s) {
+    const int nm = (int)g.m.size();
+    if (!record) k_adjb_pre<<<(nm + 127) / 128, 128, 0, s>>>(g.d_mem, nm, n);
+    const int grid = sms * kAdjbFwdCtas;
+    if (g.order == 1) k_batch_step<1><<<grid, kBThreads, 0, s>>>(g.fwd, kAdjbFwdFetch);
+    else k_batch_step<2><<<grid, kBThreads, 0, s>>>(g.fwd, kAdjbFwdFetch);
+    const int adv = std::max(1, std::min((std::max(g.nctr_fwd, nm) + 255) / 256, 2 * sms));
+    k_batch_advance<<<adv, 256, 0, s>>>(g.d_kargs, nm, g.fwd.ctr, g.nctr_fwd, g.fwd.head);
+    if (record) k_adjb_record<<<nm, 128, 0, s>>>(g.d_fmem, n);
+}
+
+// The adjoint of step n for every member (Ops::reverse_step, batched).
+void group_reverse(AdjGroup& g, int sms, int n, cudaStream_t s) {
+    const int nm = (int)g.m.size();
+    k_adjb_pre<<<(nm + 127) / 128, 128, 0, s>>>(g.d_mem, nm, n);
+    const int grid = sms * kAdjbFwdCtas;
+    if (g.order == 1) k_batch_step<1, ReconTape><<<grid, kBThreads, 0, s>>>(g.rec, kAdjbFwdFetch);
+    else k_batch_step<2, ReconTape><<<grid, kBThreads, 0, s>>>(g.rec, kAdjbFwdFetch);
+    const int rgrid = sms * LSH_ADJB_MINB;
+    if (g.order == 1) k_adjb_reverse<1><<<rgrid, kRThreads, 0, s>>>(g.rev, g.parity, n);
+    else k_adjb_reverse<2><<<rgrid, kRThreads, 0, s>>>(g.rev, g.parity, n);
+    const int rst = std::max(1, std::min((std::max(g.nctr_rec, g.nctr_rev) + 255) / 256, 2 * sms));
+    k_adjb_reset<<<rst, 256, 0, s>>>(g.rec.ctr, g.nctr_rec, g.rec.head, g.rev.ctr, g.nctr_rev, g.rev.head);
+    k_adjb_reduce_rows<<<dim3(kReduceRows, nm), 32 * kRed, 0, s>>>(g.d_red);
+    k_adjb_reduce<<<nm, 32 * kRed, 0, s>>>(g.d_red);
+    // the new adjoint is in Xbn: swap, as Ops::reverse_step does
+    for (lsh_adjoint* A : g.m) {
+        for (int k = 0; k < 6; ++k) std::swap(A->Xb[k], A->Xbn[k]);
+        A->stats.reversed_steps += 1;
+    }
+    g.parity ^= 1;
+    if (n >= 1) {
+        if (g.max_ng > 0) k_adjb_gauges<<<dim3((g.max_ng + 127) / 128, nm), 128, 0, s>>>(g.d_mis + (size_t)g.parity * nm, n);
+        k_adjb_project<<<dim3(g.proj_blocks, nm), kCellBlock, 0, s>>>(g.d_mis + (size_t)g.parity * nm);
+    }
+}
 
 }  // namespace
 
 struct lsh_adjoint_batch {
     std::vector<lsh_adjoint*> m;
+    std::vector<AdjGroup> groups;  // the members by order
+    cudaStream_t stream = nullptr; // every member's stream
+    int sms = 152;
     double budget = -1.0;  // < 0: 180 GB, capped by free memory at the forward run
     int nsteps = 0;
     int n_slots = 0;
     bool have_forward = false;
     lsh_adjoint_stats stats{};
 };
+
+namespace {
+
+// The schedule's operations for the whole batch: one schedule, one slot
+// count, every member's state at the same step; each operation one set of
+// launches per group.
+struct BatchOps : lsh::RevolveOps {
+    lsh_adjoint_batch* B;
+    explicit BatchOps(lsh_adjoint_batch* b) : B(b) {}
+    int advance(int from, int to) override {
+        for (int n = from; n < to; ++n)
+            for (AdjGroup& g : B->groups) {
+                group_forward(g, B->sms, n, false, B->stream);
+                for (lsh_adjoint* A : g.m) A->stats.recompute_steps += 1;
+            }
+        A_CUDA(cudaGetLastError());
+        return 0;
+    }
+    int store(int k) override {
+        for (lsh_adjoint* A : B->m)
+            if (int st = Ops(A).store(k)) return st;
+        return 0;
+    }
+    int restore(int k, int step) override {
+        for (lsh_adjoint* A : B->m)
+            if (int st = Ops(A).restore(k, step)) return st;
+        return 0;
+    }
+    int reverse_step(int n) override {
+        for (AdjGroup& g : B->groups) group_reverse(g, B->sms, n, B->stream);
+        A_CUDA(cudaGetLastError());
+        return 0;
+    }
+};
+
+}  // namespace
 
 // ------------------------------------------------------------------ C ABI
 
@@ -1001,7 +1738,7 @@ static void destroy_adjoint(lsh_adjoint* A) {
     cudaFree(A->tm); cudaFree(A->rmax); cudaFree(A->argmax); cudaFree(A->rsel); cudaFree(A->part); cudaFree(A->part2); cudaFree(A->red);
     cudaFree(A->d_gauges); cudaFree(A->d_eta); cudaFree(A->d_tgt); cudaFree(A->d_dts);
     cudaFree(A->slots);
-    if (A->stream) cudaStreamDestroy(A->stream);
+    if (A->stream && A->own_stream) cudaStreamDestroy(A->stream);
     (void)cudaGetLastError();
     delete A;
 }
@@ -1180,13 +1917,42 @@ int lsh_adjoint_batch_create(int n, const lsh_params* params, const int* n_gauge
         A->budget = 0.0;  // until the batch's forward run sets the slot count
         B->m.push_back(A);
     }
+    // one stream for all members, so that their own operations (uploads,
+    // checkpoint copies) and the batch's launches stay in order
+    B->sms = B->m[0]->sms;
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { const int st = afail(e, "cudaStreamCreate"); lsh_adjoint_batch_destroy(B); return st; }
+    }
+    for (lsh_adjoint* A : B->m) {
+        cudaStreamSynchronize(A->stream);
+        cudaStreamDestroy(A->stream);
+        A->stream = B->stream;
+        A->own_stream = false;
+    }
+    for (int order = 1; order <= 2; ++order) {
+        AdjGroup g;
+        g.order = order;
+        for (lsh_adjoint* A : B->m)
+            if (A->order == order) g.m.push_back(A);
+        if (g.m.empty()) continue;
+        B->groups.push_back(g);
+        if (int st = build_group(B->groups.back())) {
+            lsh_adjoint_batch_destroy(B);
+            return st;
+        }
+    }
     *out = B;
     return LSH_OK;
 }
 
 int lsh_adjoint_batch_destroy(lsh_adjoint_batch* B) {
     if (!B) return LSH_OK;
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    for (AdjGroup& g : B->groups) free_group(g);
     for (lsh_adjoint* A : B->m) destroy_adjoint(A);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    (void)cudaGetLastError();
     delete B;
     return LSH_OK;
 }
@@ -1235,15 +2001,19 @@ int lsh_adjoint_batch_forward(lsh_adjoint_batch* B, const double* const* host_st
     B->n_slots = want;
     // a member run on its own keeps the batch's slot count
     for (lsh_adjoint* A : B->m) A->budget = want * slot_bytes_of(A);
+    for (AdjGroup& g : B->groups)
+        if (int st = group_tables(g, false)) return st;
     for (int i = 0; i < n; ++i)
         if (int st = fwd_begin(B->m[i], host_states + (size_t)i * LSH_NVARS, targets ? targets[i] : nullptr)) return st;
-    BatchOps ops;
-    for (lsh_adjoint* A : B->m) ops.ops.emplace_back(A);
+    BatchOps ops(B);
     int a = 0, slot = 0;
     auto run = [&](int to) -> int {
         for (int s = a; s < to; ++s)
-            for (lsh_adjoint* A : B->m)
-                if (int st = fwd_record_step(A, s)) return st;
+            for (AdjGroup& g : B->groups) {
+                group_forward(g, B->sms, s, true, B->stream);
+                for (lsh_adjoint* A : g.m) A->stats.forward_steps += 1;
+            }
+        A_CUDA(cudaGetLastError());
         return 0;
     };
     const std::vector<int> spine = spine_steps(nsteps, want);
@@ -1287,11 +2057,12 @@ int lsh_adjoint_batch_gradient(lsh_adjoint_batch* B, const double* misfit_weight
         }
     const auto t0 = std::chrono::steady_clock::now();
     const bool pre = A0->spine_stored;
-    BatchOps ops;
-    for (lsh_adjoint* A : B->m) ops.ops.emplace_back(A);
+    BatchOps ops(B);
     ops.cur = A0->cur_step;
     for (int i = 0; i < n; ++i)
         if (int st = grad_begin(B->m[i], misfit_weights ? misfit_weights[i] : 1.0, nullptr)) return st;
+    for (AdjGroup& g : B->groups)
+        if (int st = group_tables(g, true)) return st;
     if (int st = lsh::revolve_reverse(ops, 0, B->nsteps, 0, B->n_slots - 1, pre)) return st;
     for (lsh_adjoint* A : B->m) if (int st = grad_tail(A, ops.cur)) return st;
     for (int i = 0; i < n; ++i) {

@@ -30,6 +30,7 @@
 
 #include "../../include/lsh.h"
 #include "lsh_passes.cuh"
+#include "lsh_queue.cuh"
 #include "lsh_setup.h"
 
 using lsh::KArgs;
@@ -40,235 +41,6 @@ using lsh::kRateInitBits;
 namespace {
 
 constexpr int kBatchGraphSteps = 8;
-constexpr int kBThreads = 64;    // threads per persistent CTA
-constexpr int kBMaxCtas = 20;    // CTAs per SM the step kernel is compiled for (48 registers)
-constexpr int kMaxPasses = 12;
-
-// Tilings of a scenario's passes, 64-thread tiles of the single-grid shapes:
-// horizontal edges of parity 0 / 1 (16 columns x 4 edge lines), vertical
-// edges of parity 0 / 1 (8 edge columns x 8 rows), cells (16 x 4).
-enum BKind : int { kBH0 = 0, kBH1 = 1, kBV0 = 2, kBV1 = 3, kBCell = 4, kBKinds = 5 };
-constexpr int kTileHX = 16, kTileHY = 4, kTileVX = 8, kTileVY = 8, kTileCX = 16, kTileCY = 4;
-// What a pass does.
-enum BOp : int { kOpH0 = 0, kOpH1 = 1, kOpV0 = 2, kOpV1 = 3, kOpRecon = 4, kOpVol0 = 5, kOpVol1 = 6, kOpVol2 = 7 };
-
-struct BPass {
-    int op;        // BOp
-    int kind;      // BKind of its tiles
-    int stage;     // arguments: args[s] (stage 1) or args[n + s] (stage 2)
-    int prod;      // the pass whose writes it reads (-1: the step's first pass)
-    int item_off;  // first item of the pass in the step's queue
-    int ctr_off;   // first counter of the pass
-};
-
-// Everything the step kernel needs, passed by value.
-struct BPlan {
-    int n;                  // scenarios
-    int npass;
-    int total_items;
-    BPass pass[kMaxPasses];
-    const int* tile_pre;    // [kind][n + 1]: first tile of each scenario (prefix sums)
-    const int* row_pre;     // [kind][n + 1]: first tile row of each scenario
-    const int* tiles_x;     // [kind][n]: tiles per tile row
-    const KArgs* args;      // [n] stage 1, [n, 2n) stage 2 (second order)
-    unsigned* ctr;          // completion counters: per pass, per scenario tile row
-    unsigned* head;         // the step's queue head
-    int* abort_flag;        // set when a wait gives up; later waits give up at once
-};
-
-// Cell rows an item of `op` reads (tile row ty of a scenario with ny rows).
-__device__ __forceinline__ void item_rows(int op, int ty, int ny, int& r0, int& r1) {
-    if (op == kOpH0 || op == kOpH1) {
-        const int y0 = op + 2 * kTileHY * ty;  // first edge row (parity op)
-        r0 = y0 - 1; r1 = y0 + 2 * (kTileHY - 1);
-    } else if (op == kOpV0 || op == kOpV1) {
-        r0 = kTileVY * ty; r1 = r0 + kTileVY - 1;
-    } else if (op == kOpRecon) {
-        r0 = kTileCY * ty - 1; r1 = kTileCY * ty + kTileCY;
-    } else {
-        r0 = kTileCY * ty; r1 = r0 + kTileCY - 1;
-    }
-    r0 = max(r0, 0);
-    r1 = min(r1, ny - 1);
-}
-
-// Tile rows of a pass of `kind` that write cell rows [r0, r1].
-__device__ __forceinline__ void producer_rows(int kind, int r0, int r1, int& t0, int& t1) {
-    if (kind == kBV0 || kind == kBV1) { t0 = r0 / kTileVY; t1 = r1 / kTileVY; }
-    else if (kind == kBCell) { t0 = r0 / kTileCY; t1 = r1 / kTileCY; }
-    else {
-        // horizontal edge row y = p + 2 t writes cell rows y - 1 and y
-        const int p = kind;
-        t0 = (max(r0 - p + 1, 0) / 2) / kTileHY;
-        t1 = (max(r1 + 1 - p, 0) / 2) / kTileHY;
-    }
-}
-
-// One item's work: the single-grid kernels' per-thread bodies on one tile.
-template <int ORDER, int OP>
-__device__ __forceinline__ void item_work(const KArgs& a, int tx, int ty, double dt) {
-    const int nx = a.c.nx, ny = a.c.ny, tid = threadIdx.x;
-    if (OP == kOpH0 || OP == kOpH1) {
-        const int par = OP;
-        const int x = tx * kTileHX + tid % kTileHX, line = ty * kTileHY + tid / kTileHX;
-        if (x < nx && line < (ny - par) / 2 + 1) lsh::do_edge<0, OP == kOpH0, ORDER>(a, x, par + 2 * line, dt);
-    } else if (OP == kOpV0 || OP == kOpV1) {
-        const int par = OP - kOpV0;
-        const int x = par + 2 * (tx * kTileVX + tid % kTileVX), y = ty * kTileVY + tid / kTileVX;
-        if (x <= nx && y < ny) lsh::do_edge<1, false, ORDER>(a, x, y, dt);
-    } else {
-        const int i = tx * kTileCX + tid % kTileCX, j = ty * kTileCY + tid / kTileCX;
-        const bool in = (i < nx && j < ny);
-        if (OP == kOpRecon) {
-            if (in) lsh::recon_cell(a, j * nx + i);
-        } else {
-            constexpr int MODE = OP - kOpVol0;
-            unsigned long long bits = kRateInitBits;
-            if (in) bits = lsh::volume_cell<MODE>(a, j * nx + i, dt);
-            if (MODE != 2) lsh::block_max_bits<kBThreads>(bits, &a.tm->rmax_bits);
-        }
-    }
-}
-
-// The whole step of every scenario.  Items are dequeued in pass order, and an
-// item waits only for items of earlier passes, which running CTAs took
-// before it: the earliest unfinished item always has its inputs, so the
-// queue drains whatever the number of resident CTAs.  Waits are bounded
-// (~2 s of %globaltimer); one that runs out sets LSH_ERR_TIMEOUT on its
-// scenario and the batch's abort flag, and later waits give up at once.
-template <int ORDER>
-__global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, int fetch) {
-    __shared__ __align__(16) unsigned long long sargs[(sizeof(KArgs) + 7) / 8];
-    __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy;
-    // the last decoded (pass, scenario): its items [s_lo, s_hi) of the queue,
-    // and the arguments held in sargs (stage * n + scenario, -1: none).
-    // Consecutive items of the queue share them, so most items skip the
-    // scenario search and the argument copy.
-    __shared__ int s_lo, s_hi, s_args_key;
-    const KArgs& a = *reinterpret_cast<const KArgs*>(sargs);
-    const int tid = threadIdx.x;
-    if (tid == 0) { s_lo = 0; s_hi = 0; s_args_key = -1; }
-    for (;;) {
-        if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)fetch);
-        __syncthreads();
-        const int first = s_first;
-        if (first >= P.total_items) break;
-        const int last = min(first + fetch, P.total_items);
-        for (int it = first; it < last; ++it) {
-            if (tid == 0) {
-                if (it < s_lo || it >= s_hi) {
-                    int p = 0;
-                    while (p + 1 < P.npass && it >= P.pass[p + 1].item_off) ++p;
-                    const int kind = P.pass[p].kind;
-                    const int* tp = P.tile_pre + kind * (P.n + 1);
-                    const int l = it - P.pass[p].item_off;
-                    int lo = 0, hi = P.n - 1;  // the scenario: the last one whose first tile is <= l
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (tp[mid] <= l) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    s_pass = p;
-                    s_scen = lo;
-                    s_lo = P.pass[p].item_off + tp[lo];
-                    s_hi = P.pass[p].item_off + tp[lo + 1];
-                    s_ntx = P.tiles_x[kind * P.n + lo];
-                }
-                s_tile = it - s_lo;
-                const int key = P.pass[s_pass].stage * P.n + s_scen;
-                s_copy = (key != s_args_key);
-                s_args_key = key;
-            }
-            __syncthreads();
-            const int p = s_pass, s = s_scen, t = s_tile, ntx = s_ntx;
-            const BPass ps = P.pass[p];
-            if (s_copy) {
-                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(P.args + ps.stage * P.n + s);
-                for (int k = tid; k < (int)((sizeof(KArgs) + 7) / 8); k += kBThreads) sargs[k] = src[k];
-                __syncthreads();
-            }
-            const int ty = t / ntx, tx = t - ty * ntx;
-            const bool live = !a.tm->done;  // uniform: the clock changes between steps only
-            if (live && ps.prod >= 0 && tid == 0) {
-                const BPass pp = P.pass[ps.prod];
-                int r0, r1, t0, t1;
-                item_rows(ps.op, ty, a.c.ny, r0, r1);
-                producer_rows(pp.kind, r0, r1, t0, t1);
-                const int rbase = P.row_pre[pp.kind * (P.n + 1) + s];
-                const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
-                t0 = max(t0, 0);
-                t1 = min(t1, nrows - 1);
-                const unsigned target = (unsigned)P.tiles_x[pp.kind * P.n + s];
-                const unsigned* c = P.ctr + pp.ctr_off + rbase;
-                volatile int* abort_flag = P.abort_flag;
-                unsigned long long start = 0;
-                bool gave_up = false;
-                for (int r = t0; r <= t1 && !gave_up; ++r) {
-                    unsigned ns = 32;
-                    for (;;) {
-                        unsigned v;
-                        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(c + r) : "memory");
-                        if (v >= target) break;
-                        if (*abort_flag) { gave_up = true; break; }
-                        unsigned long long now;
-                        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-                        if (start == 0) start = now;
-                        else if (now - start > 2000000000ull) { atomicExch(P.abort_flag, 1); gave_up = true; break; }
-                        __nanosleep(ns);
-                        if (ns < 1024) ns *= 2;
-                    }
-                }
-                if (gave_up) atomicOr(&a.tm->err, 1 << LSH_ERR_TIMEOUT);
-            }
-            __syncthreads();
-            if (live) {
-                const double dt = a.tm->dt;
-                switch (ps.op) {
-                    case kOpH0: item_work<ORDER, kOpH0>(a, tx, ty, dt); break;
-                    case kOpH1: item_work<ORDER, kOpH1>(a, tx, ty, dt); break;
-                    case kOpV0: item_work<ORDER, kOpV0>(a, tx, ty, dt); break;
-                    case kOpV1: item_work<ORDER, kOpV1>(a, tx, ty, dt); break;
-                    default:
-                        if constexpr (ORDER == 1) {
-                            item_work<ORDER, kOpVol0>(a, tx, ty, dt);
-                        } else {
-                            if (ps.op == kOpRecon) item_work<ORDER, kOpRecon>(a, tx, ty, dt);
-                            else if (ps.op == kOpVol1) item_work<ORDER, kOpVol1>(a, tx, ty, dt);
-                            else item_work<ORDER, kOpVol2>(a, tx, ty, dt);
-                        }
-                        break;
-                }
-            }
-            __syncthreads();  // the tile's writes are done, and sargs may be refilled
-            if (tid == 0) {
-                // release: the barrier above orders the tile's writes before it
-                unsigned* c = P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty;
-                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(c) : "memory");
-            }
-        }
-    }
-}
-
-// Every scenario's clock (k_advance of the single-grid path); the queue head
-// and the completion counters back to zero for the next step.
-__global__ void k_batch_advance(const KArgs* __restrict__ args, int n, unsigned* ctr, int n_ctr, unsigned* head) {
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-    if (gid == 0) *head = 0u;
-    for (int i = gid; i < n_ctr; i += stride) ctr[i] = 0u;
-    for (int s = gid; s < n; s += stride) {
-        lsh::TimeRec* tm = args[s].tm;
-        if (tm->done) continue;
-        tm->t += tm->dt;
-        tm->steps += 1;
-        const double nd = lsh::dt_of(tm->rmax_bits, 2.0 * args[s].c.cfl);
-        tm->dt = nd;
-        tm->rmax_bits = kRateInitBits;
-        if (tm->t >= tm->t_end) tm->done = 1;
-        if (tm->dt_min > 0.0 && nd < tm->dt_min) { tm->err |= 1 << LSH_ERR_STALL; tm->done = 1; }
-        if (tm->err) tm->done = 1;
-    }
-}
-
 // Initial dt of one scenario (set_state): wave pass, rate max, dt.
 template <int DIR, bool FIRST>
 __global__ void __launch_bounds__(kEdgeBlock) k_batch_init_wave(const KArgs* args, int s, int par) {
@@ -346,45 +118,12 @@ namespace {
 
 constexpr int kernels_per_step = 2;  // the step kernel and the clock kernel
 
-// Tiles of scenario `p` in each tiling: (tiles per row, tile rows).
-void scenario_tiles(const lsh_params& p, int kind, int& tx, int& ty) {
-    const int nx = p.nx, ny = p.ny;
-    if (kind == kBH0 || kind == kBH1) {
-        tx = (nx + kTileHX - 1) / kTileHX;
-        ty = ((ny - kind) / 2 + 1 + kTileHY - 1) / kTileHY;
-    } else if (kind == kBV0 || kind == kBV1) {
-        tx = ((nx - (kind - kBV0)) / 2 + 1 + kTileVX - 1) / kTileVX;
-        ty = (ny + kTileVY - 1) / kTileVY;
-    } else {
-        tx = (nx + kTileCX - 1) / kTileCX;
-        ty = (ny + kTileCY - 1) / kTileCY;
-    }
-}
-
-// The step's passes, their items and counters, and the device tables.
+// The step's passes: reconstruction (second order), the four colour edge
+// passes and the Euler stage, per stage.
 int build_plan(lsh_batch* b) {
-    const int n = b->n;
-    std::vector<int> tile_pre(size_t(kBKinds) * (n + 1)), row_pre(size_t(kBKinds) * (n + 1)), tiles_x(size_t(kBKinds) * n);
-    long long kind_tiles[kBKinds], kind_rows[kBKinds];
-    for (int k = 0; k < kBKinds; ++k) {
-        long long tsum = 0, rsum = 0;
-        for (int s = 0; s < n; ++s) {
-            int tx, ty;
-            scenario_tiles(b->params[s], k, tx, ty);
-            tile_pre[k * (n + 1) + s] = (int)tsum;
-            row_pre[k * (n + 1) + s] = (int)rsum;
-            tiles_x[k * n + s] = tx;
-            tsum += (long long)tx * ty;
-            rsum += ty;
-        }
-        tile_pre[k * (n + 1) + n] = (int)tsum;
-        row_pre[k * (n + 1) + n] = (int)rsum;
-        kind_tiles[k] = tsum;
-        kind_rows[k] = rsum;
-    }
-    // the passes of a step, each reading what the one before it wrote
-    struct P { int op, kind, stage; };
-    std::vector<P> passes;
+    std::vector<int> nx(b->n), ny(b->n);
+    for (int s = 0; s < b->n; ++s) { nx[s] = b->params[s].nx; ny[s] = b->params[s].ny; }
+    std::vector<QPassSpec> passes;
     const int stages = (b->order == 2) ? 2 : 1;
     for (int st = 0; st < stages; ++st) {
         if (b->order == 2) passes.push_back({kOpRecon, kBCell, st});
@@ -394,48 +133,7 @@ int build_plan(lsh_batch* b) {
         passes.push_back({kOpV1, kBV1, st});
         passes.push_back({(b->order == 1) ? kOpVol0 : (st == 0 ? kOpVol1 : kOpVol2), kBCell, st});
     }
-    BPlan& P0 = b->plan;
-    P0 = BPlan{};
-    P0.n = n;
-    P0.npass = (int)passes.size();
-    long long items = 0, ctrs = 0;
-    for (int i = 0; i < P0.npass; ++i) {
-        BPass& q = P0.pass[i];
-        q.op = passes[i].op;
-        q.kind = passes[i].kind;
-        q.stage = passes[i].stage;
-        q.prod = i - 1;
-        q.item_off = (int)items;
-        q.ctr_off = (int)ctrs;
-        items += kind_tiles[q.kind];
-        ctrs += kind_rows[q.kind];
-    }
-    if (items > 0x7fffffffLL - 1024 || ctrs > 0x7fffffffLL) {
-        lsh::set_last_error("batch too large for one step's work queue");
-        return LSH_ERR_INVALID;
-    }
-    P0.total_items = (int)items;
-    b->n_ctr = (int)ctrs;
-    // one allocation: tables, counters, queue head, abort flag
-    const size_t tbytes = (tile_pre.size() + row_pre.size() + tiles_x.size()) * sizeof(int);
-    const size_t bytes = ((tbytes + 255) & ~size_t(255)) + size_t(ctrs) * sizeof(unsigned) + 256;
-    if (b->d_plan_mem) { cudaFree(b->d_plan_mem); b->d_plan_mem = nullptr; }
-    B_CUDA(cudaMalloc(&b->d_plan_mem, bytes));
-    int* ti = static_cast<int*>(b->d_plan_mem);
-    B_CUDA(cudaMemcpy(ti, tile_pre.data(), tile_pre.size() * sizeof(int), cudaMemcpyHostToDevice));
-    B_CUDA(cudaMemcpy(ti + tile_pre.size(), row_pre.data(), row_pre.size() * sizeof(int), cudaMemcpyHostToDevice));
-    B_CUDA(cudaMemcpy(ti + tile_pre.size() + row_pre.size(), tiles_x.data(), tiles_x.size() * sizeof(int),
-                      cudaMemcpyHostToDevice));
-    P0.tile_pre = ti;
-    P0.row_pre = ti + tile_pre.size();
-    P0.tiles_x = ti + tile_pre.size() + row_pre.size();
-    char* rest = static_cast<char*>(b->d_plan_mem) + ((tbytes + 255) & ~size_t(255));
-    P0.ctr = reinterpret_cast<unsigned*>(rest);
-    P0.head = reinterpret_cast<unsigned*>(rest + size_t(ctrs) * sizeof(unsigned));
-    P0.abort_flag = reinterpret_cast<int*>(P0.head + 1);
-    B_CUDA(cudaMemset(rest, 0, size_t(ctrs) * sizeof(unsigned) + 256));
-    P0.args = b->d_args;
-    return LSH_OK;
+    return build_queue_plan(nx, ny, passes, b->d_args, &b->d_plan_mem, b->plan, b->n_ctr);
 }
 
 void enqueue_batch_step(lsh_batch* b, cudaStream_t s) {

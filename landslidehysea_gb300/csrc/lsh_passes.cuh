@@ -64,6 +64,7 @@ struct KArgs {
     // before left them, to snap[0], snap[1] -- the partial sums its limiter
     // reads, which the reverse sweep needs at exactly those cells
     double* snap[2];
+    unsigned* tape;       // the recomputation's reconstruction branch tape (kOpReconTape; null otherwise)
 };
 
 // Depths of a face (first order: the cell's; second order: reconstructed).
