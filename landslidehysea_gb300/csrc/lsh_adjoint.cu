@@ -806,9 +806,22 @@ int fwd_end(lsh_adjoint* A) {
     return 0;
 }
 
+// After the stream has drained: LSH_ERR_TIMEOUT when a pass's bounded wait
+// gave up during the run (the replayed steps keep that bit).
+int check_waits(const lsh_adjoint* A) {
+    lsh::TimeRec tm{};
+    A_CUDA(cudaMemcpy(&tm, A->tm, sizeof(tm), cudaMemcpyDeviceToHost));
+    if (tm.err & (1 << LSH_ERR_TIMEOUT)) {
+        lsh::set_last_error("adjoint: a pass waited for its producer rows past the time limit");
+        return LSH_ERR_TIMEOUT;
+    }
+    return 0;
+}
+
 // Waits for the forward run; the misfit and the gauge series.
 int fwd_host(lsh_adjoint* A, const double* target, double* misfit, double* gauge_series) {
     A_CUDA(cudaStreamSynchronize(A->stream));
+    if (int st = check_waits(A)) return st;
     double J = 0.0;
     if (A->have_target)
         for (size_t i = 0; i < A->h_eta.size(); ++i) { const double d = A->h_eta[i] - target[i]; J = lshm::fmad(d, d, J); }
@@ -875,7 +888,7 @@ int grad_copy(lsh_adjoint* A, double* const grad_state[6]) {
             A_CUDA(cudaMemcpyAsync(grad_state[k], A->Xb[k], A->N * sizeof(double), cudaMemcpyDeviceToHost, s));
     A_CUDA(cudaMemcpyAsync(A->h_red, A->red, sizeof(A->h_red), cudaMemcpyDeviceToHost, s));
     A_CUDA(cudaStreamSynchronize(s));
-    return 0;
+    return check_waits(A);
 }
 
 // d/d(angle1, mf0, mfs, r) from the constant adjoints.
