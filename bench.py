@@ -44,10 +44,11 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FJORD2048_FLOPS_PER_CELL_STEP = 804.0
 
 # Counters of the step kernels on the 2048^2 fjord, read from ncu captures
-# (one step inside the timed range: stage 2 of step 21, stage 1 of step 22):
+# (one step inside the timed range: the first step after the 20 warm-up steps):
 #   ncu --clock-control none --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,\
+#       sm__pipe_fp64_cycles_active.sum,sm__cycles_elapsed.sum,\
 #       dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
-#       -k regex:"k_edges|k_volume|k_recon" -s 282 -c 12 \
+#       -k regex:"k_edges|k_volume|k_recon" -s 240 -c 12 \
 #       python bench.py --steps 2 --warmup 20 --no-cpu-baseline --no-e2e
 # They hold only for the kernel sources and the workload generator they were
 # captured on.  Those files are hashed (COUNTER_SOURCES); when the hash is not
@@ -57,18 +58,18 @@ COUNTER_SOURCES = ("landslidehysea_gb300/csrc/lsh_core.cu", "landslidehysea_gb30
                    "landslidehysea_gb300/csrc/lsh_passes.cuh", "landslidehysea_gb300/csrc/lsh_scheme.cuh",
                    "landslidehysea_gb300/csrc/lsh_fpmath.h", "landslidehysea_gb300/csrc/lsh_setup.h",
                    "landslidehysea_gb300/build.py", "landslidehysea_gb300/scenarios.py")
-COUNTERS_SOURCE_HASH = "34750d247dfe5f92"
-# FP64-pipe thread instructions per cell-update of one step (6.941e8 per step
+COUNTERS_SOURCE_HASH = "7a596f1664993d16"
+# FP64-pipe thread instructions per cell-update of one step (6.060e8 per step
 # / 4,194,304 cells).  The FP64 pipe takes one such instruction per lane as
 # the measured peak's DFMA does, so the peak instruction rate is the measured
 # FP64 FLOP/s / 2.
-FJORD2048_FP64_INSTR_PER_CELL_STEP = 165.49
+FJORD2048_FP64_INSTR_PER_CELL_STEP = 144.49
 # DRAM bytes (read + write) per launch of each step kernel; edge_h0 is the
 # first (accumulator-writing) horizontal pass.  A second-order step launches
 # recon and the four edge passes twice, each volume kernel once.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
-    "recon": 141.05e6, "edge_h0": 373.6e6, "edge_h1": 198.1e6, "edge_v0": 193.85e6, "edge_v1": 190.1e6,
-    "volume1": 673.7e6, "volume2": 714.9e6,
+    "recon": 139.5e6, "edge_h0": 356.85e6, "edge_h1": 170.85e6, "edge_v0": 171.05e6, "edge_v1": 167.4e6,
+    "volume1": 651.6e6, "volume2": 699.1e6,
 }
 # Algorithmic HBM bytes per cell-step (FP64 state with perfect reuse): first
 # order 13 x 8 = 104 B (read 6 state + H, write 6 state); TVD-RK2 104 B for

@@ -31,7 +31,8 @@ def test_cbrt(oracle, xs):
     x = np.concatenate([np.exp(xs.uniform(np.log(1e-300), np.log(1e300), 200000)), xs.uniform(0, 10, 100000),
                         [1.0, 8.0, 27.0, 1e-310, 4.9e-324]])
     y = oracle.fpmath("cbrt", x)
-    assert np.max(ulp_err(y[:-2], np.cbrt(x[:-2]))) <= 8
+    # FP32 first guess plus two FP64 Newton steps: at most 3 ulp from numpy's cube root
+    assert np.max(ulp_err(y[:-2], np.cbrt(x[:-2]))) <= 3
     assert np.allclose(y[-2:], np.cbrt(x[-2:]), rtol=1e-12, atol=0)
     assert oracle.fpmath("cbrt", np.array([0.0]))[0] == 0.0
 
