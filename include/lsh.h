@@ -205,6 +205,16 @@ int lsh_step_noalloc(const lsh_params* p, double* const dev_state[LSH_NVARS], in
 int lsh_profile_step(lsh_ctx* ctx, float* ms_out, int cap, int* n_kernels);
 int lsh_probe_fp64_peak(int device, double* gflops);
 
+/* Diagnostic: the bounded waits between passes give up instead of hanging.
+ * One block runs the overlapped step's wait and the work queue's wait on
+ * completion counters that nothing increments; each gives up after its bound
+ * (about 2 s of device time) and records it.  *status_out = LSH_ERR_TIMEOUT
+ * when both waits gave up and reported (the expected outcome), LSH_OK when
+ * either did not; *ms_out (may be null) gets the kernel's duration.  The
+ * device is used again afterwards, and the call returns LSH_OK if it
+ * answers.  Takes about 4 s.  No reference counterpart. */
+int lsh_probe_wait_bound(int device, int* status_out, double* ms_out);
+
 /* ---------------------------------------------------------------------------
  * Batched ensemble (no counterpart in the reference): n scenarios with their
  * own parameters and uneven grids (all of one `order`) advanced together.

@@ -52,6 +52,7 @@ SIGNATURES = {
     "lsh_get_launch_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
     "lsh_profile_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsh_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, DP]),
+    "lsh_probe_wait_bound": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP]),
     "lsh_step_noalloc": (ctypes.c_int, [P, P, ctypes.c_int, DP, DP, P]),
     "lsh_batch_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]),
     "lsh_batch_destroy": (ctypes.c_int, [P]),
@@ -129,6 +130,16 @@ def probe_fp64_peak(device=0):
     g = ctypes.c_double()
     _check(load().lsh_probe_fp64_peak(int(device), ctypes.byref(g)), "lsh_probe_fp64_peak")
     return g.value
+
+
+def probe_wait_bound(device=0):
+    """(status, ms): the status the bounded waits between passes report when
+    their counters never complete (LSH_ERR_TIMEOUT expected), and the probe
+    kernel's duration."""
+    st = ctypes.c_int()
+    ms = ctypes.c_double()
+    _check(load().lsh_probe_wait_bound(int(device), ctypes.byref(st), ctypes.byref(ms)), "lsh_probe_wait_bound")
+    return st.value, ms.value
 
 
 class Solver:

@@ -1,13 +1,15 @@
 """Failures reported without faulting the GPU: a NaN in the input, the dt
-stall guard, a grid too large for device memory, an empty checkpoint budget.
-Each returns its status and leaves the context usable."""
+stall guard, a grid too large for device memory, an empty checkpoint budget,
+and the bounded waits between passes running out.  Each returns its status and
+leaves the context usable."""
 import copy
 
 import numpy as np
 import pytest
 
 from landslidehysea_gb300 import scenarios
-from landslidehysea_gb300._abi import LSH_ERR_GPU_OOM, LSH_ERR_INVALID, LSH_ERR_NUMERIC, LSH_ERR_STALL, default_params
+from landslidehysea_gb300._abi import (LSH_ERR_GPU_OOM, LSH_ERR_INVALID, LSH_ERR_NUMERIC, LSH_ERR_STALL,
+                                       LSH_ERR_TIMEOUT, default_params)
 from landslidehysea_gb300.solver import LshError
 
 pytestmark = pytest.mark.gpu
@@ -64,3 +66,19 @@ def test_adjoint_budget_without_room(gpu_lib):
         A.set_budget(1e9)
         J, eta = A.forward(sc.state, 3)
         assert eta.shape == (3, 1)
+
+
+def test_bounded_waits_give_up_and_report(gpu_lib):
+    """The overlapped step's and the work queue's waits, on counters that
+    nothing increments, give up after their ~2 s bounds and report
+    LSH_ERR_TIMEOUT; the device keeps working."""
+    from landslidehysea_gb300.solver import Solver, probe_wait_bound
+    status, ms = probe_wait_bound(0)
+    assert status == LSH_ERR_TIMEOUT
+    assert 3000.0 < ms < 20000.0  # two waits of about 2 s each
+    sc = scenarios.shelf(n=24, dx=200.0)
+    with Solver(sc.params) as s:
+        s.set_state(sc.state)
+        s.step(3)
+        s.synchronize()
+        assert s.time()[2] == 3
