@@ -303,8 +303,11 @@ int lsh_adjoint_get_state(lsh_adjoint* a, double* const host_state[6]);
  * together, for one step count.  One
  * checkpoint schedule drives every member with the same slot count, taken
  * from a joint budget (default 180 GB, capped by free device memory) over
- * the members' summed slot bytes; each member's kernels run on its own
- * stream, so the members overlap on the GPU.  Each member's misfit and
+ * the members' summed slot bytes.  Every operation of the schedule
+ * runs all members of an order at once, on one stream the members share: a
+ * forward step is one persistent work-queue launch over every member's
+ * tiles, and a reversed step is one queue launch of the recomputation plus
+ * one persistent launch of the whole adjoint step.  Each member's misfit and
  * gradient are bit-identical to an lsh_adjoint of its own with that slot
  * count.
  * ------------------------------------------------------------------------ */
