@@ -313,22 +313,22 @@ def time_oracle(sc, steps, warmup, threads=0):
 
 
 def cpu_baseline(sc, n):
-    """The bounded CPU baseline of the default run (about 15-20 s on 16
-    cores): the bench workload itself for 30 steps after 2 warm-up steps on
-    every host core; beside it the 200^2 first-order shelf of the plain
-    method for its full 1000 steps on every core, and 250 of its steps on one
-    core (the serial transcription)."""
+    """The bounded CPU baseline of the default run (about 40 s on 16 cores):
+    the bench workload itself for 100 steps after 2 warm-up steps on every
+    host core; beside it the 200^2 first-order shelf of the plain method for
+    its full 1000 steps on every core and on one core (the serial
+    transcription)."""
     from landslidehysea_gb300 import scenarios
-    v, used, el = time_oracle(sc, 30, 2)
+    v, used, el = time_oracle(sc, 100, 2)
     c0 = scenarios.shelf(n=200)
     v0, used0, el0 = time_oracle(c0, 1000, 0)
-    v1, _, el1 = time_oracle(c0, 250, 0, threads=1)
+    v1, _, el1 = time_oracle(c0, 1000, 0, threads=1)
     _oracle(0)
     return {"value": v, "unit": UNIT, "cores": used, "kind": "port",
-            "sample": f"30 steps of the {n}^2 workload after 2 warm-up steps ({el:.1f} s), FP64 oracle on "
+            "sample": f"100 steps of the {n}^2 workload after 2 warm-up steps ({el:.1f} s), FP64 oracle on "
                       f"{used} threads",
             "shelf200_order1_1000_steps": {"value": v0, "cores": used0, "seconds": round(el0, 2)},
-            "shelf200_order1_serial_250_steps": {"value": v1, "cores": 1, "seconds": round(el1, 2)}}
+            "shelf200_order1_serial_1000_steps": {"value": v1, "cores": 1, "seconds": round(el1, 2)}}
 
 
 def run_reference_cuda(args):
