@@ -139,7 +139,7 @@ def parse():
     ap.add_argument("--ens-sizes", default="128,256,512,768",
                     help="ensemble: grid sizes the scenarios are drawn from (one size: a uniform ensemble)")
     ap.add_argument("--ens-kind", choices=("shelf", "fjord"), default="shelf",
-                    help="ensemble: the config-0 shelf generator (configs[3]) or the fjord generator")
+                    help="ensemble: the 200^2 shelf generator at each size (the 256-scenario ensemble) or the fjord generator")
     ap.add_argument("--cal-count", type=int, default=64, help="batched-adjoint scenarios")
     ap.add_argument("--cal-steps", type=int, default=300, help="batched-adjoint steps (the full calibration: 3000)")
     ap.add_argument("--cal-serial", type=int, default=1, help="also run the members one by one (1) or not (0)")

@@ -1106,6 +1106,10 @@ __global__ void __launch_bounds__(kRThreads, LSH_ADJB_MINB) k_adjb_reverse(RPlan
     __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy, s_lo, s_hi, s_key;
     AdjArgs& a = *reinterpret_cast<AdjArgs*>(sargs);
     const int tid = threadIdx.x;
+    // thread 0's: the producer rows and the full passes last found complete,
+    // and the (member, rate) its patched dt and rate selection belong to
+    WaitCache wc;
+    int full_pass = -1, full_scen = -1, patch_scen = -1, patch_rate = -1;
     if (tid == 0) { s_lo = 0; s_hi = 0; s_key = -1; }
     for (;;) {
         if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)LSH_ADJB_FETCH);
@@ -1161,21 +1165,30 @@ __global__ void __launch_bounds__(kRThreads, LSH_ADJB_MINB) k_adjb_reverse(RPlan
                     const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
                     t0 = max(t0, 0);
                     t1 = min(t1, nrows - 1);
-                    gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, t0, t1, (unsigned)P.tiles_x[pp.kind * P.n + s],
-                                               P.abort_flag, start);
+                    if (!wc.covers(ps.prod, s, t0, t1)) {
+                        gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, t0, t1,
+                                             (unsigned)P.tiles_x[pp.kind * P.n + s], P.abort_flag, start);
+                        if (!gave_up) wc.set(ps.prod, s, t0, t1);
+                    }
                 }
-                if (!gave_up && ps.fprod >= 0) {
+                if (!gave_up && ps.fprod >= 0 && !(ps.fprod == full_pass && s == full_scen)) {
                     const RPass pp = P.pass[ps.fprod];
                     const int rbase = P.row_pre[pp.kind * (P.n + 1) + s];
                     const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
                     gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, 0, nrows - 1, (unsigned)P.tiles_x[pp.kind * P.n + s],
-                                               P.abort_flag, start);
+                                         P.abort_flag, start);
+                    if (!gave_up) { full_pass = ps.fprod; full_scen = s; }
                 }
                 if (gave_up) atomicOr(&M.tm->err, 1 << LSH_ERR_TIMEOUT);
                 // the step's dt and, for the stage-1 passes, the rate selection
-                a.dt = M.dts[step];
-                if (ps.rate) { a.rate_cell = M.rsel->cell; a.rate_bar = M.rsel->bar; }
-                else { a.rate_cell = -1; a.rate_bar = 0.0; }
+                // (final once the pass may run: it waits for the rate item)
+                if (s_copy || s != patch_scen || ps.rate != patch_rate) {
+                    a.dt = M.dts[step];
+                    if (ps.rate) { a.rate_cell = M.rsel->cell; a.rate_bar = M.rsel->bar; }
+                    else { a.rate_cell = -1; a.rate_bar = 0.0; }
+                    patch_scen = s;
+                    patch_rate = ps.rate;
+                }
             }
             __syncthreads();
             double* part = ps.parts ? M.part + ((size_t)P.part_off[p * P.n + s] + t) * kRed : nullptr;

@@ -131,6 +131,17 @@ __device__ __forceinline__ bool queue_wait(const unsigned* c, int t0, int t1, un
     return false;
 }
 
+// The producer rows a CTA's thread 0 last found complete: (pass, scenario,
+// tile rows [t0, t1]).  Counters only grow within a launch, so an item whose
+// wait falls inside that range needs no new acquire: the earlier acquire,
+// followed by the block barrier, already orders its reads after the
+// producers' writes.  Consecutive items of one tile row share their waits.
+struct WaitCache {
+    int pass = -1, scen = -1, t0 = 0, t1 = -1;
+    __device__ bool covers(int p, int s, int a, int b) const { return p == pass && s == scen && a >= t0 && b <= t1; }
+    __device__ void set(int p, int s, int a, int b) { pass = p; scen = s; t0 = a; t1 = b; }
+};
+
 // Marks an item of counter row c done: a release add, ordered after the
 // item's writes by the block barrier before it (one thread).
 __device__ __forceinline__ void queue_done(unsigned* c) {
@@ -183,6 +194,7 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
     __shared__ int s_lo, s_hi, s_args_key;
     const KArgs& a = *reinterpret_cast<const KArgs*>(sargs);
     const int tid = threadIdx.x;
+    WaitCache wc;  // thread 0's
     if (tid == 0) { s_lo = 0; s_hi = 0; s_args_key = -1; }
     for (;;) {
         if (tid == 0) s_first = (int)atomicAdd(P.head, (unsigned)fetch);
@@ -234,10 +246,13 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
                 const int nrows = P.row_pre[pp.kind * (P.n + 1) + s + 1] - rbase;
                 t0 = max(t0, 0);
                 t1 = min(t1, nrows - 1);
-                unsigned long long start = 0;
-                const bool gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, t0, t1, (unsigned)P.tiles_x[pp.kind * P.n + s],
-                                                P.abort_flag, start);
-                if (gave_up) atomicOr(&a.tm->err, 1 << LSH_ERR_TIMEOUT);
+                if (!wc.covers(ps.prod, s, t0, t1)) {
+                    unsigned long long start = 0;
+                    const bool gave_up = queue_wait(P.ctr + pp.ctr_off + rbase, t0, t1,
+                                                    (unsigned)P.tiles_x[pp.kind * P.n + s], P.abort_flag, start);
+                    if (gave_up) atomicOr(&a.tm->err, 1 << LSH_ERR_TIMEOUT);
+                    else wc.set(ps.prod, s, t0, t1);
+                }
             }
             __syncthreads();
             if (live) {
