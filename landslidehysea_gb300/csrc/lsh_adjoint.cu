@@ -133,9 +133,19 @@ struct RateSel {
 };
 
 // One edge per thread over a 2-D tile (adj_edge_block); one partial-sum row
-// per block.
+// per block.  With `d` the block waits for the producer pass's rows over the
+// cell rows its edges touch, and counts itself done (the overlapped reverse
+// step; `tm` takes a timed-out wait's bit).
 template <int DIR, bool FIRST, int ORDER>
-__global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_EDGE_MINB) k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part) {
+__global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_EDGE_MINB)
+    k_adj_edges(AdjArgs a, const RateSel* rs, int par, double* part, Dep d, lsh::TimeRec* tm) {
+    if (d.done || d.wait) {
+        // horizontal: edge rows par + 2 w, w in [8 by, 8 by + 7], touch cell rows
+        // y - 1 and y; vertical: rows [16 by, 16 by + 15]
+        const int r0 = (DIR == 0) ? par + 16 * (int)blockIdx.y - 1 : 16 * (int)blockIdx.y;
+        const int r1 = (DIR == 0) ? par + 16 * (int)blockIdx.y + 14 : 16 * (int)blockIdx.y + 15;
+        dep_begin(d, tm, max(r0, 0), min(r1, a.c.ny - 1));
+    }
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const int nx = a.c.nx, ny = a.c.ny;
@@ -153,11 +163,20 @@ __global__ void __launch_bounds__(kAdjEdgeBlock, LSH_ADJ_EDGE_MINB) k_adj_edges(
     double v[kRed];
     pack9(dtb, cb, v);
     block_sum9<kAdjEdgeBlock>(v, part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * kRed);
+    dep_end(d);
 }
 
-// One cell per thread over 16 x 8 tiles.
+// One cell per thread over 16 x 8 tiles.  MODE 1 (the stage-1 volume of a
+// second-order step) overwrites the slope adjoints that the stage-2
+// reconstruction adjoint reads one row around each cell, so with `d` it
+// waits for one row more on each side.
 template <int MODE>
-__global__ void __launch_bounds__(kAdjCellBlock, LSH_ADJ_MINBLOCKS) k_adj_volume(AdjArgs a, const RateSel* rs, double* part) {
+__global__ void __launch_bounds__(kAdjCellBlock, LSH_ADJ_MINBLOCKS)
+    k_adj_volume(AdjArgs a, const RateSel* rs, double* part, Dep d, lsh::TimeRec* tm) {
+    if (d.done || d.wait) {
+        const int y0 = 8 * (int)blockIdx.y, ext = (MODE == 1) ? 1 : 0;
+        dep_begin(d, tm, max(y0 - ext, 0), min(y0 + 7 + ext, a.c.ny - 1));
+    }
     a.rate_cell = rs ? rs->cell : -1;
     a.rate_bar = rs ? rs->bar : 0.0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -168,11 +187,19 @@ __global__ void __launch_bounds__(kAdjCellBlock, LSH_ADJ_MINBLOCKS) k_adj_volume
     double v[kRed];
     pack9(dtb, cb, v);
     block_sum9<kAdjCellBlock>(v, part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * kRed);
+    dep_end(d);
 }
 
-__global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a) {
+// Gathers the slope adjoints one cell around: with `d` it waits for the rows
+// around its tile.
+__global__ void __launch_bounds__(kAdjCellBlock) k_adj_recon(AdjArgs a, Dep d, lsh::TimeRec* tm) {
+    if (d.done || d.wait) {
+        const int y0 = 8 * (int)blockIdx.y;
+        dep_begin(d, tm, max(y0 - 1, 0), min(y0 + 8, a.c.ny - 1));
+    }
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i < a.c.nx && j < a.c.ny) lsh::recon_adj_cell(a, j * a.c.nx + i);
+    dep_end(d);
 }
 
 // The recomputation's reconstruction: slopes (bit-identical to k_recon's)
@@ -539,25 +566,83 @@ template <int ORDER, int MODE>
 void rev_stage(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, long long* nparts, cudaStream_t s) {
     const int nx = A->p.nx, ny = A->p.ny;
     dim3 g = adj_cell_grid(nx, ny);
-    k_adj_volume<MODE><<<g, adj_cell_block(), 0, s>>>(a, rs, A->part + *nparts * kRed);
+    k_adj_volume<MODE><<<g, adj_cell_block(), 0, s>>>(a, rs, A->part + *nparts * kRed, Dep{}, nullptr);
     *nparts += blocks_of(g);
     a.snap[0] = snaps[2][0]; a.snap[1] = snaps[2][1];
     g = adj_edge_grid(nx, ny, 1, 1);
-    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 1, A->part + *nparts * kRed, Dep{}, nullptr);
     *nparts += blocks_of(g);
     a.snap[0] = snaps[1][0]; a.snap[1] = snaps[1][1];
     g = adj_edge_grid(nx, ny, 1, 0);
-    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    k_adj_edges<1, false, ORDER><<<g, adj_edge_block(1), 0, s>>>(a, rs, 0, A->part + *nparts * kRed, Dep{}, nullptr);
     *nparts += blocks_of(g);
     a.snap[0] = snaps[0][0]; a.snap[1] = snaps[0][1];
     g = adj_edge_grid(nx, ny, 0, 1);
-    k_adj_edges<0, false, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 1, A->part + *nparts * kRed);
+    k_adj_edges<0, false, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 1, A->part + *nparts * kRed, Dep{}, nullptr);
     *nparts += blocks_of(g);
     a.snap[0] = a.snap[1] = nullptr;
     g = adj_edge_grid(nx, ny, 0, 0);
-    k_adj_edges<0, true, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 0, A->part + *nparts * kRed);
+    k_adj_edges<0, true, ORDER><<<g, adj_edge_block(0), 0, s>>>(a, rs, 0, A->part + *nparts * kRed, Dep{}, nullptr);
     *nparts += blocks_of(g);
-    if (ORDER == 2) k_adj_recon<<<adj_cell_grid(nx, ny), adj_cell_block(), 0, s>>>(a);
+    if (ORDER == 2) k_adj_recon<<<adj_cell_grid(nx, ny), adj_cell_block(), 0, s>>>(a, Dep{}, nullptr);
+}
+
+
+// The same passes as overlapped launches: each after the first is a
+// programmatic dependent launch whose blocks wait only for the rows of the
+// pass before that they read or overwrite (lsh_kernels.cuh's Dep, with the
+// adjoint's block heights).  `prev` is the Dep of the pass before this stage
+// (wait null: this stage starts the chain); `seg` the next free counter
+// segment.  Returns the Dep of this stage's last pass for the next one.
+template <int ORDER, int MODE>
+Dep rev_stage_overlap(lsh_adjoint* A, AdjArgs a, double* snaps[3][2], const RateSel* rs, long long* nparts,
+                      cudaStream_t s, Dep prev, unsigned*& seg, bool last) {
+    const int nx = A->p.nx, ny = A->p.ny, st = A->dep_stride;
+    // the Dep a consumer of a pass on grid g, of kind k and block height h, waits with
+    auto waits_on = [](const unsigned* done, dim3 g, int kind, int span) {
+        Dep w;
+        w.wait = done; w.target = g.x; w.kind = kind; w.ntiles = (int)g.y; w.span = span;
+        return w;
+    };
+    const int npass = (ORDER == 2) ? 6 : 5;
+    int k = 0;
+    auto done_of = [&](Dep d) {
+        ++k;
+        d.done = (last && k == npass) ? nullptr : seg;
+        return d;
+    };
+    dim3 g = adj_cell_grid(nx, ny);
+    Dep d = done_of(prev);
+    launch_pass(prev.wait != nullptr, g, adj_cell_block(), s, k_adj_volume<MODE>, a, rs, A->part + *nparts * kRed, d,
+                A->tm);
+    *nparts += blocks_of(g);
+    Dep w = waits_on(d.done, g, kDepCell, 8);
+    seg += st;
+    // colour passes, last first: v1, v0 (block rows of 16), h1, h0 (8 edge lines)
+    const int dirs[4] = {1, 1, 0, 0}, pars[4] = {1, 0, 1, 0};
+    for (int c = 0; c < 4; ++c) {
+        const int dir = dirs[c], par = pars[c];
+        a.snap[0] = (c < 3) ? snaps[2 - c][0] : nullptr;
+        a.snap[1] = (c < 3) ? snaps[2 - c][1] : nullptr;
+        g = adj_edge_grid(nx, ny, dir, par);
+        d = done_of(w);
+        double* part = A->part + *nparts * kRed;
+        if (c < 2) launch_pass(true, g, adj_edge_block(1), s, k_adj_edges<1, false, ORDER>, a, rs, par, part, d, A->tm);
+        else if (c == 2) launch_pass(true, g, adj_edge_block(0), s, k_adj_edges<0, false, ORDER>, a, rs, par, part, d, A->tm);
+        else launch_pass(true, g, adj_edge_block(0), s, k_adj_edges<0, true, ORDER>, a, rs, par, part, d, A->tm);
+        *nparts += blocks_of(g);
+        w = waits_on(d.done, g, dir ? kDepV : (par ? kDepH1 : kDepH0), dir ? 16 : 8);
+        seg += st;
+    }
+    a.snap[0] = a.snap[1] = nullptr;
+    if (ORDER == 2) {
+        g = adj_cell_grid(nx, ny);
+        d = done_of(w);
+        launch_pass(true, g, adj_cell_block(), s, k_adj_recon, a, d, A->tm);
+        w = waits_on(d.done, g, kDepCell, 8);
+        seg += st;
+    }
+    return w;
 }
 
 void zero6(double* const* v, size_t N, cudaStream_t s) {
@@ -670,17 +755,31 @@ int Ops::reverse_step(int n) {
     long long nparts = 0;
     if (A->order == 1) {
         AdjArgs a = adj_args(A, X, nullptr, nullptr, A->acc1, A->Xbn, A->Xb, nullptr, nullptr, dt);
-        rev_stage<1, 0>(A, a, A->snap1, A->rsel, &nparts, s);
+        if (A->dep_ctr) {
+            unsigned* seg = A->dep_ctr;
+            rev_stage_overlap<1, 0>(A, a, A->snap1, A->rsel, &nparts, s, Dep{}, seg, true);
+        } else {
+            rev_stage<1, 0>(A, a, A->snap1, A->rsel, &nparts, s);
+        }
     } else {
         double* Y7[7];
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
         Y7[6] = A->X[6];
         zero6(A->Yb, N, s);
         AdjArgs a2 = adj_args(A, Y7, A->s2x, A->s2y, A->acc2, A->Yb, A->Xb, A->Xbn, A->tape2, dt);
-        rev_stage<2, 2>(A, a2, A->snap2, nullptr, &nparts, s);
         AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
-        rev_stage<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s);
+        if (A->dep_ctr) {
+            // both stages as one chain of overlapped passes
+            unsigned* seg = A->dep_ctr;
+            const Dep w = rev_stage_overlap<2, 2>(A, a2, A->snap2, nullptr, &nparts, s, Dep{}, seg, false);
+            rev_stage_overlap<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s, w, seg, true);
+        } else {
+            rev_stage<2, 2>(A, a2, A->snap2, nullptr, &nparts, s);
+            rev_stage<2, 1>(A, a1, A->snap1, A->rsel, &nparts, s);
+        }
     }
+    // ordered after the chain: its counters back to zero
+    if (A->dep_ctr) cudaMemsetAsync(A->dep_ctr, 0, size_t(13) * A->dep_stride * sizeof(unsigned), s);
     {
         const long long chunk = (nparts + kReduceRows - 1) / kReduceRows;
         k_adj_reduce_rows<<<kReduceRows, 32 * kRed, 0, s>>>(A->part, nparts, chunk, A->part2);

@@ -114,19 +114,26 @@ struct Dep {
     unsigned target = 0;             // producer blocks per block row (its gridDim.x)
     int kind = 0;                    // producer tiling (DepKind)
     int ntiles = 0;                  // producer block rows (its gridDim.y)
+    int span = 0;                    // producer block height: cell rows, or edge lines for kDepH*
+                                     // (0: the step kernels' blocks)
 };
 
 // Producer block rows that wrote cell rows [r0, r1].
 __device__ __forceinline__ void dep_tiles(const Dep& d, int r0, int r1, int& t0, int& t1) {
-    if (d.kind == kDepV) { t0 = r0 / kEdgeVBY; t1 = r1 / kEdgeVBY; }
-    else if (d.kind == kDepCell) { t0 = r0 / kCellBY; t1 = r1 / kCellBY; }
-    else {
+    if (d.kind == kDepV) {
+        const int b = d.span ? d.span : kEdgeVBY;
+        t0 = r0 / b; t1 = r1 / b;
+    } else if (d.kind == kDepCell) {
+        const int b = d.span ? d.span : kCellBY;
+        t0 = r0 / b; t1 = r1 / b;
+    } else {
         // horizontal edge row y = p + 2 t writes cell rows y - 1 and y: the
         // edge rows touching [r0, r1] are [r0, r1 + 1]
+        const int b = d.span ? d.span : kEdgeHBY;
         const int p = d.kind;
         const int lo = max(r0 - p + 1, 0) / 2, hi = (r1 + 1 - p) / 2;
-        t0 = lo / kEdgeHBY;
-        t1 = max(hi, 0) / kEdgeHBY;
+        t0 = lo / b;
+        t1 = max(hi, 0) / b;
     }
     t0 = max(t0, 0);
     t1 = min(t1, d.ntiles - 1);
