@@ -58,7 +58,7 @@ COUNTER_SOURCES = ("landslidehysea_gb300/csrc/lsh_core.cu", "landslidehysea_gb30
                    "landslidehysea_gb300/csrc/lsh_passes.cuh", "landslidehysea_gb300/csrc/lsh_scheme.cuh",
                    "landslidehysea_gb300/csrc/lsh_fpmath.h", "landslidehysea_gb300/csrc/lsh_setup.h",
                    "landslidehysea_gb300/build.py", "landslidehysea_gb300/scenarios.py")
-COUNTERS_SOURCE_HASH = "7a596f1664993d16"
+COUNTERS_SOURCE_HASH = "032c79f00d393a67"
 # FP64-pipe thread instructions per cell-update of one step (6.060e8 per step
 # / 4,194,304 cells).  The FP64 pipe takes one such instruction per lane as
 # the measured peak's DFMA does, so the peak instruction rate is the measured
@@ -68,8 +68,8 @@ FJORD2048_FP64_INSTR_PER_CELL_STEP = 144.49
 # first (accumulator-writing) horizontal pass.  A second-order step launches
 # recon and the four edge passes twice, each volume kernel once.
 FJORD2048_DRAM_BYTES_PER_LAUNCH = {
-    "recon": 139.5e6, "edge_h0": 356.85e6, "edge_h1": 170.85e6, "edge_v0": 171.05e6, "edge_v1": 167.4e6,
-    "volume1": 651.6e6, "volume2": 699.1e6,
+    "recon": 139.65e6, "edge_h0": 356.35e6, "edge_h1": 170.95e6, "edge_v0": 170.5e6, "edge_v1": 167.4e6,
+    "volume1": 651.1e6, "volume2": 699.1e6,
 }
 # Algorithmic HBM bytes per cell-step (FP64 state with perfect reuse): first
 # order 13 x 8 = 104 B (read 6 state + H, write 6 state); TVD-RK2 104 B for
