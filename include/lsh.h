@@ -279,6 +279,10 @@ int lsh_adjoint_destroy(lsh_adjoint* a);
  * without bound through the 1/h and sqrt(h) derivatives of thin layers; a
  * few millimetres to centimetres keeps it finite. */
 int lsh_adjoint_set_thin_layer(lsh_adjoint* a, double h_adj);
+/* ordered != 0: run the forward, recomputed and adjoint passes each as a
+ * full-grid launch after the one before, instead of overlapped (the default).
+ * The results are the same bits either way; this checks that. */
+int lsh_adjoint_set_ordered(lsh_adjoint* a, int ordered);
 /* device bytes the checkpoint slots may take */
 int lsh_adjoint_set_budget(lsh_adjoint* a, double bytes);
 /* run nsteps from host_state (7 arrays); target: nsteps x n_gauges (NULL: no

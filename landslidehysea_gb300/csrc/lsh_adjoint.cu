@@ -416,6 +416,7 @@ struct lsh_adjoint {
     unsigned char* szero1 = nullptr, *szero2 = nullptr;  // slope-zero flags of s1x/s1y and s2x/s2y
     unsigned* dep_ctr = nullptr;    // pass-overlap counters of one step (13 segments of dep_stride)
     int dep_stride = 0;             // 0: the passes run fully ordered
+    bool ordered = false;           // lsh_adjoint_set_ordered: no pass overlap
     double* geo_buf = nullptr;
     Geo geo{};
     lsh::TimeRec* tm = nullptr;
@@ -454,6 +455,9 @@ struct lsh_adjoint {
 };
 
 namespace {
+
+// The counters of the overlapped passes, or null when they run in full order.
+unsigned* overlap_ctr(const lsh_adjoint* A) { return A->ordered ? nullptr : A->dep_ctr; }
 
 KArgs fwd_args(const lsh_adjoint* A, const double* const* W, double* const* Wout, const double* const* Xavg,
                double* const* acc, double* const* sx, double* const* sy) {
@@ -501,7 +505,7 @@ void fwd_passes(const lsh_adjoint* A, const KArgs& a, double* snaps[3][2], doubl
 void fwd_step(const lsh_adjoint* A, cudaStream_t s) {
     const dim3 nbc = cell_grid(A->p.nx, A->p.ny);
     double* const* X = A->X;
-    if (A->dep_ctr) {
+    if (overlap_ctr(A)) {
         // the product's overlapped step (lsh_kernels.cuh)
         double* Y7[7];
         for (int k = 0; k < 6; ++k) Y7[k] = A->Y[k];
@@ -701,7 +705,7 @@ int Ops::reverse_step(int n) {
     k_set_dt<<<1, 1, 0, s>>>(A->tm, A->d_dts + n);
     double* const* X = A->X;
     const double dt = A->h_dts[n];
-    if (A->dep_ctr) {
+    if (overlap_ctr(A)) {
         // overlapped passes; the edge passes take the accumulator snapshots
         // themselves, at the cells the reverse sweep reads them
         unsigned* c = A->dep_ctr;
@@ -755,7 +759,7 @@ int Ops::reverse_step(int n) {
     long long nparts = 0;
     if (A->order == 1) {
         AdjArgs a = adj_args(A, X, nullptr, nullptr, A->acc1, A->Xbn, A->Xb, nullptr, nullptr, dt);
-        if (A->dep_ctr) {
+        if (overlap_ctr(A)) {
             unsigned* seg = A->dep_ctr;
             rev_stage_overlap<1, 0>(A, a, A->snap1, A->rsel, &nparts, s, Dep{}, seg, true);
         } else {
@@ -768,7 +772,7 @@ int Ops::reverse_step(int n) {
         zero6(A->Yb, N, s);
         AdjArgs a2 = adj_args(A, Y7, A->s2x, A->s2y, A->acc2, A->Yb, A->Xb, A->Xbn, A->tape2, dt);
         AdjArgs a1 = adj_args(A, X, A->s1x, A->s1y, A->acc1, A->Xbn, A->Yb, nullptr, A->tape1, dt);
-        if (A->dep_ctr) {
+        if (overlap_ctr(A)) {
             // both stages as one chain of overlapped passes
             unsigned* seg = A->dep_ctr;
             const Dep w = rev_stage_overlap<2, 2>(A, a2, A->snap2, nullptr, &nparts, s, Dep{}, seg, false);
@@ -779,7 +783,7 @@ int Ops::reverse_step(int n) {
         }
     }
     // ordered after the chain: its counters back to zero
-    if (A->dep_ctr) cudaMemsetAsync(A->dep_ctr, 0, size_t(13) * A->dep_stride * sizeof(unsigned), s);
+    if (overlap_ctr(A)) cudaMemsetAsync(A->dep_ctr, 0, size_t(13) * A->dep_stride * sizeof(unsigned), s);
     {
         const long long chunk = (nparts + kReduceRows - 1) / kReduceRows;
         k_adj_reduce_rows<<<kReduceRows, 32 * kRed, 0, s>>>(A->part, nparts, chunk, A->part2);
@@ -1881,6 +1885,12 @@ int lsh_adjoint_destroy(lsh_adjoint* A) {
 int lsh_adjoint_set_thin_layer(lsh_adjoint* A, double h_adj) {
     if (!A || !(h_adj >= 0.0)) return LSH_ERR_INVALID;
     A->h_adj = h_adj;
+    return LSH_OK;
+}
+
+int lsh_adjoint_set_ordered(lsh_adjoint* A, int ordered) {
+    if (!A) return LSH_ERR_INVALID;
+    A->ordered = (ordered != 0);
     return LSH_OK;
 }
 

@@ -69,6 +69,7 @@ SIGNATURES = {
     "lsh_adjoint_destroy": (ctypes.c_int, [P]),
     "lsh_adjoint_set_budget": (ctypes.c_int, [P, ctypes.c_double]),
     "lsh_adjoint_set_thin_layer": (ctypes.c_int, [P, ctypes.c_double]),
+    "lsh_adjoint_set_ordered": (ctypes.c_int, [P, ctypes.c_int]),
     "lsh_adjoint_forward": (ctypes.c_int, [P, P, ctypes.c_int, P, DP, P]),
     "lsh_adjoint_gradient": (ctypes.c_int, [P, ctypes.c_double, P, P, P]),
     "lsh_adjoint_get_stats": (ctypes.c_int, [P, P]),
@@ -403,6 +404,10 @@ class Adjoint:
 
     def set_budget(self, nbytes):
         _check(self.lib.lsh_adjoint_set_budget(self._a, float(nbytes)), "lsh_adjoint_set_budget")
+
+    def set_ordered(self, ordered=True):
+        """Run every pass as a full-grid launch after the one before (no overlap)."""
+        _check(self.lib.lsh_adjoint_set_ordered(self._a, int(bool(ordered))), "lsh_adjoint_set_ordered")
 
     def forward(self, state, nsteps, target=None):
         """Run `nsteps` from `state` (dict or 7 arrays); returns (J, eta series [nsteps, n_gauges])."""
