@@ -368,14 +368,15 @@ int lsh_batch_get_tune(lsh_batch* b, lsh_tune* tune) {
 // taken while tuning are real steps of the simulation.
 int lsh_batch_autotune(lsh_batch* b, int trial_steps, lsh_tune* best_out) {
     if (!b || trial_steps < 1) return LSH_ERR_INVALID;
-    static const int ctas[] = {8, 12, 16, 20};
-    static const int fetches[] = {1, 2, 4};
+    static const int ctas[] = {8, 12, 16, 20, 24, 32};
+    static const int fetches[] = {1, 2, 4, 8};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     lsh_tune best = b->tune;
     best.ms_per_step = INFINITY;
     for (int c : ctas) {
+        if (c > kBMaxCtas) continue;
         for (int f : fetches) {
             lsh_tune t{c, f, 0.0};
             if (int s = lsh_batch_set_tune(b, &t)) { cudaEventDestroy(e0); cudaEventDestroy(e1); return s; }

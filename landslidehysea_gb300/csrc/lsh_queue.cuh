@@ -39,7 +39,11 @@ struct NoTape {
 };
 
 constexpr int kBThreads = 64;    // threads per persistent CTA
-constexpr int kBMaxCtas = 20;    // CTAs per SM the step kernel is compiled for (48 registers)
+// CTAs per SM the step kernel is compiled for (its register budget: 48 at 20)
+#ifndef LSH_BATCH_MAXCTAS
+#define LSH_BATCH_MAXCTAS 20
+#endif
+constexpr int kBMaxCtas = LSH_BATCH_MAXCTAS;
 constexpr int kMaxPasses = 12;
 
 // Tilings of a scenario's passes, 64-thread tiles of the single-grid shapes:
@@ -142,15 +146,17 @@ struct WaitCache {
     __device__ void set(int p, int s, int a, int b) { pass = p; scen = s; t0 = a; t1 = b; }
 };
 
-// Marks an item of counter row c done: a release add, ordered after the
-// item's writes by the block barrier before it (one thread).
-__device__ __forceinline__ void queue_done(unsigned* c) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(c) : "memory");
+// Marks n items of counter row c done: a release add, ordered after the
+// items' writes by the block barrier before it (one thread).
+__device__ __forceinline__ void queue_done(unsigned* c, unsigned n = 1u) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(c), "r"(n) : "memory");
 }
 
 // One item's work: the single-grid kernels' per-thread bodies on one tile.
+// Returns the thread's dt-rate bits for the Euler stages that take the rate
+// maximum (kOpVol0, kOpVol1), kRateInitBits otherwise; the caller reduces them.
 template <int ORDER, int OP, class TAPE>
-__device__ __forceinline__ void item_work(const KArgs& a, int tx, int ty, double dt) {
+__device__ __forceinline__ unsigned long long item_work(const KArgs& a, int tx, int ty, double dt) {
     const int nx = a.c.nx, ny = a.c.ny, tid = threadIdx.x;
     if constexpr (OP == kOpH0 || OP == kOpH1) {
         const int par = OP;
@@ -172,24 +178,40 @@ __device__ __forceinline__ void item_work(const KArgs& a, int tx, int ty, double
             constexpr int MODE = OP - kOpVol0;
             unsigned long long bits = kRateInitBits;
             if (in) bits = lsh::volume_cell<MODE>(a, j * nx + i, dt);
-            if (MODE != 2) lsh::block_max_bits<kBThreads>(bits, &a.tm->rmax_bits);
+            return (MODE != 2) ? bits : kRateInitBits;
         }
     }
+    return kRateInitBits;
+}
+
+// A run of tiles tx0 .. tx0 + run - 1 of one tile row; the largest rate bits.
+template <int ORDER, int OP, class TAPE>
+__device__ __forceinline__ unsigned long long run_work(const KArgs& a, int tx0, int run, int ty, double dt) {
+    unsigned long long bits = kRateInitBits;
+    for (int j = 0; j < run; ++j) {
+        const unsigned long long b = item_work<ORDER, OP, TAPE>(a, tx0 + j, ty, dt);
+        bits = (b > bits) ? b : bits;
+    }
+    return bits;
 }
 
 // The whole step of every scenario.  Items are dequeued in pass order, and an
 // item waits only for items of earlier passes, which running CTAs took
 // before it: the earliest unfinished item always has its inputs, so the
-// queue drains whatever the number of resident CTAs.  Waits are bounded
-// (~2 s of %globaltimer); one that runs out sets LSH_ERR_TIMEOUT on its
-// scenario and the batch's abort flag, and later waits give up at once.
+// queue drains whatever the number of resident CTAs.  A CTA takes `fetch`
+// consecutive items at a time and works them in runs: the items of one tile
+// row of one (pass, scenario) share their wait, their barriers and one
+// counter add, and an Euler stage's rate maximum is reduced once per run.
+// Waits are bounded (~2 s of %globaltimer); one that runs out sets
+// LSH_ERR_TIMEOUT on its scenario and the batch's abort flag, and later
+// waits give up at once.
 template <int ORDER, class TAPE = NoTape>
 __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, int fetch) {
     __shared__ __align__(16) unsigned long long sargs[(sizeof(KArgs) + 7) / 8];
-    __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy;
+    __shared__ int s_first, s_pass, s_scen, s_tile, s_ntx, s_copy, s_run;
     // the last decoded (pass, scenario): its items [s_lo, s_hi) of the queue,
     // and the arguments held in sargs (var * n + scenario, -1: none).
-    // Consecutive items of the queue share them, so most items skip the
+    // Consecutive items of the queue share them, so most runs skip the
     // scenario search and the argument copy.
     __shared__ int s_lo, s_hi, s_args_key;
     const KArgs& a = *reinterpret_cast<const KArgs*>(sargs);
@@ -202,7 +224,7 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
         const int first = s_first;
         if (first >= P.total_items) break;
         const int last = min(first + fetch, P.total_items);
-        for (int it = first; it < last; ++it) {
+        for (int it = first; it < last;) {
             if (tid == 0) {
                 if (it < s_lo || it >= s_hi) {
                     int p = 0;
@@ -223,12 +245,14 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
                     s_ntx = P.tiles_x[kind * P.n + lo];
                 }
                 s_tile = it - s_lo;
+                // the run: the fetched items left in this tile row of this (pass, scenario)
+                s_run = min(min(last, s_hi) - it, s_ntx - s_tile % s_ntx);
                 const int key = P.pass[s_pass].var * P.n + s_scen;
                 s_copy = (key != s_args_key);
                 s_args_key = key;
             }
             __syncthreads();
-            const int p = s_pass, s = s_scen, t = s_tile, ntx = s_ntx;
+            const int p = s_pass, s = s_scen, t = s_tile, ntx = s_ntx, run = s_run;
             const BPass ps = P.pass[p];
             if (s_copy) {
                 const unsigned long long* src = reinterpret_cast<const unsigned long long*>(P.args + ps.var * P.n + s);
@@ -257,28 +281,31 @@ __global__ void __launch_bounds__(kBThreads, kBMaxCtas) k_batch_step(BPlan P, in
             __syncthreads();
             if (live) {
                 const double dt = a.tm->dt;
+                unsigned long long bits = kRateInitBits;
                 switch (ps.op) {
-                    case kOpH0: item_work<ORDER, kOpH0, TAPE>(a, tx, ty, dt); break;
-                    case kOpH1: item_work<ORDER, kOpH1, TAPE>(a, tx, ty, dt); break;
-                    case kOpV0: item_work<ORDER, kOpV0, TAPE>(a, tx, ty, dt); break;
-                    case kOpV1: item_work<ORDER, kOpV1, TAPE>(a, tx, ty, dt); break;
+                    case kOpH0: run_work<ORDER, kOpH0, TAPE>(a, tx, run, ty, dt); break;
+                    case kOpH1: run_work<ORDER, kOpH1, TAPE>(a, tx, run, ty, dt); break;
+                    case kOpV0: run_work<ORDER, kOpV0, TAPE>(a, tx, run, ty, dt); break;
+                    case kOpV1: run_work<ORDER, kOpV1, TAPE>(a, tx, run, ty, dt); break;
                     default:
                         if constexpr (ORDER == 1) {
-                            item_work<ORDER, kOpVol0, TAPE>(a, tx, ty, dt);
+                            bits = run_work<ORDER, kOpVol0, TAPE>(a, tx, run, ty, dt);
                         } else {
-                            if (ps.op == kOpRecon) item_work<ORDER, kOpRecon, TAPE>(a, tx, ty, dt);
-                            else if (TAPE::kOn && ps.op == kOpReconTape) item_work<ORDER, kOpReconTape, TAPE>(a, tx, ty, dt);
-                            else if (ps.op == kOpVol1) item_work<ORDER, kOpVol1, TAPE>(a, tx, ty, dt);
-                            else item_work<ORDER, kOpVol2, TAPE>(a, tx, ty, dt);
+                            if (ps.op == kOpRecon) run_work<ORDER, kOpRecon, TAPE>(a, tx, run, ty, dt);
+                            else if (TAPE::kOn && ps.op == kOpReconTape) run_work<ORDER, kOpReconTape, TAPE>(a, tx, run, ty, dt);
+                            else if (ps.op == kOpVol1) bits = run_work<ORDER, kOpVol1, TAPE>(a, tx, run, ty, dt);
+                            else run_work<ORDER, kOpVol2, TAPE>(a, tx, run, ty, dt);
                         }
                         break;
                 }
+                if (ps.op == kOpVol0 || ps.op == kOpVol1) lsh::block_max_bits<kBThreads>(bits, &a.tm->rmax_bits);
             }
-            __syncthreads();  // the tile's writes are done, and sargs may be refilled
+            __syncthreads();  // the run's writes are done, and sargs may be refilled
             if (tid == 0) {
-                // release: the barrier above orders the tile's writes before it
-                queue_done(P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty);
+                // release: the barrier above orders the run's writes before it
+                queue_done(P.ctr + ps.ctr_off + P.row_pre[ps.kind * (P.n + 1) + s] + ty, (unsigned)run);
             }
+            it += run;
         }
     }
 }
