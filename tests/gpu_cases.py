@@ -61,12 +61,29 @@ def case(name):
         p.order = 2
         p.cfl = 0.45
         return p, st, 20
+    if name in ("dam1d_o2", "column_o2"):
+        # one-row and one-column grids at second order: every slope stencil
+        # meets a boundary across the degenerate direction
+        p, st = golden_case(name[:-3])
+        p.order = 2
+        p.cfl = 0.45
+        return p, st, 25
+    if name in ("cell1x1_o1", "cell1x1_o2"):
+        # a single cell between walls: only friction and the granular layer's
+        # Coulomb stop act
+        p = default_params(1, 1, dx=5.0, dy=5.0, cfl=0.5, r=0.5, angle_deg=8.0, mf0=0.03, mfs=0.03, eps_h=1e-4,
+                           gravity=9.81)
+        p.order = 2 if name.endswith("o2") else 1
+        one = np.ones((1, 1))
+        st = {"h1": 2.0 * one, "q1x": 0.3 * one, "q1y": -0.2 * one, "h2": 0.5 * one, "q2x": 0.1 * one,
+              "q2y": 0.05 * one, "H": 3.0 * one}
+        return p, st, 10
     raise KeyError(name)
 
 
 PARITY_CASES = ["shelf48_o1", "golden_random17x9", "golden_dam1d", "golden_column", "golden_slope",
                 "golden_shelf40", "shelf40x24_o2", "random_o2", "fjord64_o2", "fjord64_o1_sph", "pouliquen", "golden_pouliquen_random", "pouliquen_random_o2",
-                "shelf48_o2_fullsort"]
+                "shelf48_o2_fullsort", "dam1d_o2", "column_o2", "cell1x1_o1", "cell1x1_o2"]
 
 
 def rel_linf(a, b):
