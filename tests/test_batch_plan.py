@@ -9,7 +9,8 @@ waits, or belong to one pass and touch disjoint cells.
 The arrays are those of a batch scenario: the state X, the stage-1 output Y,
 the accumulators, and the slopes, which both stages of a second-order step
 share (the stage-2 reconstruction overwrites what the stage-1 edge passes
-read)."""
+read).  The single-grid step's overlapped launches follow the same rules with
+taller cell blocks (the last test)."""
 import itertools
 from collections import defaultdict
 
@@ -185,3 +186,13 @@ def test_model_flags_a_reconstruction_without_its_halo_rows():
     def narrow(op, kind, ty, ny):
         return item_rows("vol" if op.startswith("recon") else op, kind, ty, ny)
     assert check(37, 29, 2, rows=narrow) > 0
+
+
+def test_single_grid_overlapped_step_orders_every_conflict(monkeypatch):
+    """The single-grid step's overlapped launches (lsh_kernels.cuh: dep_begin
+    in k_recon, k_edges_h/v, k_volume) use the same row rules and edge
+    blocks, with cell blocks 16 rows high."""
+    monkeypatch.setitem(globals(), "CY", 16)
+    for nx, ny in [(40, 70), (37, 33), (1, 40), (20, 1)]:
+        assert check(nx, ny, 2) == 0, (nx, ny)
+        assert check(nx, ny, 1) == 0, (nx, ny)
