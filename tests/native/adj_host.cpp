@@ -124,7 +124,57 @@ void rev_stage(const Host& h, const double* const* W, const Stage& S, double dt,
 
 }  // namespace
 
+namespace {
+
+// The initial-dt pass over W (the host bodies of the wave pass and the
+// per-cell rate): S0 gets the accumulators, the largest rate and its cell.
+double initial_dt(const Host& h, const double* const* W, Stage& S0) {
+    const size_t N = h.N;
+    for (int k = 0; k < 7; ++k) S0.acc[k].assign(N, 0.0);
+    TimeRec tm{};
+    KArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.c = h.c; a.geo = h.G; a.tm = &tm;
+    for (int k = 0; k < 7; ++k) { a.W[k] = W[k]; a.acc[k] = S0.acc[k].data(); }
+    for (int y = 0; y <= h.ny; y += 2) for (int x = 0; x < h.nx; ++x) init_wave_edge<0, true>(a, x, y);
+    for (int y = 1; y <= h.ny; y += 2) for (int x = 0; x < h.nx; ++x) init_wave_edge<0, false>(a, x, y);
+    for (int y = 0; y < h.ny; ++y) for (int x = 0; x <= h.nx; x += 2) init_wave_edge<1, false>(a, x, y);
+    for (int y = 0; y < h.ny; ++y) for (int x = 1; x <= h.nx; x += 2) init_wave_edge<1, false>(a, x, y);
+    for (size_t id = 0; id < N; ++id) {
+        const unsigned long long b = init_cell_rate(a, int(id));
+        if (b > S0.rmax) { S0.rmax = b; S0.argmax = (long long)id; }
+    }
+    return dt_of(S0.rmax, 2.0 * h.c.cfl);
+}
+
+}  // namespace
+
 extern "C" {
+
+// The forward alone: nsteps steps of W (7 arrays, advanced in place to X_N)
+// by the product's per-edge / per-cell bodies in plain loops; dts[0..nsteps]
+// gets each step's dt and the one after the last.
+int adjh_forward(const lsh_params* p, double* const* W, int nsteps, double* dts) {
+    Host h(*p);
+    const size_t N = h.N;
+    Stage S0;
+    dts[0] = initial_dt(h, W, S0);
+    std::vector<Vec> Yv(6);
+    for (int n = 0; n < nsteps; ++n) {
+        Stage S1, S2;
+        if (p->order == 1) {
+            fwd_stage(h, W, W, nullptr, dts[n], 0, S1);
+        } else {
+            double* Y[7];
+            for (int k = 0; k < 6; ++k) { Yv[k].assign(N, 0.0); Y[k] = Yv[k].data(); }
+            Y[6] = W[6];
+            fwd_stage(h, W, Y, nullptr, dts[n], 1, S1);
+            fwd_stage(h, Y, W, W, dts[n], 2, S2);
+        }
+        dts[n + 1] = dt_of(S1.rmax, 2.0 * h.c.cfl);
+    }
+    return 0;
+}
 
 // Misfit J = sum_{n=1..nsteps} sum_g (eta1_n[g] - target)^2 (weight `wj`)
 // plus <wfin, X_N> (wfin: 6 arrays or NULL).  W (7 arrays) is the initial
@@ -143,22 +193,9 @@ int adjh_run(const lsh_params* p, const double* const* W0, int nsteps, int ng, c
     // initial dt: the initial wave pass (on the host bodies)
     Stage S0;
     {
-        for (int k = 0; k < 7; ++k) S0.acc[k].assign(N, 0.0);
-        TimeRec tm{};
-        KArgs a;
-        std::memset(&a, 0, sizeof(a));
-        a.c = h.c; a.geo = h.G; a.tm = &tm;
         const double* Wp[7];
-        for (int k = 0; k < 7; ++k) { Wp[k] = Xs(0, k).data(); a.W[k] = Wp[k]; a.acc[k] = S0.acc[k].data(); }
-        for (int y = 0; y <= h.ny; y += 2) for (int x = 0; x < h.nx; ++x) init_wave_edge<0, true>(a, x, y);
-        for (int y = 1; y <= h.ny; y += 2) for (int x = 0; x < h.nx; ++x) init_wave_edge<0, false>(a, x, y);
-        for (int y = 0; y < h.ny; ++y) for (int x = 0; x <= h.nx; x += 2) init_wave_edge<1, false>(a, x, y);
-        for (int y = 0; y < h.ny; ++y) for (int x = 1; x <= h.nx; x += 2) init_wave_edge<1, false>(a, x, y);
-        for (size_t id = 0; id < N; ++id) {
-            const unsigned long long b = init_cell_rate(a, int(id));
-            if (b > S0.rmax) { S0.rmax = b; S0.argmax = (long long)id; }
-        }
-        dts[0] = dt_of(S0.rmax, 2.0 * h.c.cfl);
+        for (int k = 0; k < 7; ++k) Wp[k] = Xs(0, k).data();
+        dts[0] = initial_dt(h, Wp, S0);
     }
     double Jv = 0.0;
     std::vector<double> eta(size_t(nsteps) * ng);

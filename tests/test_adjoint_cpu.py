@@ -174,3 +174,31 @@ def test_initial_wave_empty_edge_shortcut_is_exact():
     """The kernels skip the initial-dt bound's FP64 work on empty, still edge
     pairs: the general formula gives exactly len * eps_h there."""
     assert native_lib("adj_local").adjl_initial_wave_empty() == 0
+
+
+# ---------------------------------------------------------------- the product's forward on the host
+@pytest.mark.parametrize("kind,order", [("shelf", 1), ("shelf", 2), ("fjord", 2), ("smooth", 1), ("smooth", 2)])
+def test_host_forward_equals_oracle(kind, order):
+    """The product's per-edge / per-cell forward bodies (lsh_passes.cuh,
+    compiled for the host in plain loops) against the oracle: every state
+    field and every step's dt bit-identical.  The CUDA kernels run these
+    bodies too, so this holds the shared device code to the oracle on a
+    machine without a GPU."""
+    import ctypes
+    from adj_cases import _ptrs
+    if kind == "smooth":
+        p, arrs, _ = smooth_case(order=order, spherical=(order == 2))
+    else:
+        p, arrs, _ = scenario_case(kind, order)
+    n = 6
+    lib = native_lib("adj_host")
+    a_host = copy_arrs(arrs)
+    dts = np.zeros(n + 1)
+    assert lib.adjh_forward(ctypes.byref(p), _ptrs(a_host), n, dts.ctypes.data) == 0
+    a_o = copy_arrs(arrs)
+    dt0 = pyoracle.initial_dt(p, a_o)
+    assert dt0 == dts[0]
+    t, dt, _ = pyoracle.run(p, a_o, n, dt=dt0)
+    assert dt == dts[n]
+    for k in range(6):
+        assert np.array_equal(a_host[k], a_o[k]), k
