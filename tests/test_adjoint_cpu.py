@@ -202,3 +202,28 @@ def test_host_forward_equals_oracle(kind, order):
     assert dt == dts[n]
     for k in range(6):
         assert np.array_equal(a_host[k], a_o[k]), k
+
+
+@pytest.mark.parametrize("name", ["dam1d_o2", "column_o2", "cell1x1_o1", "cell1x1_o2", "golden_dam1d", "golden_column",
+                                  "random_o2", "pouliquen_random_o2"])
+def test_host_forward_equals_oracle_edge_cases(name):
+    """The same on the GPU parity suite's degenerate and special cases: one-row
+    and one-column grids, a single cell, random states, the Pouliquen law."""
+    import ctypes
+    from adj_cases import _ptrs
+    from gpu_cases import case
+    from landslidehysea_gb300._abi import VARS
+    p, st, steps = case(name)
+    n = min(steps, 10)
+    arrs = [np.ascontiguousarray(st[v], dtype=np.float64).reshape(-1).copy() for v in VARS]
+    lib = native_lib("adj_host")
+    a_host = copy_arrs(arrs)
+    dts = np.zeros(n + 1)
+    assert lib.adjh_forward(ctypes.byref(p), _ptrs(a_host), n, dts.ctypes.data) == 0
+    a_o = copy_arrs(arrs)
+    dt0 = pyoracle.initial_dt(p, a_o)
+    assert dt0 == dts[0]
+    t, dt, _ = pyoracle.run(p, a_o, n, dt=dt0)
+    assert dt == dts[n]
+    for k in range(6):
+        assert np.array_equal(a_host[k], a_o[k]), (name, k)
