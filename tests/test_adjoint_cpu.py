@@ -227,3 +227,24 @@ def test_host_forward_equals_oracle_edge_cases(name):
     assert dt == dts[n]
     for k in range(6):
         assert np.array_equal(a_host[k], a_o[k]), (name, k)
+
+
+@pytest.mark.parametrize("name", ["golden_dam1d", "dam1d_o2", "golden_column", "column_o2", "cell1x1_o2"])
+def test_host_adjoint_equals_tangent_linear_edge_cases(name):
+    """The host emulation of the adjoint sweep on one-row and one-column grids
+    and a single cell, against the oracle's tangent-linear."""
+    from gpu_cases import case
+    from landslidehysea_gb300._abi import VARS
+    p, st, _ = case(name)
+    arrs = [np.ascontiguousarray(st[v], dtype=np.float64).reshape(-1).copy() for v in VARS]
+    N = arrs[0].size
+    gauges = np.array(sorted({0, N // 2, N - 1}), dtype=np.int32)
+    rng = np.random.default_rng(11)
+    dl = []
+    for which in ((0, 3), (1, 2), (4, 5)):
+        d = [None] * 6
+        for k in which:
+            d[k] = rng.standard_normal(N) * (arrs[0 if k < 3 else 3] > 0)
+        dl.append((d, [0, 0, 0, 0]))
+    dl += [([None] * 6, e) for e in ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1])]
+    _dot_check(p, arrs, gauges, 4, dl, 1e-10)
